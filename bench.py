@@ -1,0 +1,317 @@
+#!/usr/bin/env python
+"""Benchmark of the SAR backprojection (adjoint) operator on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--case config2]
+
+One step = one backprojection x = A^H y of the 2048^2-pixel x 4096-pulse x 4096-sample workload
+(upsample 8, linear interpolation): range-profile upsampling (pack + cuFFT + unpack) followed by
+the tiled gather kernel, with y resident in HBM.  The metric is pixel-pulses per second.
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the reference algorithm on the host
+cores instead: the C restatement in oracle/ (bit-identical to the reference kernel where that
+kernel can be compiled), on a bounded pulse sample of the same workload, all host threads.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "backproj pixel·pulses/s @2048²×4096; CGLS s to 1e-3 resid, learned vs plain"
+UNIT = "px*pulse/s"
+SEED = 20261203
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--case", default="config2")
+    ap.add_argument("--cpu-pulses", type=int, default=96, help="pulse sample of the CPU baseline")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling in the background (200 ms period)."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.proc = None
+        ident = None
+        try:
+            import torch
+            props = torch.cuda.get_device_properties(device_index)
+            bus = getattr(props, "pci_bus_id", None)
+            dom = getattr(props, "pci_domain_id", None)
+            dev = getattr(props, "pci_device_id", None)
+            if bus is not None and dom is not None and dev is not None:
+                ident = f"{dom:08X}:{bus:02X}:{dev:02X}.0"
+        except Exception:
+            pass
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+        if ident:
+            cmd.insert(1, f"--id={ident}")
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[4:8]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        if not sm:
+            return {"samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------- ours
+def run_ours(args):
+    import torch
+    from sarsolver_gb300 import NumpySimpleSarOperator
+    from sarsolver_gb300.scenes import add_noise, config_workload, reflectivity
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    aperture, scene, upsample, desc = config_workload(args.case)
+    S, N, P = aperture.num_slow_times, aperture.num_freqs, scene.num_scatterers
+    n = scene.grid_shape[2]
+    op = NumpySimpleSarOperator(scene, aperture, upsample_ratio=upsample, interp="linear", device=dev)
+    plan = op.plan
+    x_true = reflectivity(n, 500, 8.0, SEED, device=dev)
+    y = add_noise(plan.forward(x_true), 20.0, SEED + 1)
+    x = torch.empty(P, dtype=torch.complex64, device=dev)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # ---- device-resident timing
+    for _ in range(args.warmup):
+        plan.adjoint(y, out=x)
+    barrier()
+    plan.enable_stage_timing(True)
+    sampler = ClockSampler(local)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        plan.adjoint(y, out=x)
+    e1.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    stage_ms, calls = plan.stage_times()
+    plan.enable_stage_timing(False)
+    ms_t = torch.tensor([ms], device=dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    value = world * P * S / (ms * 1e-3)
+
+    # ---- end to end through the public operator API, host buffers (pinned)
+    y_host = y.cpu().pin_memory()
+    x_host = torch.empty(P, dtype=torch.complex64).pin_memory()
+    for _ in range(args.warmup):
+        x_host.copy_(op.adjoint(y_host), non_blocking=True)
+    barrier()
+    e0.record(stream)
+    for _ in range(args.steps):
+        x_host.copy_(op.adjoint(y_host), non_blocking=True)
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    et = torch.tensor([e2e_ms], device=dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(et, op=dist.ReduceOp.MAX)
+    e2e_ms = float(et.item())
+
+    # ---- roofline of the gather kernel (SFU bound: 3 MUFU per pixel-pulse, 16 MUFU/clk/SM)
+    props = torch.cuda.get_device_properties(dev)
+    peaks = measured_peaks()
+    sm_max = float(peaks.get("sm_max_mhz", 0.0)) or float((clocks or {}).get("sm_max_mhz", 0.0)) or 2070.0
+    r_roof = props.multi_processor_count * sm_max * 1e6 * 16.0 / 3.0
+    k2_ms = stage_ms[1] / max(calls, 1)
+    fft_ms = stage_ms[0] / max(calls, 1)
+    achieved = P * S / (k2_ms * 1e-3)
+    traffic = read_profile_traffic("bp_grid")
+    result = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64 (fp32 arithmetic; double-float fp32 pairs for range/phase)",
+        "data": "synthetic, seeded: 500 point scatterers + Gaussian-filtered (sigma 8 px) clutter x complex "
+                "speckle, forward-projected by this operator, complex white noise at 20 dB SNR",
+        "config": {"workload": f"{args.case}: backprojection, {desc}, linear interpolation",
+                   "pixels": P, "pulses": S, "samples": N, "upsample": upsample,
+                   "l2": "inputs larger than L2 (phase history %.0f MB, stored range profiles %.0f MB)"
+                         % (S * N * 8 / 1e6, S * plan.profile_length * 16 / 1e6),
+                   "parallelism": "replicas (each GPU runs the whole workload)" if world > 1 else "single GPU"},
+        "stages_ms": {"upsample_fft_side": fft_ms, "gather_kernel": k2_ms},
+        "roofline": {"bound": "sfu", "kernel": "bp_grid_kernel", "achieved": achieved, "peak": r_roof,
+                     "unit": "px*pulse/s", "frac": achieved / r_roof, "traffic": traffic,
+                     "peak_basis": f"{props.multi_processor_count} SMs x {sm_max:.0f} MHz x 16 MUFU/clk/SM / "
+                                   "3 MUFU per px*pulse (sm_max_mhz of MEASURED_PEAKS.json)"},
+        "e2e": {"value": world * P * S / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": S * N * 8, "d2h_bytes_per_step": P * 8,
+                "api": "NumpySimpleSarOperator.adjoint(pinned host complex64 tensor) -> pinned host copy"},
+        # our kernels per call: pack + unpack per FFT chunk, then the gather (cuFFT's own excluded)
+        "gpu_launches": args.steps * (2 * ((S + plan_chunk(plan) - 1) // plan_chunk(plan)) + 1),
+        "clocks": clocks,
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(aperture, scene, upsample, y, args.cpu_pulses, steps=1)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(result))
+
+
+def plan_chunk(plan) -> int:
+    # one FFT chunk covers all pulses for every configuration here (4 GiB of rows)
+    return plan.num_slow_times
+
+
+def read_profile_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if one exists."""
+    path = os.path.join(HERE, "profiles", f"{kernel}_config2.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+# -------------------------------------------------------------- CPU legs
+def cpu_baseline(aperture, scene, upsample, y, pulses, steps=1):
+    """Time the oracle port (FP64 C restatement, all host threads) on a pulse sample."""
+    import oracle
+
+    oracle.build()
+    threads = oracle.default_threads()
+    S = aperture.num_slow_times
+    sel = np.linspace(0, S - 1, pulses).round().astype(int)
+    y_np = y.cpu().numpy()[sel] if hasattr(y, "cpu") else np.asarray(y)[sel]
+    prob = oracle.Problem(aperture.transmitter_positions[sel], aperture.receiver_positions[sel],
+                          aperture.stab_ref_posns[sel], scene.positions, aperture.centre_frequency,
+                          aperture.sample_bandwidth, aperture.num_freqs, upsample_ratio=upsample)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        oracle.adjoint(prob, y_np, "linear", threads=threads)
+    dt = (time.perf_counter() - t0) / steps
+    units = scene.num_scatterers * pulses
+    return {"value": units / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"full {scene.num_scatterers}-pixel image x {pulses} of {S} pulses "
+                      f"({units:.3g} px*pulses), FP64, linear interpolation, {dt:.2f} s per sample"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    import oracle
+    from sarsolver_gb300.scenes import config_workload
+
+    oracle.build()
+    aperture, scene, upsample, desc = config_workload(args.case)
+    S, N, P = aperture.num_slow_times, aperture.num_freqs, scene.num_scatterers
+    pulses = max(1, args.cpu_pulses // 2)
+    threads = oracle.default_threads()
+    rng = np.random.default_rng(SEED)
+    sel = np.linspace(0, S - 1, pulses).round().astype(int)
+    y = (rng.standard_normal((pulses, N)) + 1j * rng.standard_normal((pulses, N))) / np.sqrt(2.0)
+    prob = oracle.Problem(aperture.transmitter_positions[sel], aperture.receiver_positions[sel],
+                          aperture.stab_ref_posns[sel], scene.positions, aperture.centre_frequency,
+                          aperture.sample_bandwidth, N, upsample_ratio=upsample)
+    for _ in range(args.warmup):
+        oracle.adjoint(prob, y, "linear", threads=threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.adjoint(prob, y, "linear", threads=threads)
+    dt = (time.perf_counter() - t0) / args.steps
+    value = P * pulses / dt
+    sample = (f"full {P}-pixel image x {pulses} of {S} pulses per step ({P * pulses:.3g} px*pulses), "
+              "FP64, linear interpolation")
+    print(json.dumps({
+        "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128 (fp64)", "data": "synthetic, seeded",
+        "config": {"workload": f"{args.case}: backprojection, {desc}, linear interpolation (CPU pulse sample)"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,146 @@
+/*
+ * sargpu.h -- C ABI of the GB300 SAR operator library (libsargpu.so).
+ *
+ * Replaces the native boundary of sarsolver's C++/FFTW kernel:
+ *   src/sarsolver/cxx_binding/sarsolver_cxx.hpp:112-119  forward_evaluate / adjoint_evaluate
+ *   src/sarsolver/cxx_binding/sarsolver_cxx.hpp:28-33    SarCalculationInfo
+ *   src/sarsolver/cxx_binding/sarsolver_cxx.py:214-220   their ctypes bindings
+ *
+ * Two layers:
+ *  1. Drop-in entry points with the reference's exact signatures and struct layout
+ *     (forward_evaluate / adjoint_evaluate on SarCalculationInfo*, host FP64 buffers,
+ *     FFT-ordered phase history), computed on the current CUDA device.
+ *  2. A plan API on device buffers: geometry is uploaded once, then sar_forward /
+ *     sar_adjoint run asynchronously on a caller-provided CUDA stream.
+ *
+ * Plain C types only; a CUDA stream is passed as `void *` (a cudaStream_t).  Every plan
+ * call returns a status (SAR_OK == 0) and never aborts; sar_last_error() gives the
+ * calling thread's last message.
+ *
+ * Data layout of the plan API (device memory, complex64 = interleaved float re, im):
+ *   image x:          [P]      with P = nz*ny*nx for a grid, index (k*ny + j)*nx + i,
+ *                              matching GridSarScene.positions (src/sarsolver/numpy/hypothesis.py:192-206)
+ *   phase history y:  [S][N]   fast time fftshifted (centre frequency in the middle), the
+ *                              convention of the reference's Python API (cxx_binding/forward.py:44,
+ *                              adjoint.py:36)
+ */
+#ifndef SARGPU_H
+#define SARGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status codes */
+#define SAR_OK 0
+#define SAR_ERR_INVALID_ARGUMENT 1
+#define SAR_ERR_CUDA 2
+#define SAR_ERR_CUFFT 3
+#define SAR_ERR_OUT_OF_MEMORY 4
+#define SAR_ERR_NOT_SUPPORTED 5
+
+/* Interpolation of the upsampled range profile. */
+#define SAR_INTERP_NEAREST_REF 0 /* the reference's bins: round(v) forward (sarsolver_cxx.cpp:289),
+                                    round(0.5+v) adjoint (:347), weight unconjugated (:288, :349) */
+#define SAR_INTERP_LINEAR 1      /* linear interpolation; forward and adjoint exact transposes */
+
+/* Device check flags reported by sar_device_flags(). */
+#define SAR_FLAG_TILE_WINDOW 1u
+#define SAR_FLAG_STRIP_WINDOW 2u
+
+/* ------------------------------------------------------------ 1. drop-in boundary */
+
+/* Byte-for-byte the reference struct (sarsolver_cxx.hpp:28-33). */
+typedef struct SarCalculationInfo {
+    size_t num_fast_times, num_slow_times, num_scatterers;
+    double *transmit_posns, *receive_posns, *stab_ref_posns, *scat_posns;
+    double *phase_history, *scattering_amplitudes, *waveform_fft, *slow_time_weighting;
+    double centre_frequency, sample_frequency, c_eff, upsample_ratio, sign_multiplier;
+} SarCalculationInfo;
+
+/* Replaces forward_evaluate (sarsolver_cxx.hpp:113, sarsolver_cxx.cpp:26-30): writes
+ * info->phase_history [S][N][2] (FFT order) from info->scattering_amplitudes.  Reference
+ * conventions (SAR_INTERP_NEAREST_REF).  Like the reference it returns nothing; on failure the
+ * output is zero-filled and sar_last_error() holds the reason. */
+void forward_evaluate(SarCalculationInfo *info);
+
+/* Replaces adjoint_evaluate (sarsolver_cxx.hpp:114, sarsolver_cxx.cpp:32-36): writes
+ * info->scattering_amplitudes [P][2] from info->phase_history (FFT order). */
+void adjoint_evaluate(SarCalculationInfo *info);
+
+/* ----------------------------------------------------------------- 2. plan API */
+
+typedef struct sar_plan sar_plan;
+
+/* Geometry of one operator.  Host FP64 inputs, copied at plan creation.  Replaces the
+ * per-call SarCalculationInfo + SarWorker construction (sarsolver_cxx.cpp:219-252). */
+typedef struct sar_geometry {
+    size_t num_fast_times;              /* N */
+    size_t num_slow_times;              /* S */
+    size_t num_scatterers;              /* P (must equal nz*ny*nx when a grid is given) */
+    const double *transmit_posns;       /* [S][3] */
+    const double *receive_posns;        /* [S][3] */
+    const double *stab_ref_posns;       /* [S][3] */
+    const double *scat_posns;           /* [P][3]; used when grid_shape is all zero */
+    const double *waveform_fft;         /* [N][2] FFT order; NULL = all ones */
+    const double *slow_time_weighting;  /* [S][2]; NULL = all ones */
+    double centre_frequency, sample_frequency, c_eff, upsample_ratio, sign_multiplier;
+    int interp;                         /* SAR_INTERP_* */
+    /* Regular grid (fast path): pixel (k, j, i) sits at
+     *   grid_origin + i*grid_step_x + j*grid_step_y + k*grid_step_z,
+     * grid_shape = {nz, ny, nx}.  All-zero grid_shape selects the unstructured path. */
+    size_t grid_shape[3];
+    double grid_origin[3], grid_step_x[3], grid_step_y[3], grid_step_z[3];
+} sar_geometry;
+
+typedef struct sar_plan_info {
+    size_t working_length;      /* M = (size_t)(upsample_ratio * N), sarsolver_cxx.cpp:223 */
+    long profile_first_bin;     /* first stored range bin (may be negative) */
+    size_t profile_length;      /* stored bins per pulse */
+    size_t tile_window;         /* staged bins per (tile, pulse); 0 on the unstructured path */
+    size_t strip_window;        /* forward strip window (bins); 0 on the unstructured path */
+    size_t device_bytes;        /* device memory held by the plan */
+    int grid;                   /* 1 regular-grid path, 0 unstructured path */
+} sar_plan_info;
+
+/* Create a plan on `device` (-1: the current device).  Copies all host inputs. */
+int sar_plan_create(const sar_geometry *geom, int device, sar_plan **plan_out);
+int sar_plan_destroy(sar_plan *plan);
+int sar_plan_get_info(const sar_plan *plan, sar_plan_info *info);
+
+/* y[S][N] = A x[P].  Device complex64 buffers; asynchronous on `stream`. */
+int sar_forward(sar_plan *plan, const void *x_dev, void *y_dev, void *stream);
+/* x[P] = A^H y[S][N].  Device complex64 buffers; asynchronous on `stream`. */
+int sar_adjoint(sar_plan *plan, const void *y_dev, void *x_dev, void *stream);
+/* Upsampled range profiles over the stored span, prof[S][profile_length] complex64,
+ * bin profile_first_bin + w at column w, no slow-time weight (test and inspection aid). */
+int sar_profiles(sar_plan *plan, const void *y_dev, void *prof_dev, void *stream);
+
+/* Replace the slow-time weighting (e.g. autofocus phase corrections). */
+int sar_set_slow_time_weighting(sar_plan *plan, const double *w_host /* [S][2] */);
+int sar_set_slow_time_weighting_device(sar_plan *plan, const void *w_dev /* complex64 [S] */,
+                                       void *stream);
+
+/* Stage timing.  While enabled, every sar_forward / sar_adjoint call records CUDA events on
+ * its stream around its stages: [0] range-profile FFT side before the main kernel (adjoint:
+ * pack + inverse FFT + unpack; forward: accumulator clear), [1] the main gather / scatter
+ * kernel, [2] FFT side after it (forward: pack + FFT + extract).  sar_stage_times synchronises
+ * and returns the summed milliseconds per stage over the calls recorded since the last reset
+ * (at most 4096 calls are kept) and their count; enabling resets the record. */
+int sar_enable_stage_timing(sar_plan *plan, int enable);
+int sar_stage_times(sar_plan *plan, float *ms /* [3] */, int *calls);
+
+/* Synchronise the plan's last stream, return and clear the device check flags. */
+int sar_device_flags(sar_plan *plan, unsigned *flags);
+
+/* Last error message of the calling thread (empty if none); returns its full length. */
+size_t sar_last_error(char *buf, size_t len);
+const char *sar_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SARGPU_H */

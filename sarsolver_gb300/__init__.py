@@ -1,0 +1,17 @@
+"""sarsolver_gb300 -- GB300 (sm_103a) implementation of sarsolver's SAR operator pair.
+
+Public API (drop-in names of the reference where one exists):
+  NumpySimpleSarOperator / GpuSarOperator   scipy LinearOperator (src/sarsolver/numpy/operator.py)
+  GpuCilSarOperator / CpuSarOperator        CIL LinearOperator (src/sarsolver/cil/operator.py)
+  GridSarScene, SimpleSarScene, NumpySimpleSarAperture, NumpySimpleSarDataset
+  SarPlan                                   device-tensor plan under both
+  cxx_binding                               single_/multi_{forward,adjoint}_evaluate
+"""
+from .geometry import GridSarScene, NumpySimpleSarAperture, NumpySimpleSarDataset, SimpleSarScene, grid_axes
+from .plan import SarPlan
+from .operator import GpuSarOperator, NumpySimpleSarOperator
+
+__all__ = [
+    "GridSarScene", "SimpleSarScene", "NumpySimpleSarAperture", "NumpySimpleSarDataset", "grid_axes",
+    "SarPlan", "NumpySimpleSarOperator", "GpuSarOperator",
+]

@@ -1,0 +1,146 @@
+"""ctypes binding of libsargpu.so (C ABI declared in include/sargpu.h).
+
+The library is built in-tree by ``sarsolver_gb300.build``; there is no fallback: if it is
+missing, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_char_p, c_double, c_int, c_size_t, c_uint, c_void_p, c_long
+
+from .build import GPU_LIB, HOST_LIB
+
+SAR_OK = 0
+SAR_ERR_INVALID_ARGUMENT = 1
+SAR_ERR_CUDA = 2
+SAR_ERR_CUFFT = 3
+SAR_ERR_OUT_OF_MEMORY = 4
+SAR_ERR_NOT_SUPPORTED = 5
+
+INTERP = {"nearest_ref": 0, "linear": 1}
+
+#: Every function include/sargpu.h declares.
+EXPORTED = (
+    "forward_evaluate", "adjoint_evaluate",
+    "sar_plan_create", "sar_plan_destroy", "sar_plan_get_info",
+    "sar_forward", "sar_adjoint", "sar_profiles",
+    "sar_set_slow_time_weighting", "sar_set_slow_time_weighting_device",
+    "sar_device_flags", "sar_last_error", "sar_status_string",
+    "sar_enable_stage_timing", "sar_stage_times",
+)
+
+
+class SarGeometry(ctypes.Structure):
+    """Mirror of ``sar_geometry`` (include/sargpu.h)."""
+
+    _fields_ = [
+        ("num_fast_times", c_size_t), ("num_slow_times", c_size_t), ("num_scatterers", c_size_t),
+        ("transmit_posns", c_void_p), ("receive_posns", c_void_p), ("stab_ref_posns", c_void_p),
+        ("scat_posns", c_void_p), ("waveform_fft", c_void_p), ("slow_time_weighting", c_void_p),
+        ("centre_frequency", c_double), ("sample_frequency", c_double), ("c_eff", c_double),
+        ("upsample_ratio", c_double), ("sign_multiplier", c_double),
+        ("interp", c_int),
+        ("grid_shape", c_size_t * 3), ("grid_origin", c_double * 3), ("grid_step_x", c_double * 3),
+        ("grid_step_y", c_double * 3), ("grid_step_z", c_double * 3),
+    ]
+
+
+class SarPlanInfo(ctypes.Structure):
+    """Mirror of ``sar_plan_info``."""
+
+    _fields_ = [
+        ("working_length", c_size_t), ("profile_first_bin", c_long), ("profile_length", c_size_t),
+        ("tile_window", c_size_t), ("strip_window", c_size_t), ("device_bytes", c_size_t), ("grid", c_int),
+    ]
+
+
+class SarCalculationInfo(ctypes.Structure):
+    """Byte-for-byte the reference struct (src/sarsolver/cxx_binding/sarsolver_cxx.hpp:28-33,
+    mirrored in Python at src/sarsolver/cxx_binding/sarsolver_cxx.py:49-62)."""
+
+    _fields_ = [("num_fast_times", c_size_t), ("num_slow_times", c_size_t), ("num_scatterers", c_size_t),
+                ("transmit_posns", POINTER(c_double)), ("receive_posns", POINTER(c_double)),
+                ("stab_ref_posns", POINTER(c_double)), ("scat_posns", POINTER(c_double)),
+                ("phase_history", POINTER(c_double)), ("scattering_amplitudes", POINTER(c_double)),
+                ("waveform_fft", POINTER(c_double)), ("slow_time_weighting", POINTER(c_double)),
+                ("centre_frequency", c_double), ("sample_frequency", c_double), ("c_eff", c_double),
+                ("upsample_ratio", c_double), ("sign_multiplier", c_double)]
+
+
+_LIB = None
+
+
+def library_path() -> str:
+    return GPU_LIB
+
+
+def load() -> ctypes.CDLL:
+    """Load libsargpu.so; raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(GPU_LIB):
+        raise RuntimeError(f"libsargpu.so is not built ({GPU_LIB}); run sarsolver_gb300.build.build()")
+    lib = ctypes.CDLL(GPU_LIB)
+    lib.sar_plan_create.argtypes = [POINTER(SarGeometry), c_int, POINTER(c_void_p)]
+    lib.sar_plan_destroy.argtypes = [c_void_p]
+    lib.sar_plan_get_info.argtypes = [c_void_p, POINTER(SarPlanInfo)]
+    for name in ("sar_forward", "sar_adjoint", "sar_profiles"):
+        getattr(lib, name).argtypes = [c_void_p, c_void_p, c_void_p, c_void_p]
+    lib.sar_set_slow_time_weighting.argtypes = [c_void_p, c_void_p]
+    lib.sar_set_slow_time_weighting_device.argtypes = [c_void_p, c_void_p, c_void_p]
+    lib.sar_device_flags.argtypes = [c_void_p, POINTER(c_uint)]
+    lib.sar_enable_stage_timing.argtypes = [c_void_p, c_int]
+    lib.sar_stage_times.argtypes = [c_void_p, POINTER(ctypes.c_float), POINTER(c_int)]
+    for name in ("sar_plan_create", "sar_plan_destroy", "sar_plan_get_info", "sar_forward", "sar_adjoint",
+                 "sar_profiles", "sar_set_slow_time_weighting", "sar_set_slow_time_weighting_device",
+                 "sar_device_flags", "sar_enable_stage_timing", "sar_stage_times"):
+        getattr(lib, name).restype = c_int
+    lib.sar_last_error.argtypes = [c_char_p, c_size_t]
+    lib.sar_last_error.restype = c_size_t
+    lib.sar_status_string.argtypes = [c_int]
+    lib.sar_status_string.restype = c_char_p
+    for name in ("forward_evaluate", "adjoint_evaluate"):
+        getattr(lib, name).argtypes = [POINTER(SarCalculationInfo)]
+        getattr(lib, name).restype = None
+    _LIB = lib
+    return lib
+
+
+def last_error() -> str:
+    lib = load()
+    buf = ctypes.create_string_buffer(1024)
+    lib.sar_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+class SarError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{message} (status {status})")
+        self.status = status
+
+
+def check(status: int, what: str) -> None:
+    if status != SAR_OK:
+        lib = load()
+        raise SarError(status, f"{what}: {lib.sar_status_string(status).decode()}: {last_error()}")
+
+
+_HOST = None
+
+
+def load_host() -> ctypes.CDLL:
+    """Host build of the kernels' range geometry (precision checks on machines without a GPU)."""
+    global _HOST
+    if _HOST is None:
+        if not os.path.exists(HOST_LIB):
+            raise RuntimeError(f"{HOST_LIB} is not built; run sarsolver_gb300.build.build()")
+        lib = ctypes.CDLL(HOST_LIB)
+        P = c_void_p
+        lib.sar_geom_host_eval.argtypes = [P, P, P, P, c_int, c_int, c_int, c_size_t, P, P, P, c_double, c_double,
+                                           ctypes.c_float, P, P]
+        lib.sar_geom_host_eval_points.argtypes = [P, c_size_t, P, c_size_t, P, P, P, c_double, c_double,
+                                                  ctypes.c_float, P, P]
+        _HOST = lib
+    return _HOST

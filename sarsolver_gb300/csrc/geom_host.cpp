@@ -1,0 +1,95 @@
+// geom_host.cpp -- host build of the kernels' range geometry (sar_geom.cuh).
+//
+// Evaluates, with exactly the tiling and arithmetic the GPU kernels use (32x32 tiles, four
+// 16x16 sub-tiles, per-(sub-tile, pulse) cubic expansion, per-column/per-pixel FP32
+// evaluation), the phase (cycles, reduced to [-0.5, 0.5]) and the bin position of every
+// grid pixel for every pulse.  Tests compare these with FP64 ranges to bound the error of
+// the fast path without a GPU.
+#include <math.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "sar_geom.cuh"
+#include "sar_host_prep.h"
+
+using namespace sar;
+
+extern "C" int sar_geom_host_eval(const double* origin, const double* ex, const double* ey,
+                                  const double* ez, int nx, int ny, int nz, size_t num_pulses,
+                                  const double* tx, const double* rx, const double* srp,
+                                  double kappa, double s_r, float bin_offset, float* phase_out,
+                                  double* bin_out) {
+    if (nx <= 0 || ny <= 0 || nz <= 0) return 1;
+    GridConst g = make_grid_const(ex, ey, ez, kappa, s_r, bin_offset, nx, ny, nz);
+    const size_t P = (size_t)nx * ny * nz;
+    for (size_t s = 0; s < num_pulses; ++s) {
+        PulseGeom pg = make_pulse_geom(tx + 3 * s, rx + 3 * s, srp + 3 * s, origin);
+        for (int k = 0; k < nz; ++k)
+            for (int tj = 0; tj < g.tiles_y; ++tj)
+                for (int ti = 0; ti < g.tiles_x; ++ti) {
+                    Coeffs co[4];
+                    AnchorExpansion ae[4];
+                    df vb[4];
+                    df vsum = df_make(0.0f, 0.0f);
+                    for (int q = 0; q < 4; ++q) {
+                        int ai = ti * 32 + 8 + 16 * (q & 1);
+                        int aj = tj * 32 + 8 + 16 * (q >> 1);
+                        df3 anchor = pixel_position(ai, aj, k, g);
+                        ae[q] = expand_anchor(anchor, pg, g);
+                        phase_coeffs(ae[q], g, co[q].c);
+                        vb[q] = anchor_bin(ae[q], g);
+                        vsum = df_add(vsum, vb[q]);
+                    }
+                    int base = base_bin_of(vsum, 4.0f);
+                    for (int q = 0; q < 4; ++q) bin_coeffs(ae[q], vb[q], base, g, co[q].v);
+                    for (int lj = 0; lj < 32; ++lj)
+                        for (int li = 0; li < 32; ++li) {
+                            int i = ti * 32 + li, j = tj * 32 + lj;
+                            if (i >= nx || j >= ny) continue;
+                            int q = (li >= 16) + 2 * (lj >= 16);
+                            float di = (float)(li - 8 - 16 * (q & 1));
+                            float dj = (float)(lj - 8 - 16 * (q >> 1));
+                            ColumnTerms ct = column_terms(co[q], di, di * di, di * di * di);
+                            float ph = pixel_phase(ct, co[q].c[9], dj, dj * dj, dj * dj * dj);
+                            float v = pixel_bin(ct, co[q].v[5], dj, dj * dj);
+                            size_t p = ((size_t)k * ny + j) * nx + i;
+                            phase_out[s * P + p] = ph - round_shift(ph);
+                            bin_out[s * P + p] = (double)base + (double)v;
+                        }
+                }
+    }
+    return 0;
+}
+
+// Unstructured-position scheme: phase (cycles, [-0.5, 0.5]) and bin position per point.
+extern "C" int sar_geom_host_eval_points(const double* origin, size_t num_points, const double* pos,
+                                         size_t num_pulses, const double* tx, const double* rx,
+                                         const double* srp, double kappa, double s_r,
+                                         float bin_offset, float* phase_out, double* bin_out) {
+    df kap = to_df(kappa), sr = to_df(s_r);
+    for (size_t s = 0; s < num_pulses; ++s) {
+        PulseGeom pg = make_pulse_geom(tx + 3 * s, rx + 3 * s, srp + 3 * s, origin);
+        df3 at = pulse_tx(pg), ar = pulse_rx(pg);
+        df at2 = df_dot3(at, at), ar2 = df_dot3(ar, ar);
+        for (size_t p = 0; p < num_points; ++p) {
+            PointGeom pt;
+            double q[3] = {pos[3 * p] - origin[0], pos[3 * p + 1] - origin[1], pos[3 * p + 2] - origin[2]};
+            double qq = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+            for (int c = 0; c < 3; ++c) {
+                df d = to_df(q[c]);
+                pt.qh[c] = d.hi;
+                pt.ql[c] = d.lo;
+            }
+            df d2 = to_df(qq);
+            pt.qh[3] = d2.hi;
+            pt.ql[3] = d2.lo;
+            df r = point_range(at, at2, pt);
+            r = df_add(r, pg.monostatic != 0.0f ? r : point_range(ar, ar2, pt));
+            r = df_sub(r, df_make(pg.rref_hi, pg.rref_lo));
+            phase_out[s * num_points + p] = df_frac(df_mul(kap, r));
+            df v = df_mul(sr, r);
+            bin_out[s * num_points + p] = (double)v.hi + (double)v.lo + (double)bin_offset;
+        }
+    }
+    return 0;
+}

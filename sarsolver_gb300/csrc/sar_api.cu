@@ -1,0 +1,797 @@
+// sar_api.cu -- plan objects and the C ABI of libsargpu.so (see include/sargpu.h).
+//
+// A plan holds everything the reference rebuilds per call in SarWorker's constructor
+// (src/sarsolver/cxx_binding/sarsolver_cxx.cpp:219-252): the working length M, the bin rate
+// s_r and wavenumber, the waveform and slow-time weights, FFT plans, plus the GPU-side
+// geometry tables (double-float antenna positions relative to the scene origin) and the range
+// spans that size the stored profiles and the shared-memory windows.
+#include <cuda_runtime.h>
+#include <cufft.h>
+
+#include <algorithm>
+#include <array>
+#include <complex>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/sargpu.h"
+#include "sar_host_prep.h"
+#include "sar_kernels.cuh"
+
+using namespace sar;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    if (e == cudaErrorMemoryAllocation)
+        return fail(SAR_ERR_OUT_OF_MEMORY, "%s: %s", what, cudaGetErrorString(e));
+    return fail(SAR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define SAR_CUDA(call, what)                                  \
+    do {                                                      \
+        cudaError_t _e = (call);                              \
+        if (_e != cudaSuccess) return cuda_fail(_e, (what));  \
+    } while (0)
+
+#define SAR_CUFFT(call, what)                                                        \
+    do {                                                                             \
+        cufftResult _r = (call);                                                     \
+        if (_r != CUFFT_SUCCESS) return fail(SAR_ERR_CUFFT, "%s: cufft error %d", (what), (int)_r); \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    int target = -1;
+    cudaError_t status = cudaSuccess;
+    explicit DeviceGuard(int dev) : target(dev) {
+        status = cudaGetDevice(&prev);
+        if (status == cudaSuccess && dev >= 0 && dev != prev) status = cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        if (prev >= 0 && target >= 0 && target != prev) cudaSetDevice(prev);
+    }
+};
+
+bool finite3(const double* v, size_t n) {
+    for (size_t i = 0; i < 3 * n; ++i)
+        if (!std::isfinite(v[i])) return false;
+    return true;
+}
+
+// Shared-memory budgets: two tile CTAs per SM.
+constexpr size_t kBpSmemBudget = 110 * 1024;
+constexpr size_t kFpSmemBudget = 100 * 1024;
+constexpr size_t kSpecBudget = (size_t)4 << 30;   // bytes of FFT work rows per chunk
+
+}  // namespace
+
+struct sar_plan {
+    int device = 0;
+    size_t N = 0, S = 0, P = 0, M = 0;
+    int interp = SAR_INTERP_NEAREST_REF;
+    bool grid = false;
+    bool forward_points = false;   // grid forward through the unstructured kernels
+    GridConst gc_adj{}, gc_fwd{};
+    df kappa{}, s_r{};
+    long bg0 = 0;
+    int Lg = 0;
+    int wwin = 0, pb = 32;
+    bool staged = true;
+    int seg_tiles = 0, segs_per_column = 0, ws = 0, pbf = 16;
+    size_t n_strips = 0;
+    int chunk = 0;
+    std::vector<std::complex<double>> weights;
+
+    PulseGeom* d_pulses = nullptr;
+    float4* d_alpha2 = nullptr;
+    PointGeom* d_points = nullptr;
+    float2* d_wave = nullptr;
+    float2* d_w = nullptr;
+    float2* d_wadj = nullptr;
+    float2* d_wfwd = nullptr;
+    float2* d_spec = nullptr;
+    float4* d_prof = nullptr;   // [S][Lg] pairs (adjoint) / float2 accumulator (forward)
+    int* d_strip = nullptr;
+    unsigned* d_flags = nullptr;
+    size_t device_bytes = 0;
+    cufftHandle fft_full = 0, fft_tail = 0;
+    bool have_full = false, have_tail = false;
+    cudaStream_t last_stream = nullptr;
+    std::mutex mu;
+    // stage timing: 4 events per recorded call (start, pre-kernel done, kernel done, end)
+    bool timing = false;
+    std::vector<std::array<cudaEvent_t, 4>> events;
+    size_t events_used = 0;
+
+    // Next event slot of a timed call, or nullptr when timing is off or the record is full.
+    cudaEvent_t* timing_slot() {
+        if (!timing || events_used >= 4096) return nullptr;
+        if (events_used == events.size()) {
+            std::array<cudaEvent_t, 4> ev{};
+            for (auto& e : ev)
+                if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+            events.push_back(ev);
+        }
+        return events[events_used++].data();
+    }
+
+    template <class T>
+    int alloc(T** p, size_t count, const char* what) {
+        cudaError_t e = cudaMalloc((void**)p, sizeof(T) * std::max<size_t>(count, 1));
+        if (e != cudaSuccess) return cuda_fail(e, what);
+        device_bytes += sizeof(T) * std::max<size_t>(count, 1);
+        return SAR_OK;
+    }
+
+    ~sar_plan() {
+        DeviceGuard g(device);
+        cudaFree(d_pulses);
+        cudaFree(d_alpha2);
+        cudaFree(d_points);
+        cudaFree(d_wave);
+        cudaFree(d_w);
+        cudaFree(d_wadj);
+        cudaFree(d_wfwd);
+        cudaFree(d_spec);
+        cudaFree(d_prof);
+        cudaFree(d_strip);
+        cudaFree(d_flags);
+        if (have_full) cufftDestroy(fft_full);
+        if (have_tail) cufftDestroy(fft_tail);
+        for (auto& ev : events)
+            for (auto e : ev) cudaEventDestroy(e);
+    }
+};
+
+static inline void mark(cudaEvent_t* ev, int i, cudaStream_t st) {
+    if (ev) cudaEventRecord(ev[i], st);
+}
+
+namespace {
+
+float adjoint_bin_offset(int interp) { return interp == SAR_INTERP_LINEAR ? -0.5f : 0.5f; }
+float forward_bin_offset(int interp) { return interp == SAR_INTERP_LINEAR ? -0.5f : 0.0f; }
+
+// Bistatic differential range span [lo, hi] of a box region for pulse s.
+void region_range(const double* tx, const double* rx, const double* srp, const double* o,
+                  const double* ex, const double* ey, const double* ez, double nu, double nv,
+                  double nw, double* lo, double* hi) {
+    double a0, a1, b0, b1;
+    box_distance_bounds(tx, o, ex, ey, ez, nu, nv, nw, &a0, &a1);
+    box_distance_bounds(rx, o, ex, ey, ez, nu, nv, nw, &b0, &b1);
+    const double ref = dist3(tx, srp) + dist3(rx, srp);
+    *lo = a0 + b0 - ref;
+    *hi = a1 + b1 - ref;
+}
+
+int upload_weights(sar_plan* p, cudaStream_t st, bool sync) {
+    std::vector<float2> w(p->S);
+    for (size_t s = 0; s < p->S; ++s) w[s] = make_float2((float)p->weights[s].real(), (float)p->weights[s].imag());
+    SAR_CUDA(cudaMemcpyAsync(p->d_w, w.data(), sizeof(float2) * p->S, cudaMemcpyHostToDevice, st), "upload weights");
+    SAR_CUDA(launch_weights(p->d_w, p->d_wadj, p->d_wfwd, (int)p->S, p->interp == SAR_INTERP_LINEAR, st),
+             "weights kernel");
+    if (sync) SAR_CUDA(cudaStreamSynchronize(st), "upload weights");
+    return SAR_OK;
+}
+
+int make_fft(cufftHandle* h, long M, int batch) {
+    int n[1] = {(int)M};
+    SAR_CUFFT(cufftPlanMany(h, 1, n, nullptr, 1, (int)M, nullptr, 1, (int)M, CUFFT_C2C, batch), "cufftPlanMany");
+    return SAR_OK;
+}
+
+int run_fft(sar_plan* p, float2* data, int rows, int direction, cudaStream_t st) {
+    cufftHandle h = (rows == p->chunk) ? p->fft_full : p->fft_tail;
+    SAR_CUFFT(cufftSetStream(h, st), "cufftSetStream");
+    SAR_CUFFT(cufftExecC2C(h, reinterpret_cast<cufftComplex*>(data), reinterpret_cast<cufftComplex*>(data), direction),
+              "cufftExecC2C");
+    return SAR_OK;
+}
+
+// Host-only validation of a geometry description (no CUDA call).
+int validate_geometry(const sar_geometry* g) {
+    const size_t N = g->num_fast_times, S = g->num_slow_times, P = g->num_scatterers;
+    if (N == 0 || S == 0 || P == 0) return fail(SAR_ERR_INVALID_ARGUMENT, "empty problem: N=%zu S=%zu P=%zu", N, S, P);
+    if (!g->transmit_posns || !g->receive_posns || !g->stab_ref_posns)
+        return fail(SAR_ERR_INVALID_ARGUMENT, "antenna / SRP positions are required");
+    if (!(g->c_eff > 0.0) || !(g->sample_frequency > 0.0) || !(g->upsample_ratio > 0.0) ||
+        !std::isfinite(g->centre_frequency) || !std::isfinite(g->sign_multiplier))
+        return fail(SAR_ERR_INVALID_ARGUMENT, "c_eff, sample_frequency and upsample_ratio must be positive");
+    if (g->interp != SAR_INTERP_NEAREST_REF && g->interp != SAR_INTERP_LINEAR)
+        return fail(SAR_ERR_INVALID_ARGUMENT, "unknown interpolation mode %d", g->interp);
+    const size_t M = (size_t)(g->upsample_ratio * (double)N);   // sarsolver_cxx.cpp:223
+    if (M < N) return fail(SAR_ERR_INVALID_ARGUMENT, "upsample_ratio*N (%zu) is below N (%zu)", M, N);
+    if (M > (size_t)1 << 30 || S > (size_t)1 << 30 || N > (size_t)1 << 30)
+        return fail(SAR_ERR_NOT_SUPPORTED, "sizes beyond 2^30 are not supported");
+    if (!finite3(g->transmit_posns, S) || !finite3(g->receive_posns, S) || !finite3(g->stab_ref_posns, S))
+        return fail(SAR_ERR_INVALID_ARGUMENT, "non-finite antenna or SRP position");
+    const bool grid = g->grid_shape[0] || g->grid_shape[1] || g->grid_shape[2];
+    if (grid) {
+        if (!g->grid_shape[0] || !g->grid_shape[1] || !g->grid_shape[2])
+            return fail(SAR_ERR_INVALID_ARGUMENT, "grid_shape must be all positive or all zero");
+        if (g->grid_shape[0] * g->grid_shape[1] * g->grid_shape[2] != P)
+            return fail(SAR_ERR_INVALID_ARGUMENT, "grid_shape product != num_scatterers");
+        if (g->grid_shape[1] > (1u << 20) || g->grid_shape[2] > (1u << 20) || g->grid_shape[0] > (1u << 16))
+            return fail(SAR_ERR_NOT_SUPPORTED, "grid dimension too large");
+        if (!finite3(g->grid_origin, 1) || !finite3(g->grid_step_x, 1) || !finite3(g->grid_step_y, 1) ||
+            !finite3(g->grid_step_z, 1))
+            return fail(SAR_ERR_INVALID_ARGUMENT, "non-finite grid description");
+    } else {
+        if (!g->scat_posns) return fail(SAR_ERR_INVALID_ARGUMENT, "scat_posns is required without a grid");
+        if (!finite3(g->scat_posns, P)) return fail(SAR_ERR_INVALID_ARGUMENT, "non-finite scatterer position");
+        if (P > (size_t)1 << 31) return fail(SAR_ERR_NOT_SUPPORTED, "too many scatterers");
+    }
+
+    return SAR_OK;
+}
+
+int build_plan(const sar_geometry* g, sar_plan* p) {
+    const size_t N = g->num_fast_times, S = g->num_slow_times, P = g->num_scatterers;
+    const size_t M = (size_t)(g->upsample_ratio * (double)N);
+    const bool grid = g->grid_shape[0] || g->grid_shape[1] || g->grid_shape[2];
+    p->N = N;
+    p->S = S;
+    p->P = P;
+    p->M = M;
+    p->interp = g->interp;
+    p->grid = grid;
+    const double s_r = g->sample_frequency * (double)M / ((double)N * g->c_eff);    // :225-226
+    const double kappa = g->sign_multiplier * g->centre_frequency / g->c_eff;       // :228 / 2pi
+    p->kappa = to_df(kappa);
+    p->s_r = to_df(s_r);
+    const double* tx = g->transmit_posns;
+    const double* rx = g->receive_posns;
+    const double* srp = g->stab_ref_posns;
+
+    p->weights.resize(S);
+    for (size_t s = 0; s < S; ++s)
+        p->weights[s] = g->slow_time_weighting
+                            ? std::complex<double>(g->slow_time_weighting[2 * s], g->slow_time_weighting[2 * s + 1])
+                            : std::complex<double>(1.0, 0.0);
+
+    double origin[3];
+    double vmin = INFINITY, vmax = -INFINITY;
+    std::vector<PulseGeom> pulses(S);
+    std::vector<float4> alpha2;
+    std::vector<PointGeom> points;
+    std::vector<int> strip_start;
+
+    if (grid) {
+        const int nz = (int)g->grid_shape[0], ny = (int)g->grid_shape[1], nx = (int)g->grid_shape[2];
+        for (int c = 0; c < 3; ++c) origin[c] = g->grid_origin[c];
+        const double *ex = g->grid_step_x, *ey = g->grid_step_y, *ez = g->grid_step_z;
+        p->gc_adj = make_grid_const(ex, ey, ez, kappa, s_r, adjoint_bin_offset(p->interp), nx, ny, nz);
+        p->gc_fwd = p->gc_adj;
+        p->gc_fwd.bin_offset = forward_bin_offset(p->interp);
+        const int tx_tiles = p->gc_adj.tiles_x, ty_tiles = p->gc_adj.tiles_y;
+        for (size_t s = 0; s < S; ++s) {
+            pulses[s] = make_pulse_geom(tx + 3 * s, rx + 3 * s, srp + 3 * s, origin);
+            double lo, hi;
+            region_range(tx + 3 * s, rx + 3 * s, srp + 3 * s, origin, ex, ey, ez, tx_tiles * kTile - 1.0,
+                         ty_tiles * kTile - 1.0, nz - 1.0, &lo, &hi);
+            vmin = std::min(vmin, lo * s_r);
+            vmax = std::max(vmax, hi * s_r);
+        }
+        // Tile window: every pixel of a tile lies within 16|ex| + 16|ey| of the tile centre,
+        // and each of the two ranges changes by at most that distance.
+        const double nex = std::sqrt(ex[0] * ex[0] + ex[1] * ex[1] + ex[2] * ex[2]);
+        const double ney = std::sqrt(ey[0] * ey[0] + ey[1] * ey[1] + ey[2] * ey[2]);
+        const double h = s_r * 2.0 * 16.0 * (nex + ney);
+        if (h > 1.0e6) return fail(SAR_ERR_NOT_SUPPORTED, "grid spacing too coarse for the range sampling");
+        p->wwin = (2 * ((int)std::ceil(h) + 3) + 3) & ~3;
+        p->bg0 = (long)std::floor(vmin) - p->wwin / 2 - 4;
+        const double span = std::ceil(vmax) + p->wwin / 2 + 5 - (double)p->bg0;
+        if (span > 2.0e9) return fail(SAR_ERR_NOT_SUPPORTED, "range span too large");
+        p->Lg = (int)span;
+        // Backprojection staging: pulses per stage so that windows fit shared memory.
+        p->staged = false;
+        p->pb = 32;
+        for (int pb = 32; pb >= 8; pb -= 8)
+            if (bp_grid_smem_bytes(p->wwin, pb, 1) <= kBpSmemBudget) {
+                p->pb = pb;
+                p->staged = true;
+                break;
+            }
+        // Forward strips: tile columns split into segments whose window fits shared memory.
+        p->forward_points = true;
+        for (int pbf : {16, 8}) {
+            int seg = ty_tiles;
+            while (true) {
+                const int segs = (ty_tiles + seg - 1) / seg;
+                const size_t n_strips = (size_t)nz * tx_tiles * segs;
+                std::vector<int> starts(n_strips * S);
+                int need = 0;
+                for (int k = 0; k < nz; ++k)
+                    for (int ti = 0; ti < tx_tiles; ++ti)
+                        for (int sg = 0; sg < segs; ++sg) {
+                            const int tj0 = sg * seg, tj1 = std::min(tj0 + seg, ty_tiles);
+                            double o[3];
+                            for (int c = 0; c < 3; ++c)
+                                o[c] = origin[c] + ti * kTile * ex[c] + tj0 * kTile * ey[c] + k * ez[c];
+                            const size_t strip = ((size_t)k * tx_tiles + ti) * segs + sg;
+                            for (size_t s = 0; s < S; ++s) {
+                                double lo, hi;
+                                region_range(tx + 3 * s, rx + 3 * s, srp + 3 * s, o, ex, ey, ez, kTile - 1.0,
+                                             (tj1 - tj0) * kTile - 1.0, 0.0, &lo, &hi);
+                                const long b0 = (long)std::floor(lo * s_r) - 3;
+                                const long b1 = (long)std::ceil(hi * s_r) + 4;
+                                starts[strip * S + s] = (int)b0;
+                                need = std::max<int>(need, (int)(b1 - b0 + 1));
+                            }
+                        }
+                const int ws = (need + 31) & ~31;
+                if (fp_grid_smem_bytes(ws, pbf) <= kFpSmemBudget) {
+                    p->seg_tiles = seg;
+                    p->segs_per_column = segs;
+                    p->ws = ws;
+                    p->pbf = pbf;
+                    p->n_strips = n_strips;
+                    strip_start.swap(starts);
+                    p->forward_points = false;
+                    break;
+                }
+                if (seg == 1) break;
+                seg = (seg + 1) / 2;
+            }
+            if (!p->forward_points) break;
+        }
+        if (p->forward_points) {
+            // Extremely coarse grids: forward through the unstructured kernels.
+            points.resize(P);
+            alpha2.resize(S);
+        }
+        if (p->forward_points) {
+            for (int k = 0; k < nz; ++k)
+                for (int j = 0; j < ny; ++j)
+                    for (int i = 0; i < nx; ++i) {
+                        double q[3];
+                        for (int c = 0; c < 3; ++c) q[c] = i * ex[c] + j * ey[c] + k * ez[c];
+                        PointGeom& pt = points[((size_t)k * ny + j) * nx + i];
+                        for (int c = 0; c < 3; ++c) {
+                            const df d = to_df(q[c]);
+                            pt.qh[c] = d.hi;
+                            pt.ql[c] = d.lo;
+                        }
+                        const df d2 = to_df(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+                        pt.qh[3] = d2.hi;
+                        pt.ql[3] = d2.lo;
+                    }
+        }
+    } else {
+        const double* pos = g->scat_posns;
+        double lo3[3] = {INFINITY, INFINITY, INFINITY}, hi3[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (size_t i = 0; i < P; ++i)
+            for (int c = 0; c < 3; ++c) {
+                lo3[c] = std::min(lo3[c], pos[3 * i + c]);
+                hi3[c] = std::max(hi3[c], pos[3 * i + c]);
+            }
+        for (int c = 0; c < 3; ++c) origin[c] = 0.5 * (lo3[c] + hi3[c]);
+        points.resize(P);
+        alpha2.resize(S);
+        for (size_t i = 0; i < P; ++i) {
+            double q[3];
+            for (int c = 0; c < 3; ++c) q[c] = pos[3 * i + c] - origin[c];
+            PointGeom& pt = points[i];
+            for (int c = 0; c < 3; ++c) {
+                const df d = to_df(q[c]);
+                pt.qh[c] = d.hi;
+                pt.ql[c] = d.lo;
+            }
+            const df d2 = to_df(q[0] * q[0] + q[1] * q[1] + q[2] * q[2]);
+            pt.qh[3] = d2.hi;
+            pt.ql[3] = d2.lo;
+        }
+        const double ex[3] = {hi3[0] - lo3[0], 0, 0}, ey[3] = {0, hi3[1] - lo3[1], 0}, ez[3] = {0, 0, hi3[2] - lo3[2]};
+        for (size_t s = 0; s < S; ++s) {
+            pulses[s] = make_pulse_geom(tx + 3 * s, rx + 3 * s, srp + 3 * s, origin);
+            double lo, hi;
+            region_range(tx + 3 * s, rx + 3 * s, srp + 3 * s, lo3, ex, ey, ez, 1.0, 1.0, 1.0, &lo, &hi);
+            vmin = std::min(vmin, lo * s_r);
+            vmax = std::max(vmax, hi * s_r);
+        }
+        p->bg0 = (long)std::floor(vmin) - 4;
+        const double span = std::ceil(vmax) + 6 - (double)p->bg0;
+        if (span > 2.0e9) return fail(SAR_ERR_NOT_SUPPORTED, "range span too large");
+        p->Lg = (int)span;
+        p->wwin = 0;
+    }
+    if (!alpha2.empty()) {
+        for (size_t s = 0; s < S; ++s) {
+            double at[3], ar[3];
+            for (int c = 0; c < 3; ++c) {
+                at[c] = tx[3 * s + c] - origin[c];
+                ar[c] = rx[3 * s + c] - origin[c];
+            }
+            const df a = to_df(at[0] * at[0] + at[1] * at[1] + at[2] * at[2]);
+            const df b = to_df(ar[0] * ar[0] + ar[1] * ar[1] + ar[2] * ar[2]);
+            alpha2[s] = make_float4(a.hi, a.lo, b.hi, b.lo);
+        }
+    }
+
+    // ---- device tables
+    int rc;
+    if ((rc = p->alloc(&p->d_pulses, S, "pulse table"))) return rc;
+    SAR_CUDA(cudaMemcpy(p->d_pulses, pulses.data(), sizeof(PulseGeom) * S, cudaMemcpyHostToDevice), "pulse table");
+    if (!points.empty()) {
+        if ((rc = p->alloc(&p->d_points, P, "point table"))) return rc;
+        SAR_CUDA(cudaMemcpy(p->d_points, points.data(), sizeof(PointGeom) * P, cudaMemcpyHostToDevice), "point table");
+        if ((rc = p->alloc(&p->d_alpha2, S, "antenna norms"))) return rc;
+        SAR_CUDA(cudaMemcpy(p->d_alpha2, alpha2.data(), sizeof(float4) * S, cudaMemcpyHostToDevice), "antenna norms");
+    }
+    if (!strip_start.empty()) {
+        if ((rc = p->alloc(&p->d_strip, strip_start.size(), "strip table"))) return rc;
+        SAR_CUDA(cudaMemcpy(p->d_strip, strip_start.data(), sizeof(int) * strip_start.size(), cudaMemcpyHostToDevice),
+                 "strip table");
+    }
+    std::vector<float2> wave(N);
+    for (size_t f = 0; f < N; ++f)
+        wave[f] = g->waveform_fft ? make_float2((float)g->waveform_fft[2 * f], (float)g->waveform_fft[2 * f + 1])
+                                  : make_float2(1.f, 0.f);
+    if ((rc = p->alloc(&p->d_wave, N, "waveform"))) return rc;
+    SAR_CUDA(cudaMemcpy(p->d_wave, wave.data(), sizeof(float2) * N, cudaMemcpyHostToDevice), "waveform");
+    if ((rc = p->alloc(&p->d_w, S, "weights"))) return rc;
+    if ((rc = p->alloc(&p->d_wadj, S, "weights"))) return rc;
+    if ((rc = p->alloc(&p->d_wfwd, S, "weights"))) return rc;
+    if ((rc = upload_weights(p, nullptr, true))) return rc;
+    if ((rc = p->alloc(&p->d_flags, 1, "flags"))) return rc;
+    SAR_CUDA(cudaMemset(p->d_flags, 0, sizeof(unsigned)), "flags");
+    if ((rc = p->alloc(&p->d_prof, (size_t)S * p->Lg, "range profiles"))) return rc;
+
+    // ---- FFT work rows
+    const size_t row_bytes = M * sizeof(float2);
+    p->chunk = (int)std::min<size_t>(S, std::max<size_t>(1, kSpecBudget / row_bytes));
+    if ((rc = p->alloc(&p->d_spec, (size_t)p->chunk * M, "FFT rows"))) return rc;
+    if ((rc = make_fft(&p->fft_full, (long)M, p->chunk))) return rc;
+    p->have_full = true;
+    const int tail = (int)(S % (size_t)p->chunk);
+    if (tail) {
+        if ((rc = make_fft(&p->fft_tail, (long)M, tail))) return rc;
+        p->have_tail = true;
+    }
+    return SAR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* sar_status_string(int status) {
+    switch (status) {
+        case SAR_OK: return "ok";
+        case SAR_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case SAR_ERR_CUDA: return "CUDA error";
+        case SAR_ERR_CUFFT: return "cuFFT error";
+        case SAR_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case SAR_ERR_NOT_SUPPORTED: return "not supported";
+        default: return "unknown status";
+    }
+}
+
+size_t sar_last_error(char* buf, size_t len) {
+    if (buf && len) {
+        const size_t n = std::min(len - 1, g_last_error.size());
+        memcpy(buf, g_last_error.data(), n);
+        buf[n] = '\0';
+    }
+    return g_last_error.size();
+}
+
+int sar_plan_create(const sar_geometry* geom, int device, sar_plan** plan_out) {
+    g_last_error.clear();
+    if (!geom || !plan_out) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    *plan_out = nullptr;
+    const int vrc = validate_geometry(geom);
+    if (vrc != SAR_OK) return vrc;
+    int dev = device;
+    if (dev < 0) SAR_CUDA(cudaGetDevice(&dev), "cudaGetDevice");
+    DeviceGuard guard(dev);
+    if (guard.status != cudaSuccess) return cuda_fail(guard.status, "select device");
+    sar_plan* p = new (std::nothrow) sar_plan();
+    if (!p) return fail(SAR_ERR_OUT_OF_MEMORY, "host allocation");
+    p->device = dev;
+    const int rc = build_plan(geom, p);
+    if (rc != SAR_OK) {
+        delete p;
+        return rc;
+    }
+    *plan_out = p;
+    return SAR_OK;
+}
+
+int sar_plan_destroy(sar_plan* plan) {
+    delete plan;
+    return SAR_OK;
+}
+
+int sar_plan_get_info(const sar_plan* p, sar_plan_info* info) {
+    if (!p || !info) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    info->working_length = p->M;
+    info->profile_first_bin = p->bg0;
+    info->profile_length = (size_t)p->Lg;
+    info->tile_window = p->grid ? (size_t)p->wwin : 0;
+    info->strip_window = (p->grid && !p->forward_points) ? (size_t)p->ws : 0;
+    info->device_bytes = p->device_bytes;
+    info->grid = p->grid ? 1 : 0;
+    return SAR_OK;
+}
+
+static int upsample_into_pairs(sar_plan* p, const float2* y, cudaStream_t st, bool pairs_out, float2* prof) {
+    for (size_t first = 0; first < p->S; first += (size_t)p->chunk) {
+        const int rows = (int)std::min<size_t>(p->chunk, p->S - first);
+        SAR_CUDA(launch_pack_adjoint(y, p->d_wave, p->d_spec, (int)p->N, (long)p->M, rows, (int)first, st), "pack");
+        int rc = run_fft(p, p->d_spec, rows, CUFFT_INVERSE, st);
+        if (rc) return rc;
+        if (pairs_out)
+            SAR_CUDA(launch_unpack_pairs(p->d_spec, p->d_wadj, p->d_prof, (long)p->M, p->Lg, p->bg0, rows, (int)first,
+                                         p->interp == SAR_INTERP_LINEAR, st),
+                     "unpack");
+        else
+            SAR_CUDA(launch_unpack_profiles(p->d_spec, prof, (long)p->M, p->Lg, p->bg0, rows, (int)first, st), "unpack");
+    }
+    return SAR_OK;
+}
+
+static PointArgs point_args(sar_plan* p, float bin_offset) {
+    PointArgs a;
+    a.pulses = p->d_pulses;
+    a.alpha2 = p->d_alpha2;
+    a.points = p->d_points;
+    a.kappa = p->kappa;
+    a.s_r = p->s_r;
+    a.bin_offset = bin_offset;
+    a.S = (int)p->S;
+    a.P = (int)p->P;
+    a.Lg = p->Lg;
+    a.bg0 = (int)p->bg0;
+    a.linear = p->interp == SAR_INTERP_LINEAR;
+    a.flags = p->d_flags;
+    return a;
+}
+
+int sar_adjoint(sar_plan* p, const void* y_dev, void* x_dev, void* stream) {
+    if (!p || !y_dev || !x_dev) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(p->mu);
+    DeviceGuard guard(p->device);
+    if (guard.status != cudaSuccess) return cuda_fail(guard.status, "select device");
+    cudaStream_t st = (cudaStream_t)stream;
+    p->last_stream = st;
+    cudaEvent_t* ev = p->timing_slot();
+    mark(ev, 0, st);
+    int rc = upsample_into_pairs(p, (const float2*)y_dev, st, true, nullptr);
+    if (rc) return rc;
+    mark(ev, 1, st);
+    if (p->grid) {
+        BpGridArgs a;
+        a.g = p->gc_adj;
+        a.pulses = p->d_pulses;
+        a.pairs = p->d_prof;
+        a.x = (float2*)x_dev;
+        a.flags = p->d_flags;
+        a.S = (int)p->S;
+        a.Lg = p->Lg;
+        a.bg0 = (int)p->bg0;
+        a.wwin = p->wwin;
+        a.pb = p->pb;
+        a.staged = p->staged;
+        a.accumulate = 0;
+        SAR_CUDA(launch_bp_grid(a, st), "backprojection");
+    } else {
+        SAR_CUDA(launch_bp_points(point_args(p, adjoint_bin_offset(p->interp)), p->d_prof, (float2*)x_dev, 0, st),
+                 "backprojection");
+    }
+    mark(ev, 2, st);
+    mark(ev, 3, st);
+    return SAR_OK;
+}
+
+int sar_forward(sar_plan* p, const void* x_dev, void* y_dev, void* stream) {
+    if (!p || !y_dev || !x_dev) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(p->mu);
+    DeviceGuard guard(p->device);
+    if (guard.status != cudaSuccess) return cuda_fail(guard.status, "select device");
+    cudaStream_t st = (cudaStream_t)stream;
+    p->last_stream = st;
+    float2* acc = reinterpret_cast<float2*>(p->d_prof);
+    cudaEvent_t* ev = p->timing_slot();
+    mark(ev, 0, st);
+    SAR_CUDA(cudaMemsetAsync(acc, 0, sizeof(float2) * p->S * (size_t)p->Lg, st), "zero accumulator");
+    mark(ev, 1, st);
+    if (p->grid && !p->forward_points) {
+        FpGridArgs a;
+        a.g = p->gc_fwd;
+        a.pulses = p->d_pulses;
+        a.x = (const float2*)x_dev;
+        a.acc = acc;
+        a.strip_start = p->d_strip;
+        a.flags = p->d_flags;
+        a.S = (int)p->S;
+        a.Lg = p->Lg;
+        a.bg0 = (int)p->bg0;
+        a.seg_tiles = p->seg_tiles;
+        a.segs_per_column = p->segs_per_column;
+        a.ws = p->ws;
+        a.pbf = p->pbf;
+        a.linear = p->interp == SAR_INTERP_LINEAR;
+        SAR_CUDA(launch_fp_grid(a, st), "forward scatter");
+    } else {
+        SAR_CUDA(launch_fp_points(point_args(p, forward_bin_offset(p->interp)), (const float2*)x_dev, acc, st),
+                 "forward scatter");
+    }
+    mark(ev, 2, st);
+    for (size_t first = 0; first < p->S; first += (size_t)p->chunk) {
+        const int rows = (int)std::min<size_t>(p->chunk, p->S - first);
+        SAR_CUDA(launch_pack_forward(acc, p->d_spec, (long)p->M, p->Lg, p->bg0, rows, (int)first, st), "pack");
+        int rc = run_fft(p, p->d_spec, rows, CUFFT_FORWARD, st);
+        if (rc) return rc;
+        SAR_CUDA(launch_extract_forward(p->d_spec, p->d_wave, p->d_wfwd, (float2*)y_dev, (int)p->N, (long)p->M, rows,
+                                        (int)first, st),
+                 "extract");
+    }
+    mark(ev, 3, st);
+    return SAR_OK;
+}
+
+int sar_profiles(sar_plan* p, const void* y_dev, void* prof_dev, void* stream) {
+    if (!p || !y_dev || !prof_dev) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(p->mu);
+    DeviceGuard guard(p->device);
+    if (guard.status != cudaSuccess) return cuda_fail(guard.status, "select device");
+    p->last_stream = (cudaStream_t)stream;
+    return upsample_into_pairs(p, (const float2*)y_dev, (cudaStream_t)stream, false, (float2*)prof_dev);
+}
+
+int sar_set_slow_time_weighting(sar_plan* p, const double* w) {
+    if (!p || !w) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(p->mu);
+    DeviceGuard guard(p->device);
+    for (size_t s = 0; s < p->S; ++s) p->weights[s] = std::complex<double>(w[2 * s], w[2 * s + 1]);
+    if (p->last_stream) SAR_CUDA(cudaStreamSynchronize(p->last_stream), "synchronise");
+    return upload_weights(p, nullptr, true);
+}
+
+int sar_set_slow_time_weighting_device(sar_plan* p, const void* w_dev, void* stream) {
+    if (!p || !w_dev) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(p->mu);
+    DeviceGuard guard(p->device);
+    cudaStream_t st = (cudaStream_t)stream;
+    p->last_stream = st;
+    SAR_CUDA(launch_weights((const float2*)w_dev, p->d_wadj, p->d_wfwd, (int)p->S, p->interp == SAR_INTERP_LINEAR, st),
+             "weights kernel");
+    return SAR_OK;
+}
+
+int sar_enable_stage_timing(sar_plan* p, int enable) {
+    if (!p) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(p->mu);
+    p->timing = enable != 0;
+    p->events_used = 0;
+    return SAR_OK;
+}
+
+int sar_stage_times(sar_plan* p, float* ms, int* calls) {
+    if (!p || !ms || !calls) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(p->mu);
+    DeviceGuard guard(p->device);
+    ms[0] = ms[1] = ms[2] = 0.0f;
+    for (size_t c = 0; c < p->events_used; ++c) {
+        auto& ev = p->events[c];
+        SAR_CUDA(cudaEventSynchronize(ev[3]), "stage timing");
+        for (int i = 0; i < 3; ++i) {
+            float t = 0.0f;
+            SAR_CUDA(cudaEventElapsedTime(&t, ev[i], ev[i + 1]), "stage timing");
+            ms[i] += t;
+        }
+    }
+    *calls = (int)p->events_used;
+    return SAR_OK;
+}
+
+int sar_device_flags(sar_plan* p, unsigned* flags) {
+    if (!p || !flags) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(p->mu);
+    DeviceGuard guard(p->device);
+    if (p->last_stream) SAR_CUDA(cudaStreamSynchronize(p->last_stream), "synchronise");
+    SAR_CUDA(cudaMemcpy(flags, p->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost), "read flags");
+    SAR_CUDA(cudaMemset(p->d_flags, 0, sizeof(unsigned)), "clear flags");
+    return SAR_OK;
+}
+
+// ------------------------------------------------------------ drop-in boundary
+static void geometry_from_info(const SarCalculationInfo* info, sar_geometry* g) {
+    memset(g, 0, sizeof(*g));
+    g->num_fast_times = info->num_fast_times;
+    g->num_slow_times = info->num_slow_times;
+    g->num_scatterers = info->num_scatterers;
+    g->transmit_posns = info->transmit_posns;
+    g->receive_posns = info->receive_posns;
+    g->stab_ref_posns = info->stab_ref_posns;
+    g->scat_posns = info->scat_posns;
+    g->waveform_fft = info->waveform_fft;
+    g->slow_time_weighting = info->slow_time_weighting;
+    g->centre_frequency = info->centre_frequency;
+    g->sample_frequency = info->sample_frequency;
+    g->c_eff = info->c_eff;
+    g->upsample_ratio = info->upsample_ratio;
+    g->sign_multiplier = info->sign_multiplier;
+    g->interp = SAR_INTERP_NEAREST_REF;
+}
+
+// One synchronous operator application on host FP64 buffers (FFT-ordered phase history).
+static int dropin_run(SarCalculationInfo* info, bool forward) {
+    if (!info) return fail(SAR_ERR_INVALID_ARGUMENT, "null SarCalculationInfo");
+    if (!info->phase_history || !info->scattering_amplitudes)
+        return fail(SAR_ERR_INVALID_ARGUMENT, "null phase_history or scattering_amplitudes");
+    const size_t N = info->num_fast_times, S = info->num_slow_times, P = info->num_scatterers;
+    // Zero the output first, like setup_{forward,adjoint}_evaluate (sarsolver_cxx.cpp:264-269, :312-317).
+    if (forward)
+        memset(info->phase_history, 0, sizeof(double) * 2 * N * S);
+    else
+        memset(info->scattering_amplitudes, 0, sizeof(double) * 2 * P);
+    sar_geometry g;
+    geometry_from_info(info, &g);
+    sar_plan* plan = nullptr;
+    int rc = sar_plan_create(&g, -1, &plan);
+    if (rc) return rc;
+    const int half = (int)(N / 2);
+    std::vector<float2> hx(P), hy(N * S);
+    float2 *dx = nullptr, *dy = nullptr;
+    cudaError_t e = cudaMalloc((void**)&dx, sizeof(float2) * P);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&dy, sizeof(float2) * N * S);
+    if (e == cudaSuccess) {
+        if (forward) {
+            for (size_t p = 0; p < P; ++p)
+                hx[p] = make_float2((float)info->scattering_amplitudes[2 * p], (float)info->scattering_amplitudes[2 * p + 1]);
+            e = cudaMemcpy(dx, hx.data(), sizeof(float2) * P, cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) rc = sar_forward(plan, dx, dy, nullptr);
+            if (e == cudaSuccess && !rc) e = cudaMemcpy(hy.data(), dy, sizeof(float2) * N * S, cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess && !rc)
+                for (size_t s = 0; s < S; ++s)
+                    for (size_t i = 0; i < N; ++i) {   // device layout is fftshifted; the struct holds FFT order
+                        const float2 v = hy[s * N + (i + half) % N];
+                        info->phase_history[2 * (s * N + i)] = v.x;
+                        info->phase_history[2 * (s * N + i) + 1] = v.y;
+                    }
+        } else {
+            for (size_t s = 0; s < S; ++s)
+                for (size_t i = 0; i < N; ++i)
+                    hy[s * N + (i + half) % N] = make_float2((float)info->phase_history[2 * (s * N + i)],
+                                                             (float)info->phase_history[2 * (s * N + i) + 1]);
+            e = cudaMemcpy(dy, hy.data(), sizeof(float2) * N * S, cudaMemcpyHostToDevice);
+            if (e == cudaSuccess) rc = sar_adjoint(plan, dy, dx, nullptr);
+            if (e == cudaSuccess && !rc) e = cudaMemcpy(hx.data(), dx, sizeof(float2) * P, cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess && !rc)
+                for (size_t p = 0; p < P; ++p) {
+                    info->scattering_amplitudes[2 * p] = hx[p].x;
+                    info->scattering_amplitudes[2 * p + 1] = hx[p].y;
+                }
+        }
+    }
+    cudaFree(dx);
+    cudaFree(dy);
+    sar_plan_destroy(plan);
+    if (e != cudaSuccess) return cuda_fail(e, forward ? "forward_evaluate" : "adjoint_evaluate");
+    return rc;
+}
+
+void forward_evaluate(SarCalculationInfo* info) { dropin_run(info, true); }
+void adjoint_evaluate(SarCalculationInfo* info) { dropin_run(info, false); }
+
+}  // extern "C"

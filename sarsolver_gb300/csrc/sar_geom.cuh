@@ -1,0 +1,351 @@
+// sar_geom.cuh -- range geometry shared by every SAR kernel (host and device).
+//
+// The reference forms the differential bistatic range in FP64 per pixel and pulse
+// (src/sarsolver/cxx_binding/sarsolver_cxx.cpp:10-20, :283, :287):
+//     dR(p, s) = |tx_s - p| + |rx_s - p| - (|tx_s - srp_s| + |rx_s - srp_s|)
+// and uses it twice: the phase k*dR with k = 2*pi*sign*fc/c_eff (:228) and the range bin
+// dR * s_r with s_r = fs*M/(N*c_eff) (:225-226).  At kilometre stand-off the phase is
+// ~1e5 rad and must stay within ~1e-5 rad, which FP32 cannot carry.  Two precision schemes:
+//
+// 1. Regular grids (the fast path).  For each 16x16 pixel sub-tile and pulse, dR around the
+//    sub-tile's anchor pixel is expanded to third order in the integer pixel offsets
+//    (di, dj):  dR = dR0 + gx di + gy dj + quadratic + cubic terms, Taylor series of |w + d|
+//    (w = anchor - antenna, d = di*ex + dj*ey).  The anchor range and the gradient are formed
+//    in double-float (hi + lo FP32 pairs, error-free transforms), then scaled to cycles and
+//    reduced modulo one cycle: because di and dj are integers, frac(kappa*gx) may replace
+//    kappa*gx without changing exp(2*pi*i*phase).  Each pixel then costs a handful of FP32
+//    FMAs for the phase (magnitude < 9 cycles) and the bin position (< 64 bins), with no
+//    square root.  The quartic remainder is < 1e-10 m for |d| < 3 m at 10 km.
+// 2. Unstructured positions.  Per pixel and pulse: W = |alpha|^2 - 2 alpha.q + |q|^2 in
+//    double-float (alpha = antenna - origin, q = pixel - origin), its square root by one
+//    Newton step, then the same mod-1 reduction of the phase.
+//
+// Everything here is plain IEEE FP32 arithmetic with explicit fmaf and correctly rounded
+// sqrtf / division, so the host build (geom_host.cpp) reproduces the device numbers and the
+// precision can be checked against FP64 without a GPU.
+#pragma once
+
+#include <math.h>
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define SAR_HD __host__ __device__ __forceinline__
+#else
+#define SAR_HD static inline
+#endif
+
+namespace sar {
+
+// ------------------------------------------------------------------ double-float
+struct df {
+    float hi, lo;
+};
+struct df3 {
+    df x, y, z;
+};
+
+SAR_HD df df_make(float hi, float lo) {
+    df r;
+    r.hi = hi;
+    r.lo = lo;
+    return r;
+}
+// Knuth TwoSum: s + e == a + b exactly.
+SAR_HD df two_sum(float a, float b) {
+    float s = a + b;
+    float bb = s - a;
+    float e = (a - (s - bb)) + (b - bb);
+    return df_make(s, e);
+}
+// Dekker FastTwoSum, requires |a| >= |b| (or a == 0).
+SAR_HD df fast_two_sum(float a, float b) {
+    float s = a + b;
+    float e = b - (s - a);
+    return df_make(s, e);
+}
+// Exact product via FMA.
+SAR_HD df two_prod(float a, float b) {
+    float p = a * b;
+    float e = fmaf(a, b, -p);
+    return df_make(p, e);
+}
+SAR_HD df df_add(df a, df b) {
+    df s = two_sum(a.hi, b.hi);
+    float e = s.lo + (a.lo + b.lo);
+    return fast_two_sum(s.hi, e);
+}
+SAR_HD df df_neg(df a) { return df_make(-a.hi, -a.lo); }
+SAR_HD df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
+SAR_HD df df_mul(df a, df b) {
+    df p = two_prod(a.hi, b.hi);
+    float e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo));
+    return fast_two_sum(p.hi, e);
+}
+SAR_HD df df_mulf(df a, float b) {
+    df p = two_prod(a.hi, b);
+    float e = fmaf(a.lo, b, p.lo);
+    return fast_two_sum(p.hi, e);
+}
+// sqrt(a) for a.hi > 0: correctly rounded FP32 root plus one Newton correction.
+SAR_HD df df_sqrt(df a) {
+    float r = sqrtf(a.hi);
+    float e = fmaf(-r, r, a.hi) + a.lo;
+    return fast_two_sum(r, e / (2.0f * r));
+}
+SAR_HD df df_div(df a, df b) {
+    float q1 = a.hi / b.hi;
+    df r = df_sub(a, df_mulf(b, q1));
+    float q2 = r.hi / b.hi;
+    return fast_two_sum(q1, q2);
+}
+SAR_HD df df_dot3(const df3& a, const df3& b) {
+    df s = df_mul(a.x, b.x);
+    s = df_add(s, df_mul(a.y, b.y));
+    return df_add(s, df_mul(a.z, b.z));
+}
+SAR_HD df3 df3_sub(const df3& a, const df3& b) {
+    df3 r;
+    r.x = df_sub(a.x, b.x);
+    r.y = df_sub(a.y, b.y);
+    r.z = df_sub(a.z, b.z);
+    return r;
+}
+// Integer multiple of a df vector, n exactly representable (|n| < 2^24).
+SAR_HD df3 df3_scale_int(const df3& a, float n) {
+    df3 r;
+    r.x = df_mulf(a.x, n);
+    r.y = df_mulf(a.y, n);
+    r.z = df_mulf(a.z, n);
+    return r;
+}
+SAR_HD df3 df3_add(const df3& a, const df3& b) {
+    df3 r;
+    r.x = df_add(a.x, b.x);
+    r.y = df_add(a.y, b.y);
+    r.z = df_add(a.z, b.z);
+    return r;
+}
+// Round to nearest integer (ties to even) for |x| < 2^22 via the 1.5*2^23 shifter: keeps the
+// work on the FP32 pipe and leaves the integer in the low mantissa bits.
+#define SAR_SHIFTER 12582912.0f
+#define SAR_SHIFTER_BITS 0x4B400000
+SAR_HD float round_shift(float x) { return (x + SAR_SHIFTER) - SAR_SHIFTER; }
+// Fractional part in [-0.5, 0.5] of a df value (|value| < 2^22).
+SAR_HD float df_frac(df a) {
+    float n = round_shift(a.hi);
+    return (a.hi - n) + a.lo;
+}
+
+// ------------------------------------------------------------------ constants
+// Per-pulse geometry, everything relative to one origin (the grid's first pixel, or the
+// centre of an unstructured scene's bounding box).  16 floats.
+struct PulseGeom {
+    float atx_hi[3], atx_lo[3];   // transmitter - origin
+    float arx_hi[3], arx_lo[3];   // receiver - origin
+    float rref_hi, rref_lo;       // |tx - srp| + |rx - srp|
+    float monostatic;             // 1 if tx == rx exactly
+    float pad;
+};
+
+SAR_HD df3 pulse_tx(const PulseGeom& g) {
+    df3 r;
+    r.x = df_make(g.atx_hi[0], g.atx_lo[0]);
+    r.y = df_make(g.atx_hi[1], g.atx_lo[1]);
+    r.z = df_make(g.atx_hi[2], g.atx_lo[2]);
+    return r;
+}
+SAR_HD df3 pulse_rx(const PulseGeom& g) {
+    df3 r;
+    r.x = df_make(g.arx_hi[0], g.arx_lo[0]);
+    r.y = df_make(g.arx_hi[1], g.arx_lo[1]);
+    r.z = df_make(g.arx_hi[2], g.arx_lo[2]);
+    return r;
+}
+
+// Grid and signal constants (kernel argument by value).
+struct GridConst {
+    df3 ex, ey, ez;              // pixel steps along x (i), y (j), z (k) in metres
+    float exx, exy, eyy;         // |ex|^2, ex.ey, |ey|^2
+    df kappa;                    // cycles per metre of bistatic range: sign*fc/c_eff
+    df s_r;                      // bins per metre of bistatic range: fs*M/(N*c_eff)
+    float bin_offset;            // -0.5 (linear: n = floor(v)) or +0.5 (adjoint nearest: ceil)
+                                 // or 0 (forward nearest: round)
+    int nx, ny, nz;              // grid shape
+    int tiles_x, tiles_y;        // 32x32 tiles per plane
+};
+
+// Coefficients of one (sub-tile, pulse) pair: 16 floats.
+//  phase (cycles): ph = c0 + c1 di + c2 dj + c3 di^2 + c4 di dj + c5 dj^2
+//                       + c6 di^3 + c7 di^2 dj + c8 di dj^2 + c9 dj^3      (c0..c2 reduced mod 1)
+//  bin:            v  = v0 + v1 di + v2 dj + v3 di^2 + v4 di dj + v5 dj^2 (relative to the tile's
+//                  base bin, bin_offset already folded into v0)
+struct Coeffs {
+    float c[10];
+    float v[6];
+};
+
+struct AntennaTerms {
+    df R;          // |w|
+    df gx, gy;     // w.ex/|w|, w.ey/|w|   (m per pixel)
+    float qxx, qxy, qyy;             // quadratic coefficients (m)
+    float kxxx, kxxy, kxyy, kyyy;    // cubic coefficients (m)
+};
+
+// Taylor expansion of |w + di*ex + dj*ey| about di = dj = 0.
+SAR_HD AntennaTerms expand_antenna(const df3& anchor, const df3& antenna, const GridConst& g) {
+    AntennaTerms t;
+    df3 w = df3_sub(anchor, antenna);
+    df W = df_dot3(w, w);
+    t.R = df_sqrt(W);
+    t.gx = df_div(df_dot3(w, g.ex), t.R);
+    t.gy = df_div(df_dot3(w, g.ey), t.R);
+    const float ux = t.gx.hi, uy = t.gy.hi;
+    const float inv = 1.0f / t.R.hi;
+    const float pxx = g.exx - ux * ux;
+    const float pxy = g.exy - ux * uy;
+    const float pyy = g.eyy - uy * uy;
+    // second order: (d^T P d) / (2|w|)
+    t.qxx = 0.5f * pxx * inv;
+    t.qxy = pxy * inv;
+    t.qyy = 0.5f * pyy * inv;
+    // third order: -(u.d)(d^T P d) / (2|w|^2)
+    const float h = -0.5f * inv * inv;
+    t.kxxx = h * ux * pxx;
+    t.kxxy = h * (uy * pxx + 2.0f * ux * pxy);
+    t.kxyy = h * (2.0f * uy * pxy + ux * pyy);
+    t.kyyy = h * uy * pyy;
+    return t;
+}
+
+// Full coefficient set for a sub-tile anchor (df3 position relative to the origin).
+// Returns the anchor's absolute bin position in vbin (double-float) so the caller can pick a
+// base bin; the v-coefficients are relative to base_bin, which the caller passes back in
+// finish_bins() below.
+struct AnchorExpansion {
+    df dR;                 // differential bistatic range at the anchor (m)
+    df gx, gy;             // gradient (m per pixel), summed over the two antennas
+    float q[3];            // quadratic (m)
+    float k[4];            // cubic (m)
+};
+
+SAR_HD AnchorExpansion expand_anchor(const df3& anchor, const PulseGeom& pg, const GridConst& g) {
+    AnchorExpansion a;
+    AntennaTerms t = expand_antenna(anchor, pulse_tx(pg), g);
+    if (pg.monostatic != 0.0f) {
+        a.dR = df_mulf(t.R, 2.0f);
+        a.gx = df_mulf(t.gx, 2.0f);
+        a.gy = df_mulf(t.gy, 2.0f);
+        a.q[0] = 2.0f * t.qxx;
+        a.q[1] = 2.0f * t.qxy;
+        a.q[2] = 2.0f * t.qyy;
+        a.k[0] = 2.0f * t.kxxx;
+        a.k[1] = 2.0f * t.kxxy;
+        a.k[2] = 2.0f * t.kxyy;
+        a.k[3] = 2.0f * t.kyyy;
+    } else {
+        AntennaTerms r = expand_antenna(anchor, pulse_rx(pg), g);
+        a.dR = df_add(t.R, r.R);
+        a.gx = df_add(t.gx, r.gx);
+        a.gy = df_add(t.gy, r.gy);
+        a.q[0] = t.qxx + r.qxx;
+        a.q[1] = t.qxy + r.qxy;
+        a.q[2] = t.qyy + r.qyy;
+        a.k[0] = t.kxxx + r.kxxx;
+        a.k[1] = t.kxxy + r.kxxy;
+        a.k[2] = t.kxyy + r.kxyy;
+        a.k[3] = t.kyyy + r.kyyy;
+    }
+    a.dR = df_sub(a.dR, df_make(pg.rref_hi, pg.rref_lo));
+    return a;
+}
+
+// Phase coefficients (cycles), reduced modulo one cycle where exact.
+SAR_HD void phase_coeffs(const AnchorExpansion& a, const GridConst& g, float* c) {
+    c[0] = df_frac(df_mul(g.kappa, a.dR));
+    c[1] = df_frac(df_mul(g.kappa, a.gx));
+    c[2] = df_frac(df_mul(g.kappa, a.gy));
+    const float kap = g.kappa.hi;
+    c[3] = kap * a.q[0];
+    c[4] = kap * a.q[1];
+    c[5] = kap * a.q[2];
+    c[6] = kap * a.k[0];
+    c[7] = kap * a.k[1];
+    c[8] = kap * a.k[2];
+    c[9] = kap * a.k[3];
+}
+
+// Absolute bin position of the anchor (double-float).
+SAR_HD df anchor_bin(const AnchorExpansion& a, const GridConst& g) { return df_mul(g.s_r, a.dR); }
+
+// Base bin of a tile from the anchor positions of its sub-tiles: floor of their mean.
+SAR_HD int base_bin_of(df sum_of_bins, float count) {
+    df m = df_mulf(sum_of_bins, 1.0f / count);   // count is a power of two: exact
+    float f = floorf(m.hi);
+    if (m.hi == f && m.lo < 0.0f) f -= 1.0f;
+    return (int)f;
+}
+
+// Bin coefficients relative to base_bin, with the interpolation offset folded in.
+SAR_HD void bin_coeffs(const AnchorExpansion& a, df vbin, int base_bin, const GridConst& g, float* v) {
+    df rel = df_sub(vbin, df_make((float)base_bin, 0.0f));
+    v[0] = (rel.hi + rel.lo) + g.bin_offset;
+    const float sr = g.s_r.hi;
+    v[1] = sr * (a.gx.hi + a.gx.lo);
+    v[2] = sr * (a.gy.hi + a.gy.lo);
+    v[3] = sr * a.q[0];
+    v[4] = sr * a.q[1];
+    v[5] = sr * a.q[2];
+}
+
+// Anchor position of pixel (i, j, k) relative to the grid origin.
+SAR_HD df3 pixel_position(int i, int j, int k, const GridConst& g) {
+    df3 p = df3_scale_int(g.ex, (float)i);
+    p = df3_add(p, df3_scale_int(g.ey, (float)j));
+    if (k != 0) p = df3_add(p, df3_scale_int(g.ez, (float)k));
+    return p;
+}
+
+// ---------------------------------------------------------- per-pixel evaluation
+// Column part (di fixed) and pixel part (dj varies) of the polynomials; see sar_kernels.cu.
+struct ColumnTerms {
+    float cph, b1, b2;   // phase: cph + b1 dj + b2 dj^2 + c9 dj^3
+    float cv, bv1;       // bin:   cv + bv1 dj + v5 dj^2
+};
+
+SAR_HD ColumnTerms column_terms(const Coeffs& q, float di, float di2, float di3) {
+    ColumnTerms t;
+    t.cph = fmaf(q.c[6], di3, fmaf(q.c[3], di2, fmaf(q.c[1], di, q.c[0])));
+    t.b1 = fmaf(q.c[7], di2, fmaf(q.c[4], di, q.c[2]));
+    t.b2 = fmaf(q.c[8], di, q.c[5]);
+    t.cv = fmaf(q.v[3], di2, fmaf(q.v[1], di, q.v[0]));
+    t.bv1 = fmaf(q.v[4], di, q.v[2]);
+    return t;
+}
+
+SAR_HD float pixel_phase(const ColumnTerms& t, float c9, float dj, float dj2, float dj3) {
+    return fmaf(c9, dj3, fmaf(t.b2, dj2, fmaf(t.b1, dj, t.cph)));
+}
+SAR_HD float pixel_bin(const ColumnTerms& t, float v5, float dj, float dj2) {
+    return fmaf(v5, dj2, fmaf(t.bv1, dj, t.cv));
+}
+
+// ------------------------------------------------ unstructured positions (scheme 2)
+// Per pixel: q = p - origin as hi/lo and |q|^2 as hi/lo.
+struct PointGeom {
+    float qh[4];   // qx, qy, qz, |q|^2 (hi)
+    float ql[4];   // lo parts
+};
+
+// |alpha - q| for an antenna alpha (relative to the origin) with |alpha|^2 given.
+SAR_HD df point_range(const df3& alpha, df alpha2, const PointGeom& pt) {
+    df3 q;
+    q.x = df_make(pt.qh[0], pt.ql[0]);
+    q.y = df_make(pt.qh[1], pt.ql[1]);
+    q.z = df_make(pt.qh[2], pt.ql[2]);
+    df dot = df_dot3(alpha, q);
+    df W = df_add(alpha2, df_make(pt.qh[3], pt.ql[3]));
+    W = df_sub(W, df_mulf(dot, 2.0f));
+    return df_sqrt(W);
+}
+
+}  // namespace sar

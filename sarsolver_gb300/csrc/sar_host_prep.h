@@ -1,0 +1,109 @@
+// sar_host_prep.h -- FP64 host preparation of the per-pulse and per-grid constants that the
+// kernels consume as double-float (hi + lo FP32) values.  Host-only; included by the plan
+// code (sar_plan.cu) and by the host evaluation harness (geom_host.cpp).
+#pragma once
+
+#include <math.h>
+#include <stddef.h>
+
+#include "sar_geom.cuh"
+
+namespace sar {
+
+static inline df to_df(double x) {
+    df r;
+    r.hi = (float)x;
+    r.lo = (float)(x - (double)r.hi);
+    return r;
+}
+
+static inline df3 to_df3(const double* v) {
+    df3 r;
+    r.x = to_df(v[0]);
+    r.y = to_df(v[1]);
+    r.z = to_df(v[2]);
+    return r;
+}
+
+static inline double dist3(const double* a, const double* b) {
+    double d = 0.0;
+    for (int i = 0; i < 3; ++i) d += (a[i] - b[i]) * (a[i] - b[i]);
+    return sqrt(d);
+}
+
+// Per-pulse table: antennas relative to `origin`, reference range to the SRP
+// (sarsolver_cxx.cpp:283 / :330), monostatic flag when tx and rx coincide exactly.
+static inline PulseGeom make_pulse_geom(const double* tx, const double* rx, const double* srp,
+                                        const double* origin) {
+    PulseGeom g;
+    for (int i = 0; i < 3; ++i) {
+        df a = to_df(tx[i] - origin[i]);
+        df b = to_df(rx[i] - origin[i]);
+        g.atx_hi[i] = a.hi;
+        g.atx_lo[i] = a.lo;
+        g.arx_hi[i] = b.hi;
+        g.arx_lo[i] = b.lo;
+    }
+    df rr = to_df(dist3(tx, srp) + dist3(rx, srp));
+    g.rref_hi = rr.hi;
+    g.rref_lo = rr.lo;
+    g.monostatic = (tx[0] == rx[0] && tx[1] == rx[1] && tx[2] == rx[2]) ? 1.0f : 0.0f;
+    g.pad = 0.0f;
+    return g;
+}
+
+static inline GridConst make_grid_const(const double* ex, const double* ey, const double* ez,
+                                        double kappa, double s_r, float bin_offset, int nx, int ny,
+                                        int nz) {
+    GridConst g;
+    g.ex = to_df3(ex);
+    g.ey = to_df3(ey);
+    g.ez = to_df3(ez);
+    g.exx = (float)(ex[0] * ex[0] + ex[1] * ex[1] + ex[2] * ex[2]);
+    g.exy = (float)(ex[0] * ey[0] + ex[1] * ey[1] + ex[2] * ey[2]);
+    g.eyy = (float)(ey[0] * ey[0] + ey[1] * ey[1] + ey[2] * ey[2]);
+    g.kappa = to_df(kappa);
+    g.s_r = to_df(s_r);
+    g.bin_offset = bin_offset;
+    g.nx = nx;
+    g.ny = ny;
+    g.nz = nz;
+    g.tiles_x = (nx + 31) / 32;
+    g.tiles_y = (ny + 31) / 32;
+    return g;
+}
+
+// Minimum and maximum distance from point a to the parallelepiped
+// {o + u*ex + v*ey + w*ez : 0 <= u <= nu, 0 <= v <= nv, 0 <= w <= nw} with mutually orthogonal
+// (or zero) edge vectors; the minimum is exact for orthogonal edges, the maximum is over the
+// corners.  Used to bound the range window of the whole grid and of tile strips.
+static inline void box_distance_bounds(const double* a, const double* o, const double* ex,
+                                       const double* ey, const double* ez, double nu, double nv,
+                                       double nw, double* dmin, double* dmax) {
+    const double* e[3] = {ex, ey, ez};
+    const double n[3] = {nu, nv, nw};
+    double rel[3] = {a[0] - o[0], a[1] - o[1], a[2] - o[2]};
+    double closest[3] = {o[0], o[1], o[2]};
+    for (int ax = 0; ax < 3; ++ax) {
+        double ee = e[ax][0] * e[ax][0] + e[ax][1] * e[ax][1] + e[ax][2] * e[ax][2];
+        if (ee <= 0.0 || n[ax] <= 0.0) continue;
+        double t = (rel[0] * e[ax][0] + rel[1] * e[ax][1] + rel[2] * e[ax][2]) / ee;
+        if (t < 0.0) t = 0.0;
+        if (t > n[ax]) t = n[ax];
+        for (int c = 0; c < 3; ++c) closest[c] += t * e[ax][c];
+    }
+    *dmin = dist3(a, closest);
+    double best = 0.0;
+    for (int corner = 0; corner < 8; ++corner) {
+        double p[3] = {o[0], o[1], o[2]};
+        for (int ax = 0; ax < 3; ++ax) {
+            double t = (corner >> ax & 1) ? n[ax] : 0.0;
+            for (int c = 0; c < 3; ++c) p[c] += t * e[ax][c];
+        }
+        double d = dist3(a, p);
+        if (d > best) best = d;
+    }
+    *dmax = best;
+}
+
+}  // namespace sar

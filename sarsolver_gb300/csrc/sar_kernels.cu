@@ -1,0 +1,631 @@
+// sar_kernels.cu -- sm_103a kernels of the SAR operator pair.
+//
+//   K1  pack_adjoint / unpack_pairs    range-profile upsampling around a batched C2C FFT
+//                                      (replaces sarsolver_cxx.cpp:331-344)
+//   K2  bp_grid / bp_points            backprojection gather (replaces :345-350)
+//   K3  fp_grid / fp_points            forward scatter, the exact transpose of K2 (:284-291)
+//   K4  pack_forward / extract_forward range-profile downsampling around the FFT (:292-307)
+//
+// Layout in HBM: images are complex64 [nz][ny][nx]; phase histories complex64 [S][N] with
+// fast time fftshifted (the Python API's convention, forward.py:44); range profiles are kept
+// only over the bins the scene can reach, [S][Lg] starting at bin bg0, as float4
+// (value at the interpolation midpoint, difference to the next bin) so that one 16-byte
+// load gives a linearly interpolated sample.
+#include "sar_kernels.cuh"
+
+namespace sar {
+
+#define SAR_TWO_PI 6.28318530717958647692f
+
+__device__ __forceinline__ void raise_flag(unsigned* flags, unsigned bit) {
+    if (flags) atomicOr(flags, bit);
+}
+
+__device__ __forceinline__ PulseGeom load_pulse(const PulseGeom* p) {
+    const float4* v = reinterpret_cast<const float4*>(p);
+    const float4 a = __ldg(v), b = __ldg(v + 1), c = __ldg(v + 2), d = __ldg(v + 3);
+    PulseGeom g;
+    g.atx_hi[0] = a.x; g.atx_hi[1] = a.y; g.atx_hi[2] = a.z; g.atx_lo[0] = a.w;
+    g.atx_lo[1] = b.x; g.atx_lo[2] = b.y; g.arx_hi[0] = b.z; g.arx_hi[1] = b.w;
+    g.arx_hi[2] = c.x; g.arx_lo[0] = c.y; g.arx_lo[1] = c.z; g.arx_lo[2] = c.w;
+    g.rref_hi = d.x; g.rref_lo = d.y; g.monostatic = d.z; g.pad = d.w;
+    return g;
+}
+
+// ------------------------------------------------------------ tile bookkeeping
+// Thread layout of a 32x32 tile CTA: lane = column (i), warp w owns rows 4w .. 4w+3.
+// Sub-tile q (16x16) = (column >= 16) + 2 (row >= 16); offsets are relative to the
+// sub-tile anchor at (8, 8) inside it.
+struct TileThread {
+    int q;
+    float di, di2, di3;
+    float dj[4], dj2[4], dj3[4];
+};
+
+__device__ __forceinline__ TileThread tile_thread() {
+    TileThread t;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    t.q = (lane >= 16) + 2 * (warp >= 4);
+    t.di = (float)(lane - 8 - 16 * (lane >= 16));
+    t.di2 = t.di * t.di;
+    t.di3 = t.di2 * t.di;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const float d = (float)(4 * warp + r - 8 - 16 * (warp >= 4));
+        t.dj[r] = d;
+        t.dj2[r] = d * d;
+        t.dj3[r] = d * d * d;
+    }
+    return t;
+}
+
+__device__ __forceinline__ df3 subtile_anchor(int ti, int tj, int k, int q, const GridConst& g) {
+    return pixel_position(ti * kTile + 8 + 16 * (q & 1), tj * kTile + 8 + 16 * (q >> 1), k, g);
+}
+
+// One (pulse, sub-tile) coefficient set per thread of the first ceil(4 pb / 32) warps.
+// Coefficient sets are 4 float4: [c0 c1 c2 c3][c4 c5 c6 c7][c8 c9 v0 v1][v2 v3 v4 v5].
+// The tile's base bin (floor of the mean anchor bin) is agreed across the four lanes of a
+// pulse by shuffles, so all sub-tiles of a pulse share it.
+__device__ __forceinline__ void coeff_stage(const GridConst& g, const PulseGeom* __restrict__ pulses,
+                                            int s0, int npb, int pb, const df3* anchors,
+                                            float4* coef, int* base) {
+    const int t = threadIdx.x;
+    const int nthr = (4 * pb + 31) & ~31;
+    if (t >= nthr) return;
+    const int pi = t >> 2, q = t & 3;
+    const bool valid = (t < 4 * pb) && (pi < npb);
+    AnchorExpansion ae = {};
+    Coeffs co = {};
+    df vb = df_make(0.0f, 0.0f);
+    if (valid) {
+        const PulseGeom pg = load_pulse(pulses + s0 + pi);
+        ae = expand_anchor(anchors[q], pg, g);
+        phase_coeffs(ae, g, co.c);
+        vb = anchor_bin(ae, g);
+    }
+    const unsigned all = 0xffffffffu;
+    df sum = df_add(vb, df_make(__shfl_xor_sync(all, vb.hi, 1), __shfl_xor_sync(all, vb.lo, 1)));
+    sum = df_add(sum, df_make(__shfl_xor_sync(all, sum.hi, 2), __shfl_xor_sync(all, sum.lo, 2)));
+    int b = base_bin_of(sum, 4.0f);
+    b = __shfl_sync(all, b, (t & 31) & ~3);
+    if (valid) {
+        bin_coeffs(ae, vb, b, g, co.v);
+        float4* dst = coef + (pi * 4 + q) * 4;
+        dst[0] = make_float4(co.c[0], co.c[1], co.c[2], co.c[3]);
+        dst[1] = make_float4(co.c[4], co.c[5], co.c[6], co.c[7]);
+        dst[2] = make_float4(co.c[8], co.c[9], co.v[0], co.v[1]);
+        dst[3] = make_float4(co.v[2], co.v[3], co.v[4], co.v[5]);
+        if (q == 0) base[pi] = b;
+    }
+}
+
+struct PixelEval {
+    float f;    // phase, cycles in [-0.5, 0.5]
+    float sf;   // interpolation coordinate in [-0.5, 0.5] about bin n
+    int n;      // bin relative to the tile's base bin
+};
+
+__device__ __forceinline__ ColumnTerms load_column(const float4* cs, const TileThread& tt, float& c9,
+                                                   float& v5) {
+    const float4 A = cs[0], B = cs[1], C = cs[2], D = cs[3];
+    Coeffs co;
+    co.c[0] = A.x; co.c[1] = A.y; co.c[2] = A.z; co.c[3] = A.w;
+    co.c[4] = B.x; co.c[5] = B.y; co.c[6] = B.z; co.c[7] = B.w;
+    co.c[8] = C.x; co.c[9] = C.y; co.v[0] = C.z; co.v[1] = C.w;
+    co.v[2] = D.x; co.v[3] = D.y; co.v[4] = D.z; co.v[5] = D.w;
+    c9 = co.c[9];
+    v5 = co.v[5];
+    return column_terms(co, tt.di, tt.di2, tt.di3);
+}
+
+__device__ __forceinline__ PixelEval eval_pixel(const ColumnTerms& ct, float c9, float v5,
+                                                const TileThread& tt, int r) {
+    PixelEval e;
+    const float ph = pixel_phase(ct, c9, tt.dj[r], tt.dj2[r], tt.dj3[r]);
+    e.f = ph - round_shift(ph);
+    const float v = pixel_bin(ct, v5, tt.dj[r], tt.dj2[r]);
+    const float rr = v + SAR_SHIFTER;
+    e.sf = v - (rr - SAR_SHIFTER);
+    e.n = __float_as_int(rr) - SAR_SHIFTER_BITS;
+    return e;
+}
+
+// ------------------------------------------------------------------- K2 (grid)
+size_t bp_grid_smem_bytes(int wwin, int pb, int staged) {
+    size_t f4 = (staged ? (size_t)pb * wwin : 0) + (size_t)pb * 16 + (size_t)((pb + 3) / 4) + 6;
+    return f4 * sizeof(float4);
+}
+
+template <bool STAGED>
+__global__ void __launch_bounds__(kThreads, 2) bp_grid_kernel(const BpGridArgs a) {
+    extern __shared__ float4 smem[];
+    const int pb = a.pb;
+    float4* win = smem;
+    float4* coef = smem + (STAGED ? pb * a.wwin : 0);
+    int* base = reinterpret_cast<int*>(coef + pb * 16);
+    df3* anchors = reinterpret_cast<df3*>(base + ((pb + 3) & ~3));
+
+    const GridConst& g = a.g;
+    int tile = blockIdx.x;
+    const int ti = tile % g.tiles_x;
+    tile /= g.tiles_x;
+    const int tj = tile % g.tiles_y;
+    const int k = tile / g.tiles_y;
+    const TileThread tt = tile_thread();
+    if (threadIdx.x < 4) anchors[threadIdx.x] = subtile_anchor(ti, tj, k, threadIdx.x, g);
+
+    float acc_re[4] = {0.f, 0.f, 0.f, 0.f}, acc_im[4] = {0.f, 0.f, 0.f, 0.f};
+    const int half_w = a.wwin / 2;
+    for (int s0 = 0; s0 < a.S; s0 += pb) {
+        const int npb = min(pb, a.S - s0);
+        __syncthreads();
+        coeff_stage(g, a.pulses, s0, npb, pb, anchors, coef, base);
+        __syncthreads();
+        if (STAGED) {
+            for (int e = threadIdx.x; e < npb * a.wwin; e += kThreads) {
+                const int pi = e / a.wwin;
+                const int w = e - pi * a.wwin;
+                long gi = (long)base[pi] - half_w - a.bg0 + w;
+                if (gi < 0 || gi >= a.Lg) {
+                    raise_flag(a.flags, FLAG_TILE_WINDOW);
+                    gi = gi < 0 ? 0 : a.Lg - 1;
+                }
+                win[e] = __ldg(a.pairs + (size_t)(s0 + pi) * a.Lg + gi);
+            }
+            __syncthreads();
+        }
+        float st_re[4] = {0.f, 0.f, 0.f, 0.f}, st_im[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int pi = 0; pi < npb; ++pi) {
+            float c9, v5;
+            const ColumnTerms ct = load_column(coef + (pi * 4 + tt.q) * 4, tt, c9, v5);
+            const float4* wp = win + pi * a.wwin;
+            const float4* gp = a.pairs + (size_t)(s0 + pi) * a.Lg;
+            const int bb = base[pi] - a.bg0;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const PixelEval e = eval_pixel(ct, c9, v5, tt, r);
+                float4 pv;
+                if (STAGED) {
+                    const unsigned idx = min((unsigned)(e.n + half_w), (unsigned)(a.wwin - 1));
+                    pv = wp[idx];
+                } else {
+                    const int gi = min(max(bb + e.n, 0), a.Lg - 1);
+                    pv = __ldg(gp + gi);
+                }
+                const float re = fmaf(e.sf, pv.z, pv.x);
+                const float im = fmaf(e.sf, pv.w, pv.y);
+                float sn, cn;
+                __sincosf(SAR_TWO_PI * e.f, &sn, &cn);
+                // x += value * exp(-2 pi i f)
+                st_re[r] = fmaf(re, cn, fmaf(im, sn, st_re[r]));
+                st_im[r] = fmaf(im, cn, fmaf(-re, sn, st_im[r]));
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            acc_re[r] += st_re[r];
+            acc_im[r] += st_im[r];
+        }
+    }
+    const int i = ti * kTile + (threadIdx.x & 31);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int j = tj * kTile + 4 * (threadIdx.x >> 5) + r;
+        if (i < g.nx && j < g.ny) {
+            const size_t p = ((size_t)k * g.ny + j) * g.nx + i;
+            float2 o = make_float2(acc_re[r], acc_im[r]);
+            if (a.accumulate) {
+                const float2 old = a.x[p];
+                o.x += old.x;
+                o.y += old.y;
+            }
+            a.x[p] = o;
+        }
+    }
+}
+
+cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st) {
+    const size_t smem = bp_grid_smem_bytes(a.wwin, a.pb, a.staged);
+    const unsigned blocks = (unsigned)(a.g.tiles_x * a.g.tiles_y * a.g.nz);
+    cudaError_t e;
+    if (a.staged) {
+        e = cudaFuncSetAttribute(bp_grid_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        bp_grid_kernel<true><<<blocks, kThreads, smem, st>>>(a);
+    } else {
+        e = cudaFuncSetAttribute(bp_grid_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        bp_grid_kernel<false><<<blocks, kThreads, smem, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------- K3 (grid)
+// CTA = (strip segment of tiles along y, block of pbf pulses).  Contributions of the
+// segment's tiles are accumulated in a shared-memory window per pulse that covers the
+// segment's whole range extent, then merged into the global profile accumulator with one
+// atomic add per bin.  Each pixel uses the identical coefficient sets, bin and weights as
+// K2, so the pair is an exact transpose up to FP32 summation order.
+size_t fp_grid_smem_bytes(int ws, int pbf) {
+    size_t f4 = (size_t)pbf * ws / 2 + (size_t)pbf * 16 + (size_t)((2 * pbf + 3) / 4) + 6;
+    return f4 * sizeof(float4);
+}
+
+template <bool LINEAR>
+__global__ void __launch_bounds__(kThreads, 2) fp_grid_kernel(const FpGridArgs a) {
+    extern __shared__ float4 smem[];
+    const int pbf = a.pbf;
+    float2* win = reinterpret_cast<float2*>(smem);
+    float4* coef = smem + (pbf * a.ws) / 2;
+    int* base = reinterpret_cast<int*>(coef + pbf * 16);
+    int* wst = base + pbf;
+    df3* anchors = reinterpret_cast<df3*>(base + ((2 * pbf + 3) & ~3));
+
+    const GridConst& g = a.g;
+    int b = blockIdx.x;
+    const int seg = b % a.segs_per_column;
+    b /= a.segs_per_column;
+    const int ti = b % g.tiles_x;
+    const int k = b / g.tiles_x;
+    const int strip = (k * g.tiles_x + ti) * a.segs_per_column + seg;
+    const int s0 = blockIdx.y * pbf;
+    const int npb = min(pbf, a.S - s0);
+    const int tj0 = seg * a.seg_tiles;
+    const int tj1 = min(tj0 + a.seg_tiles, g.tiles_y);
+    const TileThread tt = tile_thread();
+
+    for (int e = threadIdx.x; e < pbf * a.ws; e += kThreads) win[e] = make_float2(0.f, 0.f);
+    if (threadIdx.x < npb) wst[threadIdx.x] = a.strip_start[(size_t)strip * a.S + s0 + threadIdx.x];
+    const int i = ti * kTile + (threadIdx.x & 31);
+
+    for (int tj = tj0; tj < tj1; ++tj) {
+        __syncthreads();
+        if (threadIdx.x < 4) anchors[threadIdx.x] = subtile_anchor(ti, tj, k, threadIdx.x, g);
+        float2 xv[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int j = tj * kTile + 4 * (threadIdx.x >> 5) + r;
+            xv[r] = (i < g.nx && j < g.ny) ? a.x[((size_t)k * g.ny + j) * g.nx + i] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        coeff_stage(g, a.pulses, s0, npb, pbf, anchors, coef, base);
+        __syncthreads();
+        for (int pi = 0; pi < npb; ++pi) {
+            float c9, v5;
+            const ColumnTerms ct = load_column(coef + (pi * 4 + tt.q) * 4, tt, c9, v5);
+            float2* wp = win + pi * a.ws;
+            const int off = base[pi] - wst[pi];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const PixelEval e = eval_pixel(ct, c9, v5, tt, r);
+                float sn, cn;
+                __sincosf(SAR_TWO_PI * e.f, &sn, &cn);
+                // contribution x * exp(+2 pi i f)
+                const float cr = xv[r].x * cn - xv[r].y * sn;
+                const float ci = fmaf(xv[r].x, sn, xv[r].y * cn);
+                const unsigned idx = min((unsigned)(e.n + off), (unsigned)(a.ws - 2));
+                if (LINEAR) {
+                    const float w0 = 0.5f - e.sf, w1 = 0.5f + e.sf;
+                    atomicAdd(&wp[idx].x, w0 * cr);
+                    atomicAdd(&wp[idx].y, w0 * ci);
+                    atomicAdd(&wp[idx + 1].x, w1 * cr);
+                    atomicAdd(&wp[idx + 1].y, w1 * ci);
+                } else {
+                    atomicAdd(&wp[idx].x, cr);
+                    atomicAdd(&wp[idx].y, ci);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < npb * a.ws; e += kThreads) {
+        const int pi = e / a.ws;
+        const int w = e - pi * a.ws;
+        const float2 v = win[e];
+        if (v.x == 0.f && v.y == 0.f) continue;
+        const long gi = (long)wst[pi] + w - a.bg0;
+        if (gi < 0 || gi >= a.Lg) {
+            raise_flag(a.flags, FLAG_STRIP_WINDOW);
+            continue;
+        }
+        float2* dst = a.acc + (size_t)(s0 + pi) * a.Lg + gi;
+        atomicAdd(&dst->x, v.x);
+        atomicAdd(&dst->y, v.y);
+    }
+}
+
+cudaError_t launch_fp_grid(const FpGridArgs& a, cudaStream_t st) {
+    const int linear = a.linear;
+    const size_t smem = fp_grid_smem_bytes(a.ws, a.pbf);
+    const dim3 grid((unsigned)(a.segs_per_column * a.g.tiles_x * a.g.nz), (unsigned)((a.S + a.pbf - 1) / a.pbf));
+    cudaError_t e;
+    if (linear) {
+        e = cudaFuncSetAttribute(fp_grid_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        fp_grid_kernel<true><<<grid, kThreads, smem, st>>>(a);
+    } else {
+        e = cudaFuncSetAttribute(fp_grid_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        fp_grid_kernel<false><<<grid, kThreads, smem, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------- K2 / K3 (points)
+constexpr int kPointThreads = 256;
+constexpr int kPointPulses = 64;
+
+__device__ __forceinline__ PointGeom load_point(const PointGeom* p) {
+    const float4* v = reinterpret_cast<const float4*>(p);
+    const float4 h = __ldg(v), l = __ldg(v + 1);
+    PointGeom g;
+    g.qh[0] = h.x; g.qh[1] = h.y; g.qh[2] = h.z; g.qh[3] = h.w;
+    g.ql[0] = l.x; g.ql[1] = l.y; g.ql[2] = l.z; g.ql[3] = l.w;
+    return g;
+}
+
+struct PointEval {
+    float f, sf;
+    int gi;
+};
+
+__device__ __forceinline__ PointEval eval_point(const PointArgs& a, const PulseGeom& pg, float4 a2,
+                                                const PointGeom& pt) {
+    df r = point_range(pulse_tx(pg), df_make(a2.x, a2.y), pt);
+    if (pg.monostatic != 0.0f)
+        r = df_mulf(r, 2.0f);
+    else
+        r = df_add(r, point_range(pulse_rx(pg), df_make(a2.z, a2.w), pt));
+    r = df_sub(r, df_make(pg.rref_hi, pg.rref_lo));
+    PointEval e;
+    e.f = df_frac(df_mul(a.kappa, r));
+    const df V = df_sub(df_mul(a.s_r, r), df_make((float)a.bg0, 0.0f));
+    const float tail = V.lo + a.bin_offset;
+    const float n = round_shift(V.hi + tail);
+    e.sf = (V.hi - n) + tail;
+    e.gi = min(max((int)n, 0), a.Lg - 2);
+    return e;
+}
+
+__global__ void __launch_bounds__(kPointThreads) bp_points_kernel(const PointArgs a, const float4* __restrict__ pairs,
+                                                                  float2* x, int accumulate) {
+    __shared__ PulseGeom sp[kPointPulses];
+    __shared__ float4 sa2[kPointPulses];
+    const int p = blockIdx.x * kPointThreads + threadIdx.x;
+    PointGeom pt = {};
+    if (p < a.P) pt = load_point(a.points + p);
+    float ar = 0.f, ai = 0.f;
+    for (int s0 = 0; s0 < a.S; s0 += kPointPulses) {
+        const int n = min(kPointPulses, a.S - s0);
+        __syncthreads();
+        for (int e = threadIdx.x; e < n; e += kPointThreads) {
+            sp[e] = load_pulse(a.pulses + s0 + e);
+            sa2[e] = __ldg(a.alpha2 + s0 + e);
+        }
+        __syncthreads();
+        float sr = 0.f, si = 0.f;
+        for (int j = 0; j < n; ++j) {
+            const PointEval e = eval_point(a, sp[j], sa2[j], pt);
+            const float4 pv = __ldg(pairs + (size_t)(s0 + j) * a.Lg + e.gi);
+            const float re = fmaf(e.sf, pv.z, pv.x), im = fmaf(e.sf, pv.w, pv.y);
+            float sn, cn;
+            __sincosf(SAR_TWO_PI * e.f, &sn, &cn);
+            sr = fmaf(re, cn, fmaf(im, sn, sr));
+            si = fmaf(im, cn, fmaf(-re, sn, si));
+        }
+        ar += sr;
+        ai += si;
+    }
+    if (p < a.P) {
+        float2 o = make_float2(ar, ai);
+        if (accumulate) {
+            o.x += x[p].x;
+            o.y += x[p].y;
+        }
+        x[p] = o;
+    }
+}
+
+template <bool LINEAR>
+__global__ void __launch_bounds__(kPointThreads) fp_points_kernel(const PointArgs a, const float2* __restrict__ x,
+                                                                  float2* acc) {
+    __shared__ PulseGeom sp[kPointPulses];
+    __shared__ float4 sa2[kPointPulses];
+    const int p = blockIdx.x * kPointThreads + threadIdx.x;
+    const int s0 = blockIdx.y * kPointPulses;
+    const int n = min(kPointPulses, a.S - s0);
+    for (int e = threadIdx.x; e < n; e += kPointThreads) {
+        sp[e] = load_pulse(a.pulses + s0 + e);
+        sa2[e] = __ldg(a.alpha2 + s0 + e);
+    }
+    __syncthreads();
+    if (p >= a.P) return;
+    const PointGeom pt = load_point(a.points + p);
+    const float2 xv = x[p];
+    for (int j = 0; j < n; ++j) {
+        const PointEval e = eval_point(a, sp[j], sa2[j], pt);
+        float sn, cn;
+        __sincosf(SAR_TWO_PI * e.f, &sn, &cn);
+        const float cr = xv.x * cn - xv.y * sn;
+        const float ci = fmaf(xv.x, sn, xv.y * cn);
+        float2* dst = acc + (size_t)(s0 + j) * a.Lg + e.gi;
+        if (LINEAR) {
+            const float w0 = 0.5f - e.sf, w1 = 0.5f + e.sf;
+            atomicAdd(&dst[0].x, w0 * cr);
+            atomicAdd(&dst[0].y, w0 * ci);
+            atomicAdd(&dst[1].x, w1 * cr);
+            atomicAdd(&dst[1].y, w1 * ci);
+        } else {
+            atomicAdd(&dst[0].x, cr);
+            atomicAdd(&dst[0].y, ci);
+        }
+    }
+}
+
+cudaError_t launch_bp_points(const PointArgs& a, const float4* pairs, float2* x, int accumulate, cudaStream_t st) {
+    const unsigned blocks = (unsigned)((a.P + kPointThreads - 1) / kPointThreads);
+    bp_points_kernel<<<blocks, kPointThreads, 0, st>>>(a, pairs, x, accumulate);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fp_points(const PointArgs& a, const float2* x, float2* acc, cudaStream_t st) {
+    const dim3 grid((unsigned)((a.P + kPointThreads - 1) / kPointThreads), (unsigned)((a.S + kPointPulses - 1) / kPointPulses));
+    if (a.linear)
+        fp_points_kernel<true><<<grid, kPointThreads, 0, st>>>(a, x, acc);
+    else
+        fp_points_kernel<false><<<grid, kPointThreads, 0, st>>>(a, x, acc);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------- K1 / K4
+__device__ __forceinline__ long pos_mod(long a, long m) {
+    long r = a % m;
+    return r < 0 ? r + m : r;
+}
+
+// spec[row][m] = conj(W[i]) y_fft[i] placed at the zero-padded position of FFT index i
+// (sarsolver_cxx.cpp:331-342); y is read from its fftshifted layout.
+__global__ void pack_adjoint_kernel(const float2* __restrict__ y, const float2* __restrict__ wave,
+                                    float2* __restrict__ spec, int N, long M, int first) {
+    const long m = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    const long row = blockIdx.y;
+    const int half = N / 2;
+    int i = -1;
+    if (m < half)
+        i = (int)m;
+    else if (m >= M - half)
+        i = (int)(N - M + m);
+    else if ((N & 1) && m == half)
+        i = half;
+    float2 v = make_float2(0.f, 0.f);
+    if (i >= 0) {
+        const float2 yv = y[(size_t)(first + row) * N + (i + half) % N];
+        const float2 w = __ldg(wave + i);
+        v = make_float2(w.x * yv.x + w.y * yv.y, w.x * yv.y - w.y * yv.x);
+    }
+    spec[row * M + m] = v;
+}
+
+// pairs[s][w] for bin b = bg0 + w: (p(b) + 0.5 d, d) with d = p(b+1) - p(b), both scaled by
+// the pulse factor (linear); (p(b), 0) for nearest-bin sampling.  Bins wrap modulo M
+// (sarsolver_cxx.cpp:22-24).
+__global__ void unpack_pairs_kernel(const float2* __restrict__ spec, const float2* __restrict__ wfac,
+                                    float4* __restrict__ pairs, long M, int Lg, long bg0, int first,
+                                    int linear) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= Lg) return;
+    const long row = blockIdx.y;
+    const long m0 = pos_mod(bg0 + w, M);
+    const long m1 = (m0 + 1 == M) ? 0 : m0 + 1;
+    const float2 f = __ldg(wfac + first + row);
+    const float2 a = spec[row * M + m0];
+    const float2 p0 = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
+    float4 out;
+    if (linear) {
+        const float2 b = spec[row * M + m1];
+        const float2 p1 = make_float2(b.x * f.x - b.y * f.y, b.x * f.y + b.y * f.x);
+        const float dx = p1.x - p0.x, dy = p1.y - p0.y;
+        out = make_float4(fmaf(0.5f, dx, p0.x), fmaf(0.5f, dy, p0.y), dx, dy);
+    } else {
+        out = make_float4(p0.x, p0.y, 0.f, 0.f);
+    }
+    pairs[(size_t)(first + row) * Lg + w] = out;
+}
+
+__global__ void unpack_profiles_kernel(const float2* __restrict__ spec, float2* __restrict__ prof, long M,
+                                       int Lg, long bg0, int first) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= Lg) return;
+    const long row = blockIdx.y;
+    prof[(size_t)(first + row) * Lg + w] = spec[row * M + pos_mod(bg0 + w, M)];
+}
+
+// spec[row][m] = sum of accumulated bins congruent to m modulo M.
+__global__ void pack_forward_kernel(const float2* __restrict__ acc, float2* __restrict__ spec, long M, int Lg,
+                                    long bg0, int first) {
+    const long m = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    const long row = blockIdx.y;
+    float2 s = make_float2(0.f, 0.f);
+    for (long w = pos_mod(m - bg0, M); w < Lg; w += M) {
+        const float2 v = acc[(size_t)(first + row) * Lg + w];
+        s.x += v.x;
+        s.y += v.y;
+    }
+    spec[row * M + m] = s;
+}
+
+// y_fft[i] = W[i] K[i] (low half), W[N-1-i] K[M-1-i] (high half), odd middle
+// (sarsolver_cxx.cpp:295-307), times the pulse factor, written fftshifted (forward.py:44).
+__global__ void extract_forward_kernel(const float2* __restrict__ spec, const float2* __restrict__ wave,
+                                       const float2* __restrict__ wfac, float2* __restrict__ y, int N, long M,
+                                       int first) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const long row = blockIdx.y;
+    const int half = N / 2;
+    long m;
+    if (i < half)
+        m = i;
+    else if (i >= N - half)
+        m = M - N + i;
+    else
+        m = half;
+    const float2 k = spec[row * M + m];
+    const float2 w = __ldg(wave + i);
+    const float2 f = __ldg(wfac + first + row);
+    const float2 a = make_float2(w.x * k.x - w.y * k.y, w.x * k.y + w.y * k.x);
+    y[(size_t)(first + row) * N + (i + half) % N] = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
+}
+
+__global__ void weights_kernel(const float2* __restrict__ w, float2* wadj, float2* wfwd, int S, int conj_adjoint) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    const float2 v = w[s];
+    wfwd[s] = v;
+    wadj[s] = conj_adjoint ? make_float2(v.x, -v.y) : v;
+}
+
+cudaError_t launch_pack_adjoint(const float2* y, const float2* wave, float2* spec, int N, long M, int rows,
+                                int first, cudaStream_t st) {
+    const dim3 grid((unsigned)((M + 255) / 256), (unsigned)rows);
+    pack_adjoint_kernel<<<grid, 256, 0, st>>>(y, wave, spec, N, M, first);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_pairs(const float2* spec, const float2* wfac, float4* pairs, long M, int Lg, long bg0,
+                                int rows, int first, int linear, cudaStream_t st) {
+    const dim3 grid((unsigned)((Lg + 255) / 256), (unsigned)rows);
+    unpack_pairs_kernel<<<grid, 256, 0, st>>>(spec, wfac, pairs, M, Lg, bg0, first, linear);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_unpack_profiles(const float2* spec, float2* prof, long M, int Lg, long bg0, int rows, int first,
+                                   cudaStream_t st) {
+    const dim3 grid((unsigned)((Lg + 255) / 256), (unsigned)rows);
+    unpack_profiles_kernel<<<grid, 256, 0, st>>>(spec, prof, M, Lg, bg0, first);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_forward(const float2* acc, float2* spec, long M, int Lg, long bg0, int rows, int first,
+                                cudaStream_t st) {
+    const dim3 grid((unsigned)((M + 255) / 256), (unsigned)rows);
+    pack_forward_kernel<<<grid, 256, 0, st>>>(acc, spec, M, Lg, bg0, first);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_extract_forward(const float2* spec, const float2* wave, const float2* wfac, float2* y, int N,
+                                   long M, int rows, int first, cudaStream_t st) {
+    const dim3 grid((unsigned)((N + 255) / 256), (unsigned)rows);
+    extract_forward_kernel<<<grid, 256, 0, st>>>(spec, wave, wfac, y, N, M, first);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_weights(const float2* w, float2* wadj, float2* wfwd, int S, int conj_adjoint, cudaStream_t st) {
+    weights_kernel<<<(S + 255) / 256, 256, 0, st>>>(w, wadj, wfwd, S, conj_adjoint);
+    return cudaGetLastError();
+}
+
+}  // namespace sar

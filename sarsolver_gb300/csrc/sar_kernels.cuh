@@ -1,0 +1,85 @@
+// sar_kernels.cuh -- launch interface of the SAR kernels (sar_kernels.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "sar_geom.cuh"
+
+namespace sar {
+
+// Device check flags (OR-ed into a plan-owned word; read back by sar_device_flags()).
+enum : unsigned {
+    FLAG_TILE_WINDOW = 1u,    // a tile's staged window left the stored profile span
+    FLAG_STRIP_WINDOW = 2u,   // a forward strip window left the stored profile span
+    FLAG_BIN_CLAMP = 4u,      // a per-pixel bin index was clamped (debug builds only)
+};
+
+constexpr int kTile = 32;          // pixels per tile side
+constexpr int kThreads = 256;      // threads per tile CTA: 32 columns x 8 warps, 4 rows each
+constexpr int kMaxStagePulses = 32;
+
+// Backprojection over a regular grid (K2).
+struct BpGridArgs {
+    GridConst g;
+    const PulseGeom* pulses;   // [S]
+    const float4* pairs;       // [S][Lg]: (value at mid-bin, difference) per bin
+    float2* x;                 // [P] image, (k*ny + j)*nx + i
+    unsigned* flags;
+    int S, Lg, bg0;            // stored profile span: bins [bg0, bg0 + Lg)
+    int wwin;                  // staged window per (tile, pulse), multiple of 4
+    int pb;                    // pulses per stage (multiple of 8, <= 32)
+    int staged;                // 1: stage windows in shared memory; 0: read global directly
+    int accumulate;            // 1: x += result
+};
+size_t bp_grid_smem_bytes(int wwin, int pb, int staged);
+cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st);
+
+// Forward projection over a regular grid (K3): scatter into strip windows, merge globally.
+struct FpGridArgs {
+    GridConst g;
+    const PulseGeom* pulses;   // [S]
+    const float2* x;           // [P]
+    float2* acc;               // [S][Lg] profile accumulator (pre-zeroed)
+    const int* strip_start;    // [n_strips][S] first bin of each strip window
+    unsigned* flags;
+    int S, Lg, bg0;
+    int seg_tiles;             // tiles per strip segment (along y)
+    int segs_per_column;       // ceil(tiles_y / seg_tiles)
+    int ws;                    // strip window length (bins), multiple of 32
+    int pbf;                   // pulses per CTA (multiple of 8, <= 32)
+    int linear;                // 1: linear interpolation weights; 0: nearest bin
+};
+size_t fp_grid_smem_bytes(int ws, int pbf);
+cudaError_t launch_fp_grid(const FpGridArgs& a, cudaStream_t st);
+
+// Unstructured positions (K2/K3 point variants).
+struct PointArgs {
+    const PulseGeom* pulses;   // [S]
+    const float4* alpha2;      // [S]: |tx-o|^2 (hi, lo), |rx-o|^2 (hi, lo)
+    const PointGeom* points;   // [P]
+    df kappa, s_r;
+    float bin_offset;
+    int S, P, Lg, bg0;
+    int linear;                // forward scatter weights: 1 linear, 0 nearest bin
+    unsigned* flags;
+};
+cudaError_t launch_bp_points(const PointArgs& a, const float4* pairs, float2* x, int accumulate,
+                             cudaStream_t st);
+cudaError_t launch_fp_points(const PointArgs& a, const float2* x, float2* acc, cudaStream_t st);
+
+// FFT-side kernels (K1 / K4).  y is [S][N] fftshifted along fast time; spec is [rows][M].
+cudaError_t launch_pack_adjoint(const float2* y, const float2* wave, float2* spec, int N, long M,
+                                int rows, int first, cudaStream_t st);
+cudaError_t launch_unpack_pairs(const float2* spec, const float2* wfac, float4* pairs, long M,
+                                int Lg, long bg0, int rows, int first, int linear, cudaStream_t st);
+cudaError_t launch_unpack_profiles(const float2* spec, float2* prof, long M, int Lg, long bg0,
+                                   int rows, int first, cudaStream_t st);
+cudaError_t launch_pack_forward(const float2* acc, float2* spec, long M, int Lg, long bg0, int rows,
+                                int first, cudaStream_t st);
+cudaError_t launch_extract_forward(const float2* spec, const float2* wave, const float2* wfac,
+                                   float2* y, int N, long M, int rows, int first, cudaStream_t st);
+cudaError_t launch_weights(const float2* w, float2* wadj, float2* wfwd, int S, int conj_adjoint,
+                           cudaStream_t st);
+
+}  // namespace sar

@@ -1,0 +1,227 @@
+"""Scene and aperture descriptions (host-side metadata of the operator).
+
+These mirror the reference's concrete classes so code written against sarsolver keeps working:
+  GridSarScene, SimpleSarScene     src/sarsolver/numpy/hypothesis.py:10-267
+  NumpySimpleSarAperture           src/sarsolver/numpy/measurement.py:13-241
+  NumpySimpleSarDataset            src/sarsolver/numpy/measurement.py:244-290
+The operator also accepts the reference's own objects (duck typing on the same attributes).
+Grid sizing from k-space (``GridSarScene.from_aperture``) and dataset resampling are not part of
+this package.
+"""
+from __future__ import annotations
+
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+C = 299792458.0
+
+
+class SimpleSarScene:
+    """Point scatterers at arbitrary positions [P, 3] (numpy/hypothesis.py:10-70)."""
+
+    def __init__(self, scatterer_positions: np.ndarray):
+        self._scatterer_positions = np.asarray(scatterer_positions)
+        self._num_scatterers = self._scatterer_positions.shape[0]
+
+    @property
+    def positions(self) -> np.ndarray:
+        return self._scatterer_positions
+
+    @property
+    def num_scatterers(self) -> int:
+        return self._num_scatterers
+
+    def to_blocks(self, num_blocks: int = 1) -> List["SimpleSarScene"]:
+        if num_blocks == 1:
+            return [self]
+        n = self.num_scatterers // num_blocks
+        out = []
+        for b in range(num_blocks):
+            hi = self.num_scatterers if b == num_blocks - 1 else (b + 1) * n
+            out.append(SimpleSarScene(self.positions[b * n:hi, :]))
+        return out
+
+
+class GridSarScene:
+    """Regular grid of scatterers (numpy/hypothesis.py:73-206).
+
+    grid_shape and grid_dimensions are in (z, y, x) order; pixel (k, j, i) sits at
+    ``rotation_matrix @ (x_i, y_j, z_k) + grid_centre`` with x_i = linspace(-lx/2, lx/2, nx)[i];
+    the flattened index is (k*ny + j)*nx + i.
+    """
+
+    def __init__(self, grid_shape: Sequence[int], grid_dimensions: Sequence[float],
+                 grid_centre: Optional[np.ndarray] = None, rotation_matrix: Optional[np.ndarray] = None):
+        self._grid_centre = np.zeros(3) if grid_centre is None else np.asarray(grid_centre, dtype=np.float64)
+        self._rotation_matrix = np.identity(3) if rotation_matrix is None else np.asarray(rotation_matrix, np.float64)
+        self._grid_shape = [int(v) for v in grid_shape]
+        self._grid_dimensions = [float(v) for v in grid_dimensions]
+
+    @property
+    def num_scatterers(self) -> int:
+        return int(np.prod(np.array(self.grid_shape)))
+
+    @property
+    def rotation_matrix(self) -> np.ndarray:
+        return self._rotation_matrix
+
+    @property
+    def grid_centre(self) -> np.ndarray:
+        return self._grid_centre
+
+    @property
+    def grid_dimensions(self) -> Sequence[float]:
+        return self._grid_dimensions
+
+    @property
+    def grid_shape(self) -> Sequence[int]:
+        return self._grid_shape
+
+    @property
+    def positions(self) -> np.ndarray:
+        xs = np.linspace(-0.5 * self.grid_dimensions[2], 0.5 * self.grid_dimensions[2], self.grid_shape[2])
+        ys = np.linspace(-0.5 * self.grid_dimensions[1], 0.5 * self.grid_dimensions[1], self.grid_shape[1])
+        zs = np.linspace(-0.5 * self.grid_dimensions[0], 0.5 * self.grid_dimensions[0], self.grid_shape[0])
+        zz, yy, xx = np.meshgrid(zs, ys, xs, indexing="ij")
+        base = np.stack([xx.reshape(-1), yy.reshape(-1), zz.reshape(-1)], axis=-1)
+        return (self.rotation_matrix @ base.T).T + self.grid_centre[None, :]
+
+    def to_blocks(self, num_blocks: int = 1) -> List:
+        if num_blocks == 1:
+            return [self]
+        return SimpleSarScene(self.positions).to_blocks(num_blocks)
+
+
+def grid_axes(scene) -> Optional[Tuple[Tuple[int, int, int], np.ndarray, np.ndarray, np.ndarray, np.ndarray]]:
+    """(shape (nz, ny, nx), origin, step_x, step_y, step_z) of a regular-grid scene, else None.
+
+    Works on any object with the GridSarScene attributes, including the reference's own.
+    """
+    needed = ("grid_shape", "grid_dimensions", "grid_centre", "rotation_matrix")
+    if not all(hasattr(scene, a) for a in needed):
+        return None
+    shape = tuple(int(v) for v in scene.grid_shape)
+    dims = [float(v) for v in scene.grid_dimensions]
+    rot = np.asarray(scene.rotation_matrix, dtype=np.float64)
+    centre = np.asarray(scene.grid_centre, dtype=np.float64).reshape(3)
+    nz, ny, nx = shape
+    first = np.array([-0.5 * dims[2], -0.5 * dims[1], -0.5 * dims[0]])
+    step = np.array([dims[2] / (nx - 1) if nx > 1 else 0.0,
+                     dims[1] / (ny - 1) if ny > 1 else 0.0,
+                     dims[0] / (nz - 1) if nz > 1 else 0.0])
+    origin = rot @ first + centre
+    return shape, origin, rot[:, 0] * step[0], rot[:, 1] * step[1], rot[:, 2] * step[2]
+
+
+class NumpySimpleSarAperture:
+    """Bistatic scalar SAR collection (numpy/measurement.py:13-241)."""
+
+    def __init__(self, trans_posns: np.ndarray, rec_posns: np.ndarray, srps: np.ndarray, centre_freq: float,
+                 sample_freq: float, waveform_fft: Optional[np.ndarray] = None,
+                 slow_time_weighting: Optional[np.ndarray] = None, num_freqs: Optional[int] = None,
+                 sign_multiplier: float = 1.0, c_eff: float = C):
+        self._transmitter_positions = np.asarray(trans_posns)
+        self._receiver_positions = np.asarray(rec_posns)
+        self._stab_ref_posns = np.asarray(srps)
+        self._centre_freq = centre_freq
+        self._sample_bandwidth = sample_freq
+        self._sign_multiplier = sign_multiplier
+        self._c_eff = c_eff
+        if waveform_fft is None:
+            if num_freqs is None:
+                raise ValueError("Number of frequencies needs to be set somehow")
+            waveform_fft = np.ones(num_freqs, dtype=np.complex128)
+        self._waveform_fft = np.asarray(waveform_fft)
+        self._num_freqs = self._waveform_fft.shape[0]
+        self._num_slow_times = self._transmitter_positions.shape[0]
+        if slow_time_weighting is None:
+            slow_time_weighting = np.ones(self._num_slow_times, dtype=np.complex128)
+        self._slow_time_weighting = np.asarray(slow_time_weighting)
+
+    @property
+    def num_slow_times(self) -> int:
+        return self._num_slow_times
+
+    @property
+    def num_freqs(self) -> int:
+        return self._num_freqs
+
+    @property
+    def centre_frequency(self) -> float:
+        return self._centre_freq
+
+    @property
+    def sample_bandwidth(self) -> float:
+        return self._sample_bandwidth
+
+    @property
+    def freqs(self) -> np.ndarray:
+        return self.centre_frequency + np.fft.fftshift(np.fft.fftfreq(self.num_freqs, 1.0 / self.sample_bandwidth))
+
+    @property
+    def transmitter_positions(self) -> np.ndarray:
+        return self._transmitter_positions
+
+    @property
+    def receiver_positions(self) -> np.ndarray:
+        return self._receiver_positions
+
+    @property
+    def stab_ref_posns(self) -> np.ndarray:
+        return self._stab_ref_posns
+
+    @property
+    def waveform_fft(self) -> np.ndarray:
+        return self._waveform_fft
+
+    @property
+    def slow_time_weighting(self) -> np.ndarray:
+        return self._slow_time_weighting
+
+    @property
+    def sign_multiplier(self) -> float:
+        return self._sign_multiplier
+
+    @property
+    def c_eff(self) -> float:
+        return self._c_eff
+
+    @property
+    def bad_slow_times(self) -> List[int]:
+        """Slow times with a non-finite position (base/measurement.py:325-339)."""
+        bad = set()
+        for arr in (self.transmitter_positions, self.receiver_positions, self.stab_ref_posns):
+            bad.update(np.argwhere(~np.isfinite(arr).all(axis=-1))[:, 0].tolist())
+        return sorted(bad)
+
+    def get_subset(self, item: slice = None) -> "NumpySimpleSarAperture":
+        return NumpySimpleSarAperture(self.transmitter_positions[item, :], self.receiver_positions[item, :],
+                                      self.stab_ref_posns[item, :], self.centre_frequency, self.sample_bandwidth,
+                                      self.waveform_fft, self.slow_time_weighting[item],
+                                      sign_multiplier=self.sign_multiplier, c_eff=self.c_eff)
+
+    def to_blocks(self, num_blocks: int = 1) -> List["NumpySimpleSarAperture"]:
+        if num_blocks == 1:
+            return [self.get_subset(slice(None))]
+        n = self.num_slow_times // num_blocks
+        return [self.get_subset(slice(b * n, self.num_slow_times if b == num_blocks - 1 else (b + 1) * n))
+                for b in range(num_blocks)]
+
+
+class NumpySimpleSarDataset:
+    """An aperture plus its phase history [S, N] (numpy/measurement.py:244-290)."""
+
+    def __init__(self, aperture, phase_history: np.ndarray):
+        self._aperture = aperture
+        self._phase_history = phase_history
+
+    @property
+    def aperture(self):
+        return self._aperture
+
+    def phase_history(self, item: slice = slice(None)) -> np.ndarray:
+        return self._phase_history[item, :]
+
+    def get_subset(self, item: slice = None) -> "NumpySimpleSarDataset":
+        return NumpySimpleSarDataset(self.aperture.get_subset(item), self._phase_history[item, :])

@@ -1,0 +1,198 @@
+"""SarPlan: one scene + aperture uploaded to a GPU, applied to device tensors.
+
+This is the device-resident layer under the drop-in operator classes.  It replaces the
+per-call work of src/sarsolver/cxx_binding/forward.py:13-44 and adjoint.py:13-44 (building a
+SarCalculationInfo, fftshift handling, one C++ call per process block) with one plan whose
+forward / adjoint run asynchronously on the current torch CUDA stream.
+
+Tensors: image x complex64 [P] (grid order (k*ny + j)*nx + i); phase history y complex64
+[S, N] with fast time fftshifted, as the reference's Python API returns it (forward.py:44).
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+import torch
+
+from . import _lib
+from .geometry import grid_axes
+
+
+def _f64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+
+
+def _interleave(z) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(z, dtype=np.complex128).reshape(-1)).view(np.float64)
+
+
+class SarPlan:
+    """Operator plan on one CUDA device.
+
+    Parameters mirror NumpySimpleSarOperator (src/sarsolver/numpy/operator.py:12-13):
+    ``upsample_ratio`` (default 128, as the reference) and the added ``interp``
+    ("nearest_ref": the reference's bins and conventions; "linear": exact transpose pair).
+    """
+
+    def __init__(self, scene, aperture, upsample_ratio: float = 128.0, interp: str = "nearest_ref",
+                 device: Optional[torch.device] = None):
+        if interp not in _lib.INTERP:
+            raise ValueError(f"interp must be one of {sorted(_lib.INTERP)}")
+        if not torch.cuda.is_available():
+            raise RuntimeError("SarPlan needs a CUDA device")
+        self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        if self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
+        lib = _lib.load()
+        self.num_slow_times = int(aperture.num_slow_times)
+        self.num_freqs = int(aperture.num_freqs)
+        self.num_scatterers = int(scene.num_scatterers)
+        self.interp = interp
+        self.upsample_ratio = float(upsample_ratio)
+        keep = {}
+        keep["tx"] = _f64(aperture.transmitter_positions).reshape(-1, 3)
+        keep["rx"] = _f64(aperture.receiver_positions).reshape(-1, 3)
+        keep["srp"] = _f64(aperture.stab_ref_posns).reshape(-1, 3)
+        # The kernel consumes the waveform in FFT order (forward.py:39, adjoint.py:38).
+        keep["wave"] = _interleave(np.fft.ifftshift(np.asarray(aperture.waveform_fft, dtype=np.complex128)))
+        keep["wt"] = _interleave(aperture.slow_time_weighting)
+        g = _lib.SarGeometry()
+        g.num_fast_times = self.num_freqs
+        g.num_slow_times = self.num_slow_times
+        g.num_scatterers = self.num_scatterers
+        g.transmit_posns = keep["tx"].ctypes.data
+        g.receive_posns = keep["rx"].ctypes.data
+        g.stab_ref_posns = keep["srp"].ctypes.data
+        g.waveform_fft = keep["wave"].ctypes.data
+        g.slow_time_weighting = keep["wt"].ctypes.data
+        g.centre_frequency = float(aperture.centre_frequency)
+        g.sample_frequency = float(aperture.sample_bandwidth)
+        g.c_eff = float(aperture.c_eff)
+        g.upsample_ratio = self.upsample_ratio
+        g.sign_multiplier = float(aperture.sign_multiplier)
+        g.interp = _lib.INTERP[interp]
+        axes = grid_axes(scene)
+        if axes is not None:
+            shape, origin, ex, ey, ez = axes
+            for i in range(3):
+                g.grid_shape[i] = shape[i]
+                g.grid_origin[i] = origin[i]
+                g.grid_step_x[i] = ex[i]
+                g.grid_step_y[i] = ey[i]
+                g.grid_step_z[i] = ez[i]
+            self.grid_shape = tuple(shape)
+        else:
+            keep["pos"] = _f64(scene.positions).reshape(-1, 3)
+            g.scat_posns = keep["pos"].ctypes.data
+            self.grid_shape = None
+        handle = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            torch.cuda.current_stream(self.device)   # make sure the context exists
+            _lib.check(lib.sar_plan_create(ctypes.byref(g), self.device.index, ctypes.byref(handle)), "sar_plan_create")
+        self._handle = handle
+        self._lib = lib
+        info = _lib.SarPlanInfo()
+        _lib.check(lib.sar_plan_get_info(handle, ctypes.byref(info)), "sar_plan_get_info")
+        self.working_length = int(info.working_length)
+        self.profile_first_bin = int(info.profile_first_bin)
+        self.profile_length = int(info.profile_length)
+        self.tile_window = int(info.tile_window)
+        self.strip_window = int(info.strip_window)
+        self.device_bytes = int(info.device_bytes)
+        self.is_grid = bool(info.grid)
+
+    # ------------------------------------------------------------------ helpers
+    def _stream(self) -> ctypes.c_void_p:
+        return ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    def _as_input(self, t: torch.Tensor, numel: int, name: str) -> torch.Tensor:
+        if not isinstance(t, torch.Tensor):
+            t = torch.as_tensor(np.asarray(t))
+        if t.numel() != numel:
+            raise ValueError(f"{name} has {t.numel()} elements, expected {numel}")
+        t = t.to(device=self.device, non_blocking=True)
+        if t.dtype != torch.complex64:
+            t = t.to(torch.complex64)
+        return t.contiguous()
+
+    def _check_out(self, out: Optional[torch.Tensor], shape, name: str) -> torch.Tensor:
+        if out is None:
+            return torch.empty(shape, dtype=torch.complex64, device=self.device)
+        if out.dtype != torch.complex64 or out.device != self.device or not out.is_contiguous():
+            raise ValueError(f"{name} must be a contiguous complex64 tensor on {self.device}")
+        if out.numel() != int(np.prod(shape)):
+            raise ValueError(f"{name} has the wrong size")
+        return out
+
+    # ---------------------------------------------------------------- operators
+    def forward(self, x: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """y = A x, complex64 [S, N] (fast time fftshifted)."""
+        x = self._as_input(x, self.num_scatterers, "x")
+        y = self._check_out(out, (self.num_slow_times, self.num_freqs), "out")
+        with torch.cuda.device(self.device):
+            _lib.check(self._lib.sar_forward(self._handle, ctypes.c_void_p(x.data_ptr()),
+                                             ctypes.c_void_p(y.data_ptr()), self._stream()), "sar_forward")
+        return y
+
+    def adjoint(self, y: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """x = A^H y, complex64 [P]."""
+        y = self._as_input(y, self.num_slow_times * self.num_freqs, "y")
+        x = self._check_out(out, (self.num_scatterers,), "out")
+        with torch.cuda.device(self.device):
+            _lib.check(self._lib.sar_adjoint(self._handle, ctypes.c_void_p(y.data_ptr()),
+                                             ctypes.c_void_p(x.data_ptr()), self._stream()), "sar_adjoint")
+        return x
+
+    def profiles(self, y: torch.Tensor) -> torch.Tensor:
+        """Upsampled range profiles over the stored span, complex64 [S, profile_length]."""
+        y = self._as_input(y, self.num_slow_times * self.num_freqs, "y")
+        prof = torch.empty((self.num_slow_times, self.profile_length), dtype=torch.complex64, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.check(self._lib.sar_profiles(self._handle, ctypes.c_void_p(y.data_ptr()),
+                                              ctypes.c_void_p(prof.data_ptr()), self._stream()), "sar_profiles")
+        return prof
+
+    def set_slow_time_weighting(self, w) -> None:
+        """Replace the slow-time weighting (numpy on the host, or a CUDA tensor, stream-ordered)."""
+        if isinstance(w, torch.Tensor) and w.is_cuda:
+            w = self._as_input(w, self.num_slow_times, "w")
+            with torch.cuda.device(self.device):
+                _lib.check(self._lib.sar_set_slow_time_weighting_device(
+                    self._handle, ctypes.c_void_p(w.data_ptr()), self._stream()), "sar_set_slow_time_weighting")
+            self._keep_w = w
+            return
+        arr = _interleave(np.asarray(w))
+        if arr.size != 2 * self.num_slow_times:
+            raise ValueError("weighting has the wrong length")
+        _lib.check(self._lib.sar_set_slow_time_weighting(self._handle, arr.ctypes.data), "sar_set_slow_time_weighting")
+
+    def enable_stage_timing(self, enable: bool = True) -> None:
+        """Record CUDA events around each call's stages (see sar_enable_stage_timing)."""
+        _lib.check(self._lib.sar_enable_stage_timing(self._handle, int(bool(enable))), "sar_enable_stage_timing")
+
+    def stage_times(self):
+        """(ms per stage [pre-FFT side, main kernel, post-FFT side] summed over recorded calls, calls)."""
+        ms = (ctypes.c_float * 3)()
+        calls = ctypes.c_int(0)
+        _lib.check(self._lib.sar_stage_times(self._handle, ms, ctypes.byref(calls)), "sar_stage_times")
+        return [float(v) for v in ms], int(calls.value)
+
+    def device_flags(self) -> int:
+        """Synchronise and return (then clear) the device check flags; 0 means no check fired."""
+        f = ctypes.c_uint(0)
+        _lib.check(self._lib.sar_device_flags(self._handle, ctypes.byref(f)), "sar_device_flags")
+        return int(f.value)
+
+    def close(self) -> None:
+        if getattr(self, "_handle", None):
+            torch.cuda.synchronize(self.device)
+            self._lib.sar_plan_destroy(self._handle)
+            self._handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,111 @@
+"""Precision of the kernels' range geometry, evaluated by the host build of the same code.
+
+The GPU kernels never form the range in FP64 per pixel (sar_geom.cuh).  This checks, without a
+GPU, that their phase (cycles, mod 1) and range-bin position agree with FP64 ranges computed as
+the reference does (sarsolver_cxx.cpp:10-20, :283, :287) to well inside the 1e-5 relative-error
+budget, on the benchmark geometry at full size.
+"""
+import numpy as np
+import pytest
+
+from cases import C, load_golden, spotlight
+from sarsolver_gb300 import _lib
+from sarsolver_gb300.geometry import GridSarScene, grid_axes
+
+
+def fp64_truth(tx, rx, srp, pos, kappa, s_r):
+    dr = (np.linalg.norm(tx[None] - pos, axis=1) + np.linalg.norm(rx[None] - pos, axis=1)
+          - np.linalg.norm(tx - srp) - np.linalg.norm(rx - srp))
+    cyc = kappa * dr
+    return cyc - np.round(cyc), s_r * dr
+
+
+def host_eval_grid(scene, tx, rx, srp, kappa, s_r):
+    lib = _lib.load_host()
+    shape, origin, ex, ey, ez = grid_axes(scene)
+    nz, ny, nx = shape
+    S = tx.shape[0]
+    ph = np.zeros((S, nz * ny * nx), np.float32)
+    bn = np.zeros((S, nz * ny * nx))
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (origin, ex, ey, ez, tx, rx, srp)]
+    assert lib.sar_geom_host_eval(*[a.ctypes.data for a in arrs[:4]], nx, ny, nz, S,
+                                  *[a.ctypes.data for a in arrs[4:]], kappa, s_r, 0.0,
+                                  ph.ctypes.data, bn.ctypes.data) == 0
+    return ph, bn
+
+
+def errors(ph, bn, truth_ph, truth_bn):
+    e = ph.astype(np.float64) - truth_ph
+    e -= np.round(e)
+    return np.abs(e).max() * 2 * np.pi, np.sqrt(np.mean(e ** 2)) * 2 * np.pi, np.abs(bn - truth_bn).max()
+
+
+@pytest.mark.parametrize("name", ["little", "spot_small", "bistatic_odd"])
+def test_grid_axes_reproduce_positions(name):
+    case = load_golden(name)
+    shape, origin, ex, ey, ez = grid_axes(case.scene)
+    nz, ny, nx = shape
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    pos = origin[None] + i.reshape(-1, 1) * ex + j.reshape(-1, 1) * ey + k.reshape(-1, 1) * ez
+    assert np.abs(pos - case.scene.positions).max() < 1e-9
+
+
+@pytest.mark.parametrize("n,spacing,aperture,pulses", [
+    (2048, 0.25, 5.0, [0, 4095]),     # benchmark image, first and last pulse of 4096
+    (256, 0.5, 3.0, [0, 64, 127]),    # CPU-runnable configuration
+])
+def test_grid_phase_and_bin_precision(n, spacing, aperture, pulses):
+    S_full = 4096 if n == 2048 else 128
+    tx = spotlight(S_full, aperture)[pulses]
+    srp = np.zeros_like(tx)
+    scene = GridSarScene([1, n, n], [0.0, spacing * (n - 1), spacing * (n - 1)])
+    kappa, s_r = 10.0e9 / C, 200.0e6 * 8 / C
+    ph, bn = host_eval_grid(scene, tx, tx, srp, kappa, s_r)
+    pos = scene.positions
+    worst = []
+    for s in range(len(pulses)):
+        tp, tb = fp64_truth(tx[s], tx[s], srp[s], pos, kappa, s_r)
+        worst.append(errors(ph[s], bn[s], tp, tb))
+    pmax = max(w[0] for w in worst)
+    prms = max(w[1] for w in worst)
+    bmax = max(w[2] for w in worst)
+    assert pmax < 1.0e-5, pmax      # radians
+    assert prms < 1.5e-6, prms
+    assert bmax < 5.0e-5, bmax      # range bins
+
+
+def test_bistatic_rotated_grid_precision():
+    case = load_golden("bistatic_odd")
+    ap = case.aperture
+    kappa = ap.sign_multiplier * ap.centre_frequency / ap.c_eff
+    s_r = ap.sample_bandwidth * 8.0 / ap.c_eff
+    ph, bn = host_eval_grid(case.scene, ap.transmitter_positions, ap.receiver_positions, ap.stab_ref_posns,
+                            kappa, s_r)
+    pos = case.scene.positions
+    for s in range(ap.num_slow_times):
+        tp, tb = fp64_truth(ap.transmitter_positions[s], ap.receiver_positions[s], ap.stab_ref_posns[s], pos,
+                            kappa, s_r)
+        pmax, _, bmax = errors(ph[s], bn[s], tp, tb)
+        assert pmax < 1.0e-5 and bmax < 5.0e-5
+
+
+def test_unstructured_point_precision():
+    lib = _lib.load_host()
+    rng = np.random.default_rng(0)
+    P, S = 50000, 3
+    tx = spotlight(S, 5.0)
+    rx = spotlight(S, 3.0, 8.0e3, 3.0e3, 20.0)
+    srp = np.zeros((S, 3))
+    pos = np.stack([rng.uniform(-256, 256, P), rng.uniform(-256, 256, P), rng.uniform(-2, 2, P)], -1)
+    origin = 0.5 * (pos.min(0) + pos.max(0))
+    kappa, s_r = 10.0e9 / C, 200.0e6 * 8 / C
+    ph = np.zeros((S, P), np.float32)
+    bn = np.zeros((S, P))
+    arrs = [np.ascontiguousarray(a) for a in (origin, pos, tx, rx, srp)]
+    lib.sar_geom_host_eval_points(arrs[0].ctypes.data, P, arrs[1].ctypes.data, S, arrs[2].ctypes.data,
+                                  arrs[3].ctypes.data, arrs[4].ctypes.data, kappa, s_r, 0.0, ph.ctypes.data,
+                                  bn.ctypes.data)
+    for s in range(S):
+        tp, tb = fp64_truth(tx[s], rx[s], srp[s], pos, kappa, s_r)
+        pmax, _, bmax = errors(ph[s], bn[s], tp, tb)
+        assert pmax < 1.0e-6 and bmax < 1.0e-6
