@@ -171,11 +171,11 @@ def run_ours(args):
     y_host = y.cpu().pin_memory()
     x_host = torch.empty(P, dtype=torch.complex64).pin_memory()
     for _ in range(args.warmup):
-        x_host.copy_(op.adjoint(y_host), non_blocking=True)
+        x_host.copy_(op.backproject(y_host), non_blocking=True)
     barrier()
     e0.record(stream)
     for _ in range(args.steps):
-        x_host.copy_(op.adjoint(y_host), non_blocking=True)
+        x_host.copy_(op.backproject(y_host), non_blocking=True)
     e1.record(stream)
     barrier()
     e2e_ms = e0.elapsed_time(e1) / args.steps
@@ -212,7 +212,7 @@ def run_ours(args):
                                    "3 MUFU per px*pulse (sm_max_mhz of MEASURED_PEAKS.json)"},
         "e2e": {"value": world * P * S / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": S * N * 8, "d2h_bytes_per_step": P * 8,
-                "api": "NumpySimpleSarOperator.adjoint(pinned host complex64 tensor) -> pinned host copy"},
+                "api": "NumpySimpleSarOperator.backproject(pinned host complex64 tensor) -> pinned host copy"},
         # our kernels per call: pack + unpack per FFT chunk, then the gather (cuFFT's own excluded)
         "gpu_launches": args.steps * (2 * ((S + plan_chunk(plan) - 1) // plan_chunk(plan)) + 1),
         "clocks": clocks,

@@ -139,7 +139,7 @@ def load_host() -> ctypes.CDLL:
         lib = ctypes.CDLL(HOST_LIB)
         P = c_void_p
         lib.sar_geom_host_eval.argtypes = [P, P, P, P, c_int, c_int, c_int, c_size_t, P, P, P, c_double, c_double,
-                                           ctypes.c_float, P, P]
+                                           ctypes.c_float, c_int, P, P]
         lib.sar_geom_host_eval_points.argtypes = [P, c_size_t, P, c_size_t, P, P, P, c_double, c_double,
                                                   ctypes.c_float, P, P]
         _HOST = lib

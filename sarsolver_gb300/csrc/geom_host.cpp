@@ -17,10 +17,11 @@ using namespace sar;
 extern "C" int sar_geom_host_eval(const double* origin, const double* ex, const double* ey,
                                   const double* ez, int nx, int ny, int nz, size_t num_pulses,
                                   const double* tx, const double* rx, const double* srp,
-                                  double kappa, double s_r, float bin_offset, float* phase_out,
-                                  double* bin_out) {
+                                  double kappa, double s_r, float bin_offset, int precise_bins,
+                                  float* phase_out, double* bin_out) {
     if (nx <= 0 || ny <= 0 || nz <= 0) return 1;
     GridConst g = make_grid_const(ex, ey, ez, kappa, s_r, bin_offset, nx, ny, nz);
+    g.precise_bins = precise_bins;
     const size_t P = (size_t)nx * ny * nz;
     for (size_t s = 0; s < num_pulses; ++s) {
         PulseGeom pg = make_pulse_geom(tx + 3 * s, rx + 3 * s, srp + 3 * s, origin);
@@ -41,7 +42,7 @@ extern "C" int sar_geom_host_eval(const double* origin, const double* ex, const 
                         vsum = df_add(vsum, vb[q]);
                     }
                     int base = base_bin_of(vsum, 4.0f);
-                    for (int q = 0; q < 4; ++q) bin_coeffs(ae[q], vb[q], base, g, co[q].v);
+                    for (int q = 0; q < 4; ++q) bin_coeffs(ae[q], vb[q], base, g, co[q]);
                     for (int lj = 0; lj < 32; ++lj)
                         for (int li = 0; li < 32; ++li) {
                             int i = ti * 32 + li, j = tj * 32 + lj;
@@ -49,12 +50,18 @@ extern "C" int sar_geom_host_eval(const double* origin, const double* ex, const 
                             int q = (li >= 16) + 2 * (lj >= 16);
                             float di = (float)(li - 8 - 16 * (q & 1));
                             float dj = (float)(lj - 8 - 16 * (q >> 1));
-                            ColumnTerms ct = column_terms(co[q], di, di * di, di * di * di);
+                            const bool pr = g.precise_bins != 0;
+                            ColumnTerms ct = pr ? column_terms<true>(co[q], di, di * di, di * di * di)
+                                                : column_terms<false>(co[q], di, di * di, di * di * di);
                             float ph = pixel_phase(ct, co[q].c[9], dj, dj * dj, dj * dj * dj);
-                            float v = pixel_bin(ct, co[q].v[5], dj, dj * dj);
+                            float v = pr ? pixel_bin<true>(ct, co[q].w[3], dj, dj * dj, dj * dj * dj)
+                                         : pixel_bin<false>(ct, 0.0f, dj, dj * dj, dj * dj * dj);
                             size_t p = ((size_t)k * ny + j) * nx + i;
                             phase_out[s * P + p] = ph - round_shift(ph);
-                            bin_out[s * P + p] = (double)base + (double)v;
+                            // the kernels' bin index and in-bin coordinate, recombined
+                            BinPos bp = pr ? bin_position<true>(v, fmaf(co[q].ib, dj, ct.ci))
+                                           : bin_position<false>(v, 0.0f);
+                            bin_out[s * P + p] = (double)base + (double)bp.n + (double)bp.s;
                         }
                 }
     }

@@ -297,6 +297,9 @@ int build_plan(const sar_geometry* g, sar_plan* p) {
         const double h = s_r * 2.0 * 16.0 * (nex + ney);
         if (h > 1.0e6) return fail(SAR_ERR_NOT_SUPPORTED, "grid spacing too coarse for the range sampling");
         p->wwin = (2 * ((int)std::ceil(h) + 3) + 3) & ~3;
+        // Nearest-bin decisions must match FP64, and wide tiles need the exact integer part:
+        // split the linear bin rates in both cases (sar_geom.cuh, bin_coeffs).
+        p->gc_adj.precise_bins = p->gc_fwd.precise_bins = (p->interp == SAR_INTERP_NEAREST_REF || p->wwin > 256) ? 1 : 0;
         p->bg0 = (long)std::floor(vmin) - p->wwin / 2 - 4;
         const double span = std::ceil(vmax) + p->wwin / 2 + 5 - (double)p->bg0;
         if (span > 2.0e9) return fail(SAR_ERR_NOT_SUPPORTED, "range span too large");

@@ -172,6 +172,7 @@ struct GridConst {
                                  // or 0 (forward nearest: round)
     int nx, ny, nz;              // grid shape
     int tiles_x, tiles_y;        // 32x32 tiles per plane
+    int precise_bins;            // 1: integer/fraction split of the linear bin rates + cubic bin terms
 };
 
 // Coefficients of one (sub-tile, pulse) pair: 16 floats.
@@ -179,9 +180,16 @@ struct GridConst {
 //                       + c6 di^3 + c7 di^2 dj + c8 di dj^2 + c9 dj^3      (c0..c2 reduced mod 1)
 //  bin:            v  = v0 + v1 di + v2 dj + v3 di^2 + v4 di dj + v5 dj^2 (relative to the tile's
 //                  base bin, bin_offset already folded into v0)
+//  precise bins (used where nearest-bin decisions must match FP64, or for wide tiles): v1, v2
+//  hold only the fractional parts of the linear bin rates and their integer parts (ia, ib) are
+//  accumulated exactly, so the FP32 part stays below ~17 bins for any upsample ratio; the
+//  cubic terms w6..w9 (same monomials as c6..c9) are added, which matters at short stand-off
+//  and fine bins (e.g. 2 km and upsample 128: ~2e-4 bins over a 16x16 sub-tile).
 struct Coeffs {
     float c[10];
     float v[6];
+    float i0, ia, ib;   // exact integer parts (precise mode)
+    float w[4];
 };
 
 struct AntennaTerms {
@@ -285,16 +293,31 @@ SAR_HD int base_bin_of(df sum_of_bins, float count) {
     return (int)f;
 }
 
-// Bin coefficients relative to base_bin, with the interpolation offset folded in.
-SAR_HD void bin_coeffs(const AnchorExpansion& a, df vbin, int base_bin, const GridConst& g, float* v) {
+// Bin coefficients relative to base_bin, with the interpolation offset folded in.  In precise
+// mode the linear rates s_r*gx, s_r*gy are formed in double-float and split into an integer
+// (ia, ib) and a fraction in [-0.5, 0.5] (v[1], v[2]), and the cubic terms are kept.
+SAR_HD void bin_coeffs(const AnchorExpansion& a, df vbin, int base_bin, const GridConst& g, Coeffs& co) {
     df rel = df_sub(vbin, df_make((float)base_bin, 0.0f));
-    v[0] = (rel.hi + rel.lo) + g.bin_offset;
     const float sr = g.s_r.hi;
-    v[1] = sr * (a.gx.hi + a.gx.lo);
-    v[2] = sr * (a.gy.hi + a.gy.lo);
-    v[3] = sr * a.q[0];
-    v[4] = sr * a.q[1];
-    v[5] = sr * a.q[2];
+    if (g.precise_bins) {
+        co.i0 = round_shift(rel.hi);
+        co.v[0] = ((rel.hi - co.i0) + rel.lo) + g.bin_offset;
+        const df rx = df_mul(g.s_r, a.gx), ry = df_mul(g.s_r, a.gy);
+        co.ia = round_shift(rx.hi);
+        co.ib = round_shift(ry.hi);
+        co.v[1] = (rx.hi - co.ia) + rx.lo;
+        co.v[2] = (ry.hi - co.ib) + ry.lo;
+        for (int i = 0; i < 4; ++i) co.w[i] = sr * a.k[i];
+    } else {
+        co.v[0] = (rel.hi + rel.lo) + g.bin_offset;
+        co.i0 = co.ia = co.ib = 0.0f;
+        co.v[1] = sr * (a.gx.hi + a.gx.lo);
+        co.v[2] = sr * (a.gy.hi + a.gy.lo);
+        for (int i = 0; i < 4; ++i) co.w[i] = 0.0f;
+    }
+    co.v[3] = sr * a.q[0];
+    co.v[4] = sr * a.q[1];
+    co.v[5] = sr * a.q[2];
 }
 
 // Anchor position of pixel (i, j, k) relative to the grid origin.
@@ -309,24 +332,63 @@ SAR_HD df3 pixel_position(int i, int j, int k, const GridConst& g) {
 // Column part (di fixed) and pixel part (dj varies) of the polynomials; see sar_kernels.cu.
 struct ColumnTerms {
     float cph, b1, b2;   // phase: cph + b1 dj + b2 dj^2 + c9 dj^3
-    float cv, bv1;       // bin:   cv + bv1 dj + v5 dj^2
+    float cv, bv1, bv2;  // bin:   cv + bv1 dj + bv2 dj^2 (+ w9 dj^3, and + ci + ib dj exactly, when precise)
+    float ci;
 };
 
+template <bool PRECISE>
 SAR_HD ColumnTerms column_terms(const Coeffs& q, float di, float di2, float di3) {
     ColumnTerms t;
     t.cph = fmaf(q.c[6], di3, fmaf(q.c[3], di2, fmaf(q.c[1], di, q.c[0])));
     t.b1 = fmaf(q.c[7], di2, fmaf(q.c[4], di, q.c[2]));
     t.b2 = fmaf(q.c[8], di, q.c[5]);
-    t.cv = fmaf(q.v[3], di2, fmaf(q.v[1], di, q.v[0]));
-    t.bv1 = fmaf(q.v[4], di, q.v[2]);
+    if (PRECISE) {
+        t.cv = fmaf(q.w[0], di3, fmaf(q.v[3], di2, fmaf(q.v[1], di, q.v[0])));
+        t.bv1 = fmaf(q.w[1], di2, fmaf(q.v[4], di, q.v[2]));
+        t.bv2 = fmaf(q.w[2], di, q.v[5]);
+        t.ci = fmaf(q.ia, di, q.i0);
+    } else {
+        t.cv = fmaf(q.v[3], di2, fmaf(q.v[1], di, q.v[0]));
+        t.bv1 = fmaf(q.v[4], di, q.v[2]);
+        t.bv2 = q.v[5];
+        t.ci = 0.0f;
+    }
     return t;
 }
 
 SAR_HD float pixel_phase(const ColumnTerms& t, float c9, float dj, float dj2, float dj3) {
     return fmaf(c9, dj3, fmaf(t.b2, dj2, fmaf(t.b1, dj, t.cph)));
 }
-SAR_HD float pixel_bin(const ColumnTerms& t, float v5, float dj, float dj2) {
-    return fmaf(v5, dj2, fmaf(t.bv1, dj, t.cv));
+template <bool PRECISE>
+SAR_HD float pixel_bin(const ColumnTerms& t, float w9, float dj, float dj2, float dj3) {
+    const float v = fmaf(t.bv2, dj2, fmaf(t.bv1, dj, t.cv));
+    return PRECISE ? fmaf(w9, dj3, v) : v;
+}
+
+// Bin index n (relative to the tile base) and coordinate s in [-0.5, 0.5] about it, from the
+// FP32 part v and, when split, the exact integer part ni.  (v + shifter) holds rint(v) in its
+// low mantissa bits; adding the integer ni keeps the sum in [2^23, 2^24), hence exact.
+struct BinPos {
+    int n;
+    float s;
+};
+template <bool PRECISE>
+SAR_HD BinPos bin_position(float v, float ni) {
+    const float r1 = v + SAR_SHIFTER;
+    BinPos b;
+    b.s = v - (r1 - SAR_SHIFTER);
+    const float rr = PRECISE ? r1 + ni : r1;
+#if defined(__CUDA_ARCH__)
+    b.n = __float_as_int(rr) - SAR_SHIFTER_BITS;
+#else
+    union {
+        float f;
+        int32_t i;
+    } u;
+    u.f = rr;
+    b.n = u.i - SAR_SHIFTER_BITS;
+#endif
+    return b;
 }
 
 // ------------------------------------------------ unstructured positions (scheme 2)

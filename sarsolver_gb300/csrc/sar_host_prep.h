@@ -70,6 +70,7 @@ static inline GridConst make_grid_const(const double* ex, const double* ey, cons
     g.nz = nz;
     g.tiles_x = (nx + 31) / 32;
     g.tiles_y = (ny + 31) / 32;
+    g.precise_bins = 0;
     return g;
 }
 

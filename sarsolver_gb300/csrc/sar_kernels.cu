@@ -64,7 +64,9 @@ __device__ __forceinline__ df3 subtile_anchor(int ti, int tj, int k, int q, cons
 }
 
 // One (pulse, sub-tile) coefficient set per thread of the first ceil(4 pb / 32) warps.
-// Coefficient sets are 4 float4: [c0 c1 c2 c3][c4 c5 c6 c7][c8 c9 v0 v1][v2 v3 v4 v5].
+// Coefficient sets are kSetF4 = 6 float4:
+//   [c0 c1 c2 c3][c4 c5 c6 c7][c8 c9 v0 v1][v2 v3 v4 v5][ia ib w6 w7][w8 w9 i0 -]
+// (the last two are read only in precise-bin mode).
 // The tile's base bin (floor of the mean anchor bin) is agreed across the four lanes of a
 // pulse by shuffles, so all sub-tiles of a pulse share it.
 __device__ __forceinline__ void coeff_stage(const GridConst& g, const PulseGeom* __restrict__ pulses,
@@ -90,12 +92,14 @@ __device__ __forceinline__ void coeff_stage(const GridConst& g, const PulseGeom*
     int b = base_bin_of(sum, 4.0f);
     b = __shfl_sync(all, b, (t & 31) & ~3);
     if (valid) {
-        bin_coeffs(ae, vb, b, g, co.v);
-        float4* dst = coef + (pi * 4 + q) * 4;
+        bin_coeffs(ae, vb, b, g, co);
+        float4* dst = coef + (pi * 4 + q) * kSetF4;
         dst[0] = make_float4(co.c[0], co.c[1], co.c[2], co.c[3]);
         dst[1] = make_float4(co.c[4], co.c[5], co.c[6], co.c[7]);
         dst[2] = make_float4(co.c[8], co.c[9], co.v[0], co.v[1]);
         dst[3] = make_float4(co.v[2], co.v[3], co.v[4], co.v[5]);
+        dst[4] = make_float4(co.ia, co.ib, co.w[0], co.w[1]);
+        dst[5] = make_float4(co.w[2], co.w[3], co.i0, 0.f);
         if (q == 0) base[pi] = b;
     }
 }
@@ -106,44 +110,60 @@ struct PixelEval {
     int n;      // bin relative to the tile's base bin
 };
 
+template <bool PRECISE>
 __device__ __forceinline__ ColumnTerms load_column(const float4* cs, const TileThread& tt, float& c9,
-                                                   float& v5) {
+                                                   float& w9, float& ib) {
     const float4 A = cs[0], B = cs[1], C = cs[2], D = cs[3];
     Coeffs co;
+    if (PRECISE) {
+        const float4 E = cs[4], F = cs[5];
+        co.ia = E.x;
+        co.ib = E.y;
+        co.w[0] = E.z;
+        co.w[1] = E.w;
+        co.w[2] = F.x;
+        co.w[3] = F.y;
+        co.i0 = F.z;
+    } else {
+        co.i0 = co.ia = co.ib = 0.f;
+        co.w[0] = co.w[1] = co.w[2] = co.w[3] = 0.f;
+    }
+    ib = co.ib;
+    w9 = co.w[3];
     co.c[0] = A.x; co.c[1] = A.y; co.c[2] = A.z; co.c[3] = A.w;
     co.c[4] = B.x; co.c[5] = B.y; co.c[6] = B.z; co.c[7] = B.w;
     co.c[8] = C.x; co.c[9] = C.y; co.v[0] = C.z; co.v[1] = C.w;
     co.v[2] = D.x; co.v[3] = D.y; co.v[4] = D.z; co.v[5] = D.w;
     c9 = co.c[9];
-    v5 = co.v[5];
-    return column_terms(co, tt.di, tt.di2, tt.di3);
+    return column_terms<PRECISE>(co, tt.di, tt.di2, tt.di3);
 }
 
-__device__ __forceinline__ PixelEval eval_pixel(const ColumnTerms& ct, float c9, float v5,
+template <bool PRECISE>
+__device__ __forceinline__ PixelEval eval_pixel(const ColumnTerms& ct, float c9, float w9, float ib,
                                                 const TileThread& tt, int r) {
     PixelEval e;
     const float ph = pixel_phase(ct, c9, tt.dj[r], tt.dj2[r], tt.dj3[r]);
     e.f = ph - round_shift(ph);
-    const float v = pixel_bin(ct, v5, tt.dj[r], tt.dj2[r]);
-    const float rr = v + SAR_SHIFTER;
-    e.sf = v - (rr - SAR_SHIFTER);
-    e.n = __float_as_int(rr) - SAR_SHIFTER_BITS;
+    const float v = pixel_bin<PRECISE>(ct, w9, tt.dj[r], tt.dj2[r], tt.dj3[r]);
+    const BinPos b = bin_position<PRECISE>(v, PRECISE ? fmaf(ib, tt.dj[r], ct.ci) : 0.f);
+    e.sf = b.s;
+    e.n = b.n;
     return e;
 }
 
 // ------------------------------------------------------------------- K2 (grid)
 size_t bp_grid_smem_bytes(int wwin, int pb, int staged) {
-    size_t f4 = (staged ? (size_t)pb * wwin : 0) + (size_t)pb * 16 + (size_t)((pb + 3) / 4) + 6;
+    size_t f4 = (staged ? (size_t)pb * wwin : 0) + (size_t)pb * 4 * kSetF4 + (size_t)((pb + 3) / 4) + 6;
     return f4 * sizeof(float4);
 }
 
-template <bool STAGED>
+template <bool STAGED, bool PRECISE>
 __global__ void __launch_bounds__(kThreads, 2) bp_grid_kernel(const BpGridArgs a) {
     extern __shared__ float4 smem[];
     const int pb = a.pb;
     float4* win = smem;
     float4* coef = smem + (STAGED ? pb * a.wwin : 0);
-    int* base = reinterpret_cast<int*>(coef + pb * 16);
+    int* base = reinterpret_cast<int*>(coef + pb * 4 * kSetF4);
     df3* anchors = reinterpret_cast<df3*>(base + ((pb + 3) & ~3));
 
     const GridConst& g = a.g;
@@ -177,14 +197,14 @@ __global__ void __launch_bounds__(kThreads, 2) bp_grid_kernel(const BpGridArgs a
         }
         float st_re[4] = {0.f, 0.f, 0.f, 0.f}, st_im[4] = {0.f, 0.f, 0.f, 0.f};
         for (int pi = 0; pi < npb; ++pi) {
-            float c9, v5;
-            const ColumnTerms ct = load_column(coef + (pi * 4 + tt.q) * 4, tt, c9, v5);
+            float c9, w9, ib;
+            const ColumnTerms ct = load_column<PRECISE>(coef + (pi * 4 + tt.q) * kSetF4, tt, c9, w9, ib);
             const float4* wp = win + pi * a.wwin;
             const float4* gp = a.pairs + (size_t)(s0 + pi) * a.Lg;
             const int bb = base[pi] - a.bg0;
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
-                const PixelEval e = eval_pixel(ct, c9, v5, tt, r);
+                const PixelEval e = eval_pixel<PRECISE>(ct, c9, w9, ib, tt, r);
                 float4 pv;
                 if (STAGED) {
                     const unsigned idx = min((unsigned)(e.n + half_w), (unsigned)(a.wwin - 1));
@@ -225,20 +245,20 @@ __global__ void __launch_bounds__(kThreads, 2) bp_grid_kernel(const BpGridArgs a
     }
 }
 
-cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st) {
+template <bool STAGED, bool PRECISE>
+static cudaError_t launch_bp_grid_t(const BpGridArgs& a, cudaStream_t st) {
     const size_t smem = bp_grid_smem_bytes(a.wwin, a.pb, a.staged);
     const unsigned blocks = (unsigned)(a.g.tiles_x * a.g.tiles_y * a.g.nz);
-    cudaError_t e;
-    if (a.staged) {
-        e = cudaFuncSetAttribute(bp_grid_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        bp_grid_kernel<true><<<blocks, kThreads, smem, st>>>(a);
-    } else {
-        e = cudaFuncSetAttribute(bp_grid_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        bp_grid_kernel<false><<<blocks, kThreads, smem, st>>>(a);
-    }
+    cudaError_t e = cudaFuncSetAttribute(bp_grid_kernel<STAGED, PRECISE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    bp_grid_kernel<STAGED, PRECISE><<<blocks, kThreads, smem, st>>>(a);
     return cudaGetLastError();
+}
+
+cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st) {
+    if (a.staged) return a.g.precise_bins ? launch_bp_grid_t<true, true>(a, st) : launch_bp_grid_t<true, false>(a, st);
+    return a.g.precise_bins ? launch_bp_grid_t<false, true>(a, st) : launch_bp_grid_t<false, false>(a, st);
 }
 
 // ------------------------------------------------------------------- K3 (grid)
@@ -248,17 +268,17 @@ cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st) {
 // atomic add per bin.  Each pixel uses the identical coefficient sets, bin and weights as
 // K2, so the pair is an exact transpose up to FP32 summation order.
 size_t fp_grid_smem_bytes(int ws, int pbf) {
-    size_t f4 = (size_t)pbf * ws / 2 + (size_t)pbf * 16 + (size_t)((2 * pbf + 3) / 4) + 6;
+    size_t f4 = (size_t)pbf * ws / 2 + (size_t)pbf * 4 * kSetF4 + (size_t)((2 * pbf + 3) / 4) + 6;
     return f4 * sizeof(float4);
 }
 
-template <bool LINEAR>
+template <bool LINEAR, bool PRECISE>
 __global__ void __launch_bounds__(kThreads, 2) fp_grid_kernel(const FpGridArgs a) {
     extern __shared__ float4 smem[];
     const int pbf = a.pbf;
     float2* win = reinterpret_cast<float2*>(smem);
     float4* coef = smem + (pbf * a.ws) / 2;
-    int* base = reinterpret_cast<int*>(coef + pbf * 16);
+    int* base = reinterpret_cast<int*>(coef + pbf * 4 * kSetF4);
     int* wst = base + pbf;
     df3* anchors = reinterpret_cast<df3*>(base + ((2 * pbf + 3) & ~3));
 
@@ -292,13 +312,13 @@ __global__ void __launch_bounds__(kThreads, 2) fp_grid_kernel(const FpGridArgs a
         coeff_stage(g, a.pulses, s0, npb, pbf, anchors, coef, base);
         __syncthreads();
         for (int pi = 0; pi < npb; ++pi) {
-            float c9, v5;
-            const ColumnTerms ct = load_column(coef + (pi * 4 + tt.q) * 4, tt, c9, v5);
+            float c9, w9, ib;
+            const ColumnTerms ct = load_column<PRECISE>(coef + (pi * 4 + tt.q) * kSetF4, tt, c9, w9, ib);
             float2* wp = win + pi * a.ws;
             const int off = base[pi] - wst[pi];
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
-                const PixelEval e = eval_pixel(ct, c9, v5, tt, r);
+                const PixelEval e = eval_pixel<PRECISE>(ct, c9, w9, ib, tt, r);
                 float sn, cn;
                 __sincosf(SAR_TWO_PI * e.f, &sn, &cn);
                 // contribution x * exp(+2 pi i f)
@@ -335,21 +355,20 @@ __global__ void __launch_bounds__(kThreads, 2) fp_grid_kernel(const FpGridArgs a
     }
 }
 
-cudaError_t launch_fp_grid(const FpGridArgs& a, cudaStream_t st) {
-    const int linear = a.linear;
+template <bool LINEAR, bool PRECISE>
+static cudaError_t launch_fp_grid_t(const FpGridArgs& a, cudaStream_t st) {
     const size_t smem = fp_grid_smem_bytes(a.ws, a.pbf);
     const dim3 grid((unsigned)(a.segs_per_column * a.g.tiles_x * a.g.nz), (unsigned)((a.S + a.pbf - 1) / a.pbf));
-    cudaError_t e;
-    if (linear) {
-        e = cudaFuncSetAttribute(fp_grid_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        fp_grid_kernel<true><<<grid, kThreads, smem, st>>>(a);
-    } else {
-        e = cudaFuncSetAttribute(fp_grid_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        fp_grid_kernel<false><<<grid, kThreads, smem, st>>>(a);
-    }
+    cudaError_t e = cudaFuncSetAttribute(fp_grid_kernel<LINEAR, PRECISE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    fp_grid_kernel<LINEAR, PRECISE><<<grid, kThreads, smem, st>>>(a);
     return cudaGetLastError();
+}
+
+cudaError_t launch_fp_grid(const FpGridArgs& a, cudaStream_t st) {
+    if (a.linear) return a.g.precise_bins ? launch_fp_grid_t<true, true>(a, st) : launch_fp_grid_t<true, false>(a, st);
+    return a.g.precise_bins ? launch_fp_grid_t<false, true>(a, st) : launch_fp_grid_t<false, false>(a, st);
 }
 
 // ------------------------------------------------------- K2 / K3 (points)

@@ -18,6 +18,7 @@ enum : unsigned {
 constexpr int kTile = 32;          // pixels per tile side
 constexpr int kThreads = 256;      // threads per tile CTA: 32 columns x 8 warps, 4 rows each
 constexpr int kMaxStagePulses = 32;
+constexpr int kSetF4 = 6;          // float4 per (pulse, sub-tile) coefficient set
 
 // Backprojection over a regular grid (K2).
 struct BpGridArgs {

@@ -6,7 +6,8 @@ and shape (num_freqs*num_slow_times, num_scatterers), whose _matvec runs the for
 
 Here both run on the GPU through one SarPlan.  numpy inputs are copied to the device, computed
 in complex64, and returned as complex128 numpy arrays like the reference; torch tensors (CPU or
-CUDA) can be passed to ``forward`` / ``adjoint`` directly and stay tensors.
+CUDA) can be passed to ``forward`` / ``backproject`` directly and stay tensors.  (``adjoint()``
+keeps scipy's meaning: the Hermitian-adjoint LinearOperator.)
 """
 from __future__ import annotations
 
@@ -56,7 +57,7 @@ class NumpySimpleSarOperator(LinearOperator):
         """A x for a tensor (any device); returns complex64 [S, N] on the plan's device."""
         return self.plan.forward(_to_device(x, self.plan.device).reshape(-1))
 
-    def adjoint(self, y) -> torch.Tensor:
+    def backproject(self, y) -> torch.Tensor:
         """A^H y for a tensor (any device); returns complex64 [P] on the plan's device."""
         return self.plan.adjoint(_to_device(y, self.plan.device).reshape(-1))
 
@@ -68,7 +69,7 @@ class NumpySimpleSarOperator(LinearOperator):
 
     def _rmatvec(self, y: np.ndarray) -> np.ndarray:
         v = np.asarray(y).reshape(self._aperture.num_slow_times, self._aperture.num_freqs)
-        u = self.adjoint(v)
+        u = self.backproject(v)
         return _to_numpy128(u).reshape(self._scene.num_scatterers)
 
 

@@ -20,7 +20,7 @@ def fp64_truth(tx, rx, srp, pos, kappa, s_r):
     return cyc - np.round(cyc), s_r * dr
 
 
-def host_eval_grid(scene, tx, rx, srp, kappa, s_r):
+def host_eval_grid(scene, tx, rx, srp, kappa, s_r, bin_offset=0.0, precise=0):
     lib = _lib.load_host()
     shape, origin, ex, ey, ez = grid_axes(scene)
     nz, ny, nx = shape
@@ -29,7 +29,7 @@ def host_eval_grid(scene, tx, rx, srp, kappa, s_r):
     bn = np.zeros((S, nz * ny * nx))
     arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (origin, ex, ey, ez, tx, rx, srp)]
     assert lib.sar_geom_host_eval(*[a.ctypes.data for a in arrs[:4]], nx, ny, nz, S,
-                                  *[a.ctypes.data for a in arrs[4:]], kappa, s_r, 0.0,
+                                  *[a.ctypes.data for a in arrs[4:]], kappa, s_r, bin_offset, precise,
                                   ph.ctypes.data, bn.ctypes.data) == 0
     return ph, bn
 
@@ -109,3 +109,28 @@ def test_unstructured_point_precision():
         tp, tb = fp64_truth(tx[s], rx[s], srp[s], pos, kappa, s_r)
         pmax, _, bmax = errors(ph[s], bn[s], tp, tb)
         assert pmax < 1.0e-6 and bmax < 1.0e-6
+
+
+def test_precise_bins_match_fp64_rounding_at_short_range_and_fine_bins():
+    """The reference's 'little' case: 2 km stand-off, upsample 128 (M = 32128).  Nearest-bin
+    sampling (round(0.5 + v), sarsolver_cxx.cpp:347) must pick the FP64 bin; the precise-bin
+    mode (integer/fraction split + cubic bin terms) keeps the bin position within ~1e-6."""
+    case = load_golden("little")
+    ap = case.aperture
+    M = int(128 * ap.num_freqs)
+    s_r = ap.sample_bandwidth * M / (ap.num_freqs * ap.c_eff)
+    kappa = ap.centre_frequency / ap.c_eff
+    pos = case.scene.positions
+    for precise, max_flips, max_err in ((0, None, 5e-4), (1, 10, 5e-6)):
+        ph, bn = host_eval_grid(case.scene, ap.transmitter_positions, ap.receiver_positions, ap.stab_ref_posns,
+                                kappa, s_r, 0.5, precise)
+        flips, err = 0, 0.0
+        for s in range(ap.num_slow_times):
+            _, tb = fp64_truth(ap.transmitter_positions[s], ap.receiver_positions[s], ap.stab_ref_posns[s], pos,
+                               kappa, s_r)
+            v = tb + 0.5
+            flips += int(np.sum(np.round(v) != np.round(bn[s])))
+            err = max(err, float(np.abs(bn[s] - v).max()))
+        assert err < max_err, (precise, err)
+        if max_flips is not None:
+            assert flips <= max_flips, flips

@@ -193,5 +193,5 @@ def test_numpy_operator_api_shapes_and_dtypes():
     z = (op.H @ (op @ case.data["x"]))
     assert z.shape == (op.shape[1],)
     # tensors stay on the device
-    xt = op.adjoint(torch.from_numpy(case.data["y"]).cuda())
+    xt = op.backproject(torch.from_numpy(case.data["y"]).cuda())
     assert xt.is_cuda and xt.dtype == torch.complex64
