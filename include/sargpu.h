@@ -49,6 +49,7 @@ extern "C" {
 /* Device check flags reported by sar_device_flags(). */
 #define SAR_FLAG_TILE_WINDOW 1u
 #define SAR_FLAG_STRIP_WINDOW 2u
+#define SAR_FLAG_WAIT_TIMEOUT 8u /* a bounded in-kernel wait expired; that call's result is invalid */
 
 /* ------------------------------------------------------------ 1. drop-in boundary */
 
@@ -93,7 +94,15 @@ typedef struct sar_geometry {
      * grid_shape = {nz, ny, nx}.  All-zero grid_shape selects the unstructured path. */
     size_t grid_shape[3];
     double grid_origin[3], grid_step_x[3], grid_step_y[3], grid_step_z[3];
+    /* Kernel path for grids: SAR_PATH_AUTO picks the grid fast path for SAR_INTERP_LINEAR and the
+     * per-pixel double-float path for SAR_INTERP_NEAREST_REF (nearest-bin decisions then match
+     * FP64 ranges); SAR_PATH_GRID / SAR_PATH_POINTS force one. */
+    int path;
 } sar_geometry;
+
+#define SAR_PATH_AUTO 0
+#define SAR_PATH_GRID 1
+#define SAR_PATH_POINTS 2
 
 typedef struct sar_plan_info {
     size_t working_length;      /* M = (size_t)(upsample_ratio * N), sarsolver_cxx.cpp:223 */

@@ -19,6 +19,7 @@ SAR_ERR_OUT_OF_MEMORY = 4
 SAR_ERR_NOT_SUPPORTED = 5
 
 INTERP = {"nearest_ref": 0, "linear": 1}
+PATH = {"auto": 0, "grid": 1, "points": 2}
 
 #: Every function include/sargpu.h declares.
 EXPORTED = (
@@ -43,6 +44,7 @@ class SarGeometry(ctypes.Structure):
         ("interp", c_int),
         ("grid_shape", c_size_t * 3), ("grid_origin", c_double * 3), ("grid_step_x", c_double * 3),
         ("grid_step_y", c_double * 3), ("grid_step_z", c_double * 3),
+        ("path", c_int),
     ]
 
 

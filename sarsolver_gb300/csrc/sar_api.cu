@@ -217,6 +217,8 @@ int validate_geometry(const sar_geometry* g) {
         return fail(SAR_ERR_INVALID_ARGUMENT, "c_eff, sample_frequency and upsample_ratio must be positive");
     if (g->interp != SAR_INTERP_NEAREST_REF && g->interp != SAR_INTERP_LINEAR)
         return fail(SAR_ERR_INVALID_ARGUMENT, "unknown interpolation mode %d", g->interp);
+    if (g->path < SAR_PATH_AUTO || g->path > SAR_PATH_POINTS)
+        return fail(SAR_ERR_INVALID_ARGUMENT, "unknown path %d", g->path);
     const size_t M = (size_t)(g->upsample_ratio * (double)N);   // sarsolver_cxx.cpp:223
     if (M < N) return fail(SAR_ERR_INVALID_ARGUMENT, "upsample_ratio*N (%zu) is below N (%zu)", M, N);
     if (M > (size_t)1 << 30 || S > (size_t)1 << 30 || N > (size_t)1 << 30)
@@ -243,10 +245,33 @@ int validate_geometry(const sar_geometry* g) {
     return SAR_OK;
 }
 
-int build_plan(const sar_geometry* g, sar_plan* p) {
+int build_plan(const sar_geometry* g_in, sar_plan* p) {
+    const sar_geometry* g = g_in;
     const size_t N = g->num_fast_times, S = g->num_slow_times, P = g->num_scatterers;
     const size_t M = (size_t)(g->upsample_ratio * (double)N);
-    const bool grid = g->grid_shape[0] || g->grid_shape[1] || g->grid_shape[2];
+    bool grid = g->grid_shape[0] || g->grid_shape[1] || g->grid_shape[2];
+    // A grid routed to the per-pixel path is expanded into explicit positions.
+    sar_geometry expanded;
+    std::vector<double> grid_positions;
+    const bool to_points =
+        grid && (g->path == SAR_PATH_POINTS || (g->path == SAR_PATH_AUTO && g->interp == SAR_INTERP_NEAREST_REF));
+    if (to_points) {
+        const size_t nz = g->grid_shape[0], ny = g->grid_shape[1], nx = g->grid_shape[2];
+        grid_positions.resize(3 * P);
+        for (size_t k = 0; k < nz; ++k)
+            for (size_t j = 0; j < ny; ++j)
+                for (size_t i = 0; i < nx; ++i) {
+                    double* q = &grid_positions[3 * ((k * ny + j) * nx + i)];
+                    for (int c = 0; c < 3; ++c)
+                        q[c] = g->grid_origin[c] + (double)i * g->grid_step_x[c] + (double)j * g->grid_step_y[c] +
+                               (double)k * g->grid_step_z[c];
+                }
+        expanded = *g;
+        expanded.scat_posns = grid_positions.data();
+        expanded.grid_shape[0] = expanded.grid_shape[1] = expanded.grid_shape[2] = 0;
+        g = &expanded;
+        grid = false;
+    }
     p->N = N;
     p->S = S;
     p->P = P;
@@ -304,11 +329,13 @@ int build_plan(const sar_geometry* g, sar_plan* p) {
         const double span = std::ceil(vmax) + p->wwin / 2 + 5 - (double)p->bg0;
         if (span > 2.0e9) return fail(SAR_ERR_NOT_SUPPORTED, "range span too large");
         p->Lg = (int)span;
-        // Backprojection staging: pulses per stage so that windows fit shared memory.
+        // Backprojection staging: pulses per stage so that the double-buffered windows of the
+        // pipelined kernel fit shared memory with two CTAs per SM; otherwise read windows
+        // from global memory directly.
         p->staged = false;
         p->pb = 32;
         for (int pb = 32; pb >= 8; pb -= 8)
-            if (bp_grid_smem_bytes(p->wwin, pb, 1) <= kBpSmemBudget) {
+            if (bp_grid_ws_smem_bytes(p->wwin, pb) <= kBpSmemBudget) {
                 p->pb = pb;
                 p->staged = true;
                 break;
@@ -595,7 +622,7 @@ int sar_adjoint(sar_plan* p, const void* y_dev, void* x_dev, void* stream) {
         a.pb = p->pb;
         a.staged = p->staged;
         a.accumulate = 0;
-        SAR_CUDA(launch_bp_grid(a, st), "backprojection");
+        SAR_CUDA(p->staged ? launch_bp_grid_ws(a, st) : launch_bp_grid(a, st), "backprojection");
     } else {
         SAR_CUDA(launch_bp_points(point_args(p, adjoint_bin_offset(p->interp)), p->d_prof, (float2*)x_dev, 0, st),
                  "backprojection");

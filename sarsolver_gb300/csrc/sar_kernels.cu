@@ -261,6 +261,240 @@ cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st) {
     return a.g.precise_bins ? launch_bp_grid_t<false, true>(a, st) : launch_bp_grid_t<false, false>(a, st);
 }
 
+// ------------------------------------------- K2 (grid, warp-specialised pipeline)
+// Producer warp (warp 8): for stage k+1 it computes the (pulse, sub-tile) coefficient sets
+// and the tile base bins, then one lane per pulse issues a 1-D bulk copy (cp.async.bulk) of
+// that pulse's profile window into the stage's shared-memory buffer, completing on the
+// buffer's "full" mbarrier.  Consumer warps (0..7) wait on "full", gather, and arrive on the
+// buffer's "empty" mbarrier, which the producer waits on before reusing the buffer.  Every
+// wait is bounded by a clock budget; on expiry the kernel raises FLAG_WAIT_TIMEOUT and
+// leaves the loop instead of hanging.
+constexpr int kWsConsumers = 256;
+constexpr int kWsThreads = kWsConsumers + 32;
+constexpr long long kWaitBudgetCycles = 4000000000ll;   // ~2 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(smem_addr(bar))
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(
+                     smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+// Bounded wait for completion of the barrier phase with the given parity.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > kWaitBudgetCycles) return false;
+    return true;
+}
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// 1-D bulk copy global -> shared (16-byte aligned addresses, size a multiple of 16).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// Producer: coefficient sets for pulses s0 + pass .. s0 + pass + 7 (lane = 4*pulse + sub-tile).
+__device__ __forceinline__ void producer_coeffs(const GridConst& g, const PulseGeom* __restrict__ pulses, int s0,
+                                                int npb, int pass, const df3* anchors, float4* coef, int* base,
+                                                int lane) {
+    const int pi = pass + (lane >> 2), q = lane & 3;
+    const bool valid = pi < npb;
+    AnchorExpansion ae = {};
+    Coeffs co = {};
+    df vb = df_make(0.0f, 0.0f);
+    if (valid) {
+        const PulseGeom pg = load_pulse(pulses + s0 + pi);
+        ae = expand_anchor(anchors[q], pg, g);
+        phase_coeffs(ae, g, co.c);
+        vb = anchor_bin(ae, g);
+    }
+    const unsigned all = 0xffffffffu;
+    df sum = df_add(vb, df_make(__shfl_xor_sync(all, vb.hi, 1), __shfl_xor_sync(all, vb.lo, 1)));
+    sum = df_add(sum, df_make(__shfl_xor_sync(all, sum.hi, 2), __shfl_xor_sync(all, sum.lo, 2)));
+    int b = base_bin_of(sum, 4.0f);
+    b = __shfl_sync(all, b, lane & ~3);
+    if (valid) {
+        bin_coeffs(ae, vb, b, g, co);
+        float4* dst = coef + (pi * 4 + q) * kSetF4;
+        dst[0] = make_float4(co.c[0], co.c[1], co.c[2], co.c[3]);
+        dst[1] = make_float4(co.c[4], co.c[5], co.c[6], co.c[7]);
+        dst[2] = make_float4(co.c[8], co.c[9], co.v[0], co.v[1]);
+        dst[3] = make_float4(co.v[2], co.v[3], co.v[4], co.v[5]);
+        dst[4] = make_float4(co.ia, co.ib, co.w[0], co.w[1]);
+        dst[5] = make_float4(co.w[2], co.w[3], co.i0, 0.f);
+        if (q == 0) base[pi] = b;
+    }
+}
+
+size_t bp_grid_ws_smem_bytes(int wwin, int pb) {
+    // windows [2][pb][wwin] + coefficient sets [2][pb][4] + base bins [2][pb] + 4 mbarriers + 4 anchors
+    return sizeof(float4) * ((size_t)2 * pb * wwin + (size_t)2 * pb * 4 * kSetF4) + sizeof(int) * 2 * pb +
+           4 * sizeof(uint64_t) + 4 * sizeof(df3);
+}
+
+template <bool PRECISE>
+__global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_kernel(const BpGridArgs a) {
+    extern __shared__ __align__(16) float4 smem[];
+    const int pb = a.pb, ww = a.wwin;
+    float4* win0 = smem;
+    float4* coef0 = win0 + 2 * pb * ww;
+    int* base0 = reinterpret_cast<int*>(coef0 + 2 * pb * 4 * kSetF4);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(base0 + 2 * pb);   // full[0..1], empty[2..3]
+    df3* anchors = reinterpret_cast<df3*>(bars + 4);
+
+    const GridConst& g = a.g;
+    int tile = blockIdx.x;
+    const int ti = tile % g.tiles_x;
+    tile /= g.tiles_x;
+    const int tj = tile % g.tiles_y;
+    const int k = tile / g.tiles_y;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x < 4) anchors[threadIdx.x] = subtile_anchor(ti, tj, k, threadIdx.x, g);
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        mbar_init(&bars[2], kWsConsumers / 32);
+        mbar_init(&bars[3], kWsConsumers / 32);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const int nst = (a.S + pb - 1) / pb;
+
+    if (warp == kWsConsumers / 32) {
+        // ------------------------------------------------------------ producer
+        bool ok = true;
+        int issued = 0;
+        for (int st = 0; st < nst; ++st) {
+            const int b = st & 1;
+            if (st >= 2 && !mbar_wait(&bars[2 + b], ((st - 2) >> 1) & 1)) {
+                ok = false;
+                break;
+            }
+            const int s0 = st * pb, npb = min(pb, a.S - s0);
+            float4* coef = coef0 + b * pb * 4 * kSetF4;
+            int* base = base0 + b * pb;
+            for (int pass = 0; pass < npb; pass += 8) producer_coeffs(g, a.pulses, s0, npb, pass, anchors, coef, base, lane);
+            __syncwarp();
+            if (lane == 0) mbar_arrive_expect_tx(&bars[b], (uint32_t)(npb * ww * sizeof(float4)));
+            if (lane < npb) {
+                long gi = (long)base[lane] - ww / 2 - a.bg0;
+                if (gi < 0 || gi > (long)a.Lg - ww) {
+                    raise_flag(a.flags, FLAG_TILE_WINDOW);
+                    gi = gi < 0 ? 0 : (long)a.Lg - ww;
+                }
+                fence_proxy_async_smem();
+                bulk_g2s(win0 + (size_t)(b * pb + lane) * ww, a.pairs + (size_t)(s0 + lane) * a.Lg + gi,
+                         (uint32_t)(ww * sizeof(float4)), &bars[b]);
+            }
+            issued = st + 1;
+        }
+        // Do not leave while this warp's copies may still be landing (bounded).
+        for (int st = max(0, issued - 2); st < issued; ++st)
+            if (!mbar_wait(&bars[st & 1], (st >> 1) & 1)) ok = false;
+        if (!ok && lane == 0) raise_flag(a.flags, FLAG_WAIT_TIMEOUT);
+        return;
+    }
+
+    // -------------------------------------------------------------- consumers
+    const TileThread tt = tile_thread();
+    float acc_re[4] = {0.f, 0.f, 0.f, 0.f}, acc_im[4] = {0.f, 0.f, 0.f, 0.f};
+    const int half_w = ww / 2;
+    bool ok = true;
+    for (int st = 0; st < nst; ++st) {
+        const int b = st & 1;
+        if (!mbar_wait(&bars[b], (st >> 1) & 1)) {
+            ok = false;
+            break;
+        }
+        const int npb = min(pb, a.S - st * pb);
+        const float4* coef = coef0 + b * pb * 4 * kSetF4;
+        const float4* win = win0 + (size_t)b * pb * ww;
+        float st_re[4] = {0.f, 0.f, 0.f, 0.f}, st_im[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int pi = 0; pi < npb; ++pi) {
+            float c9, w9, ib;
+            const ColumnTerms ct = load_column<PRECISE>(coef + (pi * 4 + tt.q) * kSetF4, tt, c9, w9, ib);
+            const float4* wp = win + pi * ww;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const PixelEval e = eval_pixel<PRECISE>(ct, c9, w9, ib, tt, r);
+                const unsigned idx = min((unsigned)(e.n + half_w), (unsigned)(ww - 1));
+                const float4 pv = wp[idx];
+                const float re = fmaf(e.sf, pv.z, pv.x);
+                const float im = fmaf(e.sf, pv.w, pv.y);
+                float sn, cn;
+                __sincosf(SAR_TWO_PI * e.f, &sn, &cn);
+                st_re[r] = fmaf(re, cn, fmaf(im, sn, st_re[r]));
+                st_im[r] = fmaf(im, cn, fmaf(-re, sn, st_im[r]));
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            acc_re[r] += st_re[r];
+            acc_im[r] += st_im[r];
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&bars[2 + b]);
+    }
+    if (!ok) {
+        if (lane == 0) raise_flag(a.flags, FLAG_WAIT_TIMEOUT);
+        return;
+    }
+    const int i = ti * kTile + lane;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int j = tj * kTile + 4 * warp + r;
+        if (i < g.nx && j < g.ny) {
+            const size_t p = ((size_t)k * g.ny + j) * g.nx + i;
+            float2 o = make_float2(acc_re[r], acc_im[r]);
+            if (a.accumulate) {
+                const float2 old = a.x[p];
+                o.x += old.x;
+                o.y += old.y;
+            }
+            a.x[p] = o;
+        }
+    }
+}
+
+cudaError_t launch_bp_grid_ws(const BpGridArgs& a, cudaStream_t st) {
+    if (a.pb < 1 || a.pb > 32 || a.wwin < 4 || (a.wwin & 3)) return cudaErrorInvalidValue;
+    const size_t smem = bp_grid_ws_smem_bytes(a.wwin, a.pb);
+    const unsigned blocks = (unsigned)(a.g.tiles_x * a.g.tiles_y * a.g.nz);
+    cudaError_t e;
+    if (a.g.precise_bins) {
+        e = cudaFuncSetAttribute(bp_grid_ws_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        bp_grid_ws_kernel<true><<<blocks, kWsThreads, smem, st>>>(a);
+    } else {
+        e = cudaFuncSetAttribute(bp_grid_ws_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        bp_grid_ws_kernel<false><<<blocks, kWsThreads, smem, st>>>(a);
+    }
+    return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------- K3 (grid)
 // CTA = (strip segment of tiles along y, block of pbf pulses).  Contributions of the
 // segment's tiles are accumulated in a shared-memory window per pulse that covers the

@@ -13,6 +13,7 @@ enum : unsigned {
     FLAG_TILE_WINDOW = 1u,    // a tile's staged window left the stored profile span
     FLAG_STRIP_WINDOW = 2u,   // a forward strip window left the stored profile span
     FLAG_BIN_CLAMP = 4u,      // a per-pixel bin index was clamped (debug builds only)
+    FLAG_WAIT_TIMEOUT = 8u,   // a bounded mbarrier wait gave up (the result is invalid)
 };
 
 constexpr int kTile = 32;          // pixels per tile side
@@ -35,6 +36,10 @@ struct BpGridArgs {
 };
 size_t bp_grid_smem_bytes(int wwin, int pb, int staged);
 cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st);
+// Warp-specialised variant: one producer warp computes coefficients and stages windows with
+// bulk copies into a double buffer while eight consumer warps gather (pb <= 32).
+size_t bp_grid_ws_smem_bytes(int wwin, int pb);
+cudaError_t launch_bp_grid_ws(const BpGridArgs& a, cudaStream_t st);
 
 // Forward projection over a regular grid (K3): scatter into strip windows, merge globally.
 struct FpGridArgs {

@@ -33,13 +33,17 @@ class SarPlan:
 
     Parameters mirror NumpySimpleSarOperator (src/sarsolver/numpy/operator.py:12-13):
     ``upsample_ratio`` (default 128, as the reference) and the added ``interp``
-    ("nearest_ref": the reference's bins and conventions; "linear": exact transpose pair).
+    ("nearest_ref": the reference's bins and conventions; "linear": exact transpose pair) and
+    ``path`` ("auto": grid fast path for linear, per-pixel double-float path for nearest_ref;
+    "grid" / "points" force one).
     """
 
     def __init__(self, scene, aperture, upsample_ratio: float = 128.0, interp: str = "nearest_ref",
-                 device: Optional[torch.device] = None):
+                 device: Optional[torch.device] = None, path: str = "auto"):
         if interp not in _lib.INTERP:
             raise ValueError(f"interp must be one of {sorted(_lib.INTERP)}")
+        if path not in _lib.PATH:
+            raise ValueError(f"path must be one of {sorted(_lib.PATH)}")
         if not torch.cuda.is_available():
             raise RuntimeError("SarPlan needs a CUDA device")
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
@@ -73,6 +77,7 @@ class SarPlan:
         g.upsample_ratio = self.upsample_ratio
         g.sign_multiplier = float(aperture.sign_multiplier)
         g.interp = _lib.INTERP[interp]
+        g.path = _lib.PATH[path]
         axes = grid_axes(scene)
         if axes is not None:
             shape, origin, ex, ey, ez = axes
