@@ -193,7 +193,7 @@ def run_ours(args):
     k2_ms = stage_ms[1] / max(calls, 1)
     fft_ms = stage_ms[0] / max(calls, 1)
     achieved = P * S / (k2_ms * 1e-3)
-    traffic = read_profile_traffic("bp_grid")
+    traffic = read_profile_traffic("bp_grid_ws")
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -206,7 +206,7 @@ def run_ours(args):
                          % (S * N * 8 / 1e6, S * plan.profile_length * 16 / 1e6),
                    "parallelism": "replicas (each GPU runs the whole workload)" if world > 1 else "single GPU"},
         "stages_ms": {"upsample_fft_side": fft_ms, "gather_kernel": k2_ms},
-        "roofline": {"bound": "sfu", "kernel": "bp_grid_kernel", "achieved": achieved, "peak": r_roof,
+        "roofline": {"bound": "sfu", "kernel": "bp_grid_ws_kernel", "achieved": achieved, "peak": r_roof,
                      "unit": "px*pulse/s", "frac": achieved / r_roof, "traffic": traffic,
                      "peak_basis": f"{props.multi_processor_count} SMs x {sm_max:.0f} MHz x 16 MUFU/clk/SM / "
                                    "3 MUFU per px*pulse (sm_max_mhz of MEASURED_PEAKS.json)"},

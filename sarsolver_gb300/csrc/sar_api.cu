@@ -107,7 +107,8 @@ struct sar_plan {
     float2* d_w = nullptr;
     float2* d_wadj = nullptr;
     float2* d_wfwd = nullptr;
-    float2* d_spec = nullptr;
+    void* d_spec = nullptr;        // FFT rows: float2, or double2 when fft_double
+    bool fft_double = false;
     float4* d_prof = nullptr;   // [S][Lg] pairs (adjoint) / float2 accumulator (forward)
     int* d_strip = nullptr;
     unsigned* d_flags = nullptr;
@@ -192,18 +193,33 @@ int upload_weights(sar_plan* p, cudaStream_t st, bool sync) {
     return SAR_OK;
 }
 
-int make_fft(cufftHandle* h, long M, int batch) {
+int make_fft(cufftHandle* h, long M, int batch, bool dbl) {
     int n[1] = {(int)M};
-    SAR_CUFFT(cufftPlanMany(h, 1, n, nullptr, 1, (int)M, nullptr, 1, (int)M, CUFFT_C2C, batch), "cufftPlanMany");
+    SAR_CUFFT(cufftPlanMany(h, 1, n, nullptr, 1, (int)M, nullptr, 1, (int)M, dbl ? CUFFT_Z2Z : CUFFT_C2C, batch),
+              "cufftPlanMany");
     return SAR_OK;
 }
 
-int run_fft(sar_plan* p, float2* data, int rows, int direction, cudaStream_t st) {
+int run_fft(sar_plan* p, void* data, int rows, int direction, cudaStream_t st) {
     cufftHandle h = (rows == p->chunk) ? p->fft_full : p->fft_tail;
     SAR_CUFFT(cufftSetStream(h, st), "cufftSetStream");
-    SAR_CUFFT(cufftExecC2C(h, reinterpret_cast<cufftComplex*>(data), reinterpret_cast<cufftComplex*>(data), direction),
-              "cufftExecC2C");
+    if (p->fft_double)
+        SAR_CUFFT(cufftExecZ2Z(h, reinterpret_cast<cufftDoubleComplex*>(data),
+                               reinterpret_cast<cufftDoubleComplex*>(data), direction),
+                  "cufftExecZ2Z");
+    else
+        SAR_CUFFT(cufftExecC2C(h, reinterpret_cast<cufftComplex*>(data), reinterpret_cast<cufftComplex*>(data),
+                               direction),
+                  "cufftExecC2C");
     return SAR_OK;
+}
+
+// Working lengths with a prime factor above 7 go through a double-precision transform: the
+// single-precision transform of such lengths measured ~1e-4 relative image error.
+bool smooth_length(size_t m) {
+    for (size_t f : {2, 3, 5, 7})
+        while (m % f == 0) m /= f;
+    return m == 1;
 }
 
 // Host-only validation of a geometry description (no CUDA call).
@@ -486,14 +502,20 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
     if ((rc = p->alloc(&p->d_prof, (size_t)S * p->Lg, "range profiles"))) return rc;
 
     // ---- FFT work rows
-    const size_t row_bytes = M * sizeof(float2);
-    p->chunk = (int)std::min<size_t>(S, std::max<size_t>(1, kSpecBudget / row_bytes));
-    if ((rc = p->alloc(&p->d_spec, (size_t)p->chunk * M, "FFT rows"))) return rc;
-    if ((rc = make_fft(&p->fft_full, (long)M, p->chunk))) return rc;
+    p->fft_double = !smooth_length(M);
+    const size_t elem = p->fft_double ? sizeof(double2) : sizeof(float2);
+    p->chunk = (int)std::min<size_t>(S, std::max<size_t>(1, kSpecBudget / (M * elem)));
+    {
+        double2* spec = nullptr;
+        if ((rc = p->alloc(&spec, ((size_t)p->chunk * M * elem + sizeof(double2) - 1) / sizeof(double2), "FFT rows")))
+            return rc;
+        p->d_spec = spec;
+    }
+    if ((rc = make_fft(&p->fft_full, (long)M, p->chunk, p->fft_double))) return rc;
     p->have_full = true;
     const int tail = (int)(S % (size_t)p->chunk);
     if (tail) {
-        if ((rc = make_fft(&p->fft_tail, (long)M, tail))) return rc;
+        if ((rc = make_fft(&p->fft_tail, (long)M, tail, p->fft_double))) return rc;
         p->have_tail = true;
     }
     return SAR_OK;
@@ -566,15 +588,17 @@ int sar_plan_get_info(const sar_plan* p, sar_plan_info* info) {
 static int upsample_into_pairs(sar_plan* p, const float2* y, cudaStream_t st, bool pairs_out, float2* prof) {
     for (size_t first = 0; first < p->S; first += (size_t)p->chunk) {
         const int rows = (int)std::min<size_t>(p->chunk, p->S - first);
-        SAR_CUDA(launch_pack_adjoint(y, p->d_wave, p->d_spec, (int)p->N, (long)p->M, rows, (int)first, st), "pack");
+        const int dbl = p->fft_double;
+        SAR_CUDA(launch_pack_adjoint(y, p->d_wave, p->d_spec, dbl, (int)p->N, (long)p->M, rows, (int)first, st), "pack");
         int rc = run_fft(p, p->d_spec, rows, CUFFT_INVERSE, st);
         if (rc) return rc;
         if (pairs_out)
-            SAR_CUDA(launch_unpack_pairs(p->d_spec, p->d_wadj, p->d_prof, (long)p->M, p->Lg, p->bg0, rows, (int)first,
-                                         p->interp == SAR_INTERP_LINEAR, st),
+            SAR_CUDA(launch_unpack_pairs(p->d_spec, dbl, p->d_wadj, p->d_prof, (long)p->M, p->Lg, p->bg0, rows,
+                                         (int)first, p->interp == SAR_INTERP_LINEAR, st),
                      "unpack");
         else
-            SAR_CUDA(launch_unpack_profiles(p->d_spec, prof, (long)p->M, p->Lg, p->bg0, rows, (int)first, st), "unpack");
+            SAR_CUDA(launch_unpack_profiles(p->d_spec, dbl, prof, (long)p->M, p->Lg, p->bg0, rows, (int)first, st),
+                     "unpack");
     }
     return SAR_OK;
 }
@@ -668,11 +692,12 @@ int sar_forward(sar_plan* p, const void* x_dev, void* y_dev, void* stream) {
     mark(ev, 2, st);
     for (size_t first = 0; first < p->S; first += (size_t)p->chunk) {
         const int rows = (int)std::min<size_t>(p->chunk, p->S - first);
-        SAR_CUDA(launch_pack_forward(acc, p->d_spec, (long)p->M, p->Lg, p->bg0, rows, (int)first, st), "pack");
+        SAR_CUDA(launch_pack_forward(acc, p->d_spec, p->fft_double, (long)p->M, p->Lg, p->bg0, rows, (int)first, st),
+                 "pack");
         int rc = run_fft(p, p->d_spec, rows, CUFFT_FORWARD, st);
         if (rc) return rc;
-        SAR_CUDA(launch_extract_forward(p->d_spec, p->d_wave, p->d_wfwd, (float2*)y_dev, (int)p->N, (long)p->M, rows,
-                                        (int)first, st),
+        SAR_CUDA(launch_extract_forward(p->d_spec, p->fft_double, p->d_wave, p->d_wfwd, (float2*)y_dev, (int)p->N,
+                                        (long)p->M, rows, (int)first, st),
                  "extract");
     }
     mark(ev, 3, st);

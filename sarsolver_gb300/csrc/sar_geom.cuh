@@ -86,16 +86,43 @@ SAR_HD df df_mulf(df a, float b) {
     float e = fmaf(a.lo, b, p.lo);
     return fast_two_sum(p.hi, e);
 }
-// sqrt(a) for a.hi > 0: correctly rounded FP32 root plus one Newton correction.
-SAR_HD df df_sqrt(df a) {
-    float r = sqrtf(a.hi);
-    float e = fmaf(-r, r, a.hi) + a.lo;
-    return fast_two_sum(r, e / (2.0f * r));
+// Approximate reciprocal and reciprocal square root (about 1 ulp): the hardware approximations
+// on the device, correctly rounded equivalents on the host.  The double-float routines below
+// only use them as starting points and correct the result with one exact residual, so the
+// double-float accuracy does not depend on their last bit.
+SAR_HD float approx_rcp(float x) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return 1.0f / x;
+#endif
 }
+SAR_HD float approx_rsqrt(float x) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return 1.0f / sqrtf(x);
+#endif
+}
+// sqrt(a) for a.hi > 0: r0 = a.hi * rsqrt(a.hi), then the Newton correction
+// (a - r0^2) / (2 r0) from the exact FMA residual (Karp-Markstein form).
+SAR_HD df df_sqrt(df a) {
+    const float y = approx_rsqrt(a.hi);
+    const float r = a.hi * y;
+    const float e = fmaf(-r, r, a.hi) + a.lo;
+    return fast_two_sum(r, e * (0.5f * y));
+}
+// a / b: q1 = a.hi / b.hi from the approximate reciprocal, then the correction from the
+// double-float residual a - b q1 (Markstein-style refinement).
 SAR_HD df df_div(df a, df b) {
-    float q1 = a.hi / b.hi;
-    df r = df_sub(a, df_mulf(b, q1));
-    float q2 = r.hi / b.hi;
+    const float inv = approx_rcp(b.hi);
+    const float q1 = a.hi * inv;
+    const df r = df_sub(a, df_mulf(b, q1));
+    const float q2 = r.hi * inv;
     return fast_two_sum(q1, q2);
 }
 SAR_HD df df_dot3(const df3& a, const df3& b) {
@@ -208,7 +235,7 @@ SAR_HD AntennaTerms expand_antenna(const df3& anchor, const df3& antenna, const 
     t.gx = df_div(df_dot3(w, g.ex), t.R);
     t.gy = df_div(df_dot3(w, g.ey), t.R);
     const float ux = t.gx.hi, uy = t.gy.hi;
-    const float inv = 1.0f / t.R.hi;
+    const float inv = approx_rcp(t.R.hi);
     const float pxx = g.exx - ux * ux;
     const float pxy = g.exy - ux * uy;
     const float pyy = g.eyy - uy * uy;

@@ -270,7 +270,8 @@ cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st) {
 // wait is bounded by a clock budget; on expiry the kernel raises FLAG_WAIT_TIMEOUT and
 // leaves the loop instead of hanging.
 constexpr int kWsConsumers = 256;
-constexpr int kWsThreads = kWsConsumers + 32;
+constexpr int kWsProducers = 2;   // producer warps; producer w handles pulse passes 8w, 8w + 16, ...
+constexpr int kWsThreads = kWsConsumers + 32 * kWsProducers;
 constexpr long long kWaitBudgetCycles = 4000000000ll;   // ~2 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -373,8 +374,8 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_kernel(const BpGridA
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x < 4) anchors[threadIdx.x] = subtile_anchor(ti, tj, k, threadIdx.x, g);
     if (threadIdx.x == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        mbar_init(&bars[0], kWsProducers);
+        mbar_init(&bars[1], kWsProducers);
         mbar_init(&bars[2], kWsConsumers / 32);
         mbar_init(&bars[3], kWsConsumers / 32);
         mbar_fence_init();
@@ -382,8 +383,9 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_kernel(const BpGridA
     __syncthreads();
     const int nst = (a.S + pb - 1) / pb;
 
-    if (warp == kWsConsumers / 32) {
-        // ------------------------------------------------------------ producer
+    if (warp >= kWsConsumers / 32) {
+        // ----------------------------------------------------------- producers
+        const int pw = warp - kWsConsumers / 32;
         bool ok = true;
         int issued = 0;
         for (int st = 0; st < nst; ++st) {
@@ -395,18 +397,25 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_kernel(const BpGridA
             const int s0 = st * pb, npb = min(pb, a.S - s0);
             float4* coef = coef0 + b * pb * 4 * kSetF4;
             int* base = base0 + b * pb;
-            for (int pass = 0; pass < npb; pass += 8) producer_coeffs(g, a.pulses, s0, npb, pass, anchors, coef, base, lane);
+            int mine = 0;   // pulses of this stage staged by this warp
+            for (int pass = 8 * pw; pass < npb; pass += 8 * kWsProducers) {
+                producer_coeffs(g, a.pulses, s0, npb, pass, anchors, coef, base, lane);
+                mine += min(8, npb - pass);
+            }
             __syncwarp();
-            if (lane == 0) mbar_arrive_expect_tx(&bars[b], (uint32_t)(npb * ww * sizeof(float4)));
-            if (lane < npb) {
-                long gi = (long)base[lane] - ww / 2 - a.bg0;
-                if (gi < 0 || gi > (long)a.Lg - ww) {
-                    raise_flag(a.flags, FLAG_TILE_WINDOW);
-                    gi = gi < 0 ? 0 : (long)a.Lg - ww;
+            if (lane == 0) mbar_arrive_expect_tx(&bars[b], (uint32_t)(mine * ww * sizeof(float4)));
+            for (int pass = 8 * pw; pass < npb; pass += 8 * kWsProducers) {
+                const int pi = pass + lane;
+                if (lane < 8 && pi < npb) {
+                    long gi = (long)base[pi] - ww / 2 - a.bg0;
+                    if (gi < 0 || gi > (long)a.Lg - ww) {
+                        raise_flag(a.flags, FLAG_TILE_WINDOW);
+                        gi = gi < 0 ? 0 : (long)a.Lg - ww;
+                    }
+                    fence_proxy_async_smem();
+                    bulk_g2s(win0 + (size_t)(b * pb + pi) * ww, a.pairs + (size_t)(s0 + pi) * a.Lg + gi,
+                             (uint32_t)(ww * sizeof(float4)), &bars[b]);
                 }
-                fence_proxy_async_smem();
-                bulk_g2s(win0 + (size_t)(b * pb + lane) * ww, a.pairs + (size_t)(s0 + lane) * a.Lg + gi,
-                         (uint32_t)(ww * sizeof(float4)), &bars[b]);
             }
             issued = st + 1;
         }
@@ -737,10 +746,22 @@ __device__ __forceinline__ long pos_mod(long a, long m) {
     return r < 0 ? r + m : r;
 }
 
+// Spectrum rows are complex64 (float2) or, for working lengths with large prime factors
+// where the FP32 transform loses accuracy, complex128 (double2).
+__device__ __forceinline__ float2 to_f2(float2 v) { return v; }
+__device__ __forceinline__ float2 to_f2(double2 v) { return make_float2((float)v.x, (float)v.y); }
+template <class T>
+__device__ __forceinline__ T make_spec(float x, float y);
+template <>
+__device__ __forceinline__ float2 make_spec<float2>(float x, float y) { return make_float2(x, y); }
+template <>
+__device__ __forceinline__ double2 make_spec<double2>(float x, float y) { return make_double2(x, y); }
+
 // spec[row][m] = conj(W[i]) y_fft[i] placed at the zero-padded position of FFT index i
 // (sarsolver_cxx.cpp:331-342); y is read from its fftshifted layout.
+template <class T>
 __global__ void pack_adjoint_kernel(const float2* __restrict__ y, const float2* __restrict__ wave,
-                                    float2* __restrict__ spec, int N, long M, int first) {
+                                    T* __restrict__ spec, int N, long M, int first) {
     const long m = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M) return;
     const long row = blockIdx.y;
@@ -758,13 +779,14 @@ __global__ void pack_adjoint_kernel(const float2* __restrict__ y, const float2* 
         const float2 w = __ldg(wave + i);
         v = make_float2(w.x * yv.x + w.y * yv.y, w.x * yv.y - w.y * yv.x);
     }
-    spec[row * M + m] = v;
+    spec[row * M + m] = make_spec<T>(v.x, v.y);
 }
 
 // pairs[s][w] for bin b = bg0 + w: (p(b) + 0.5 d, d) with d = p(b+1) - p(b), both scaled by
 // the pulse factor (linear); (p(b), 0) for nearest-bin sampling.  Bins wrap modulo M
 // (sarsolver_cxx.cpp:22-24).
-__global__ void unpack_pairs_kernel(const float2* __restrict__ spec, const float2* __restrict__ wfac,
+template <class T>
+__global__ void unpack_pairs_kernel(const T* __restrict__ spec, const float2* __restrict__ wfac,
                                     float4* __restrict__ pairs, long M, int Lg, long bg0, int first,
                                     int linear) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
@@ -773,11 +795,11 @@ __global__ void unpack_pairs_kernel(const float2* __restrict__ spec, const float
     const long m0 = pos_mod(bg0 + w, M);
     const long m1 = (m0 + 1 == M) ? 0 : m0 + 1;
     const float2 f = __ldg(wfac + first + row);
-    const float2 a = spec[row * M + m0];
+    const float2 a = to_f2(spec[row * M + m0]);
     const float2 p0 = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
     float4 out;
     if (linear) {
-        const float2 b = spec[row * M + m1];
+        const float2 b = to_f2(spec[row * M + m1]);
         const float2 p1 = make_float2(b.x * f.x - b.y * f.y, b.x * f.y + b.y * f.x);
         const float dx = p1.x - p0.x, dy = p1.y - p0.y;
         out = make_float4(fmaf(0.5f, dx, p0.x), fmaf(0.5f, dy, p0.y), dx, dy);
@@ -787,17 +809,19 @@ __global__ void unpack_pairs_kernel(const float2* __restrict__ spec, const float
     pairs[(size_t)(first + row) * Lg + w] = out;
 }
 
-__global__ void unpack_profiles_kernel(const float2* __restrict__ spec, float2* __restrict__ prof, long M,
-                                       int Lg, long bg0, int first) {
+template <class T>
+__global__ void unpack_profiles_kernel(const T* __restrict__ spec, float2* __restrict__ prof, long M, int Lg,
+                                       long bg0, int first) {
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= Lg) return;
     const long row = blockIdx.y;
-    prof[(size_t)(first + row) * Lg + w] = spec[row * M + pos_mod(bg0 + w, M)];
+    prof[(size_t)(first + row) * Lg + w] = to_f2(spec[row * M + pos_mod(bg0 + w, M)]);
 }
 
 // spec[row][m] = sum of accumulated bins congruent to m modulo M.
-__global__ void pack_forward_kernel(const float2* __restrict__ acc, float2* __restrict__ spec, long M, int Lg,
-                                    long bg0, int first) {
+template <class T>
+__global__ void pack_forward_kernel(const float2* __restrict__ acc, T* __restrict__ spec, long M, int Lg, long bg0,
+                                    int first) {
     const long m = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M) return;
     const long row = blockIdx.y;
@@ -807,12 +831,13 @@ __global__ void pack_forward_kernel(const float2* __restrict__ acc, float2* __re
         s.x += v.x;
         s.y += v.y;
     }
-    spec[row * M + m] = s;
+    spec[row * M + m] = make_spec<T>(s.x, s.y);
 }
 
 // y_fft[i] = W[i] K[i] (low half), W[N-1-i] K[M-1-i] (high half), odd middle
 // (sarsolver_cxx.cpp:295-307), times the pulse factor, written fftshifted (forward.py:44).
-__global__ void extract_forward_kernel(const float2* __restrict__ spec, const float2* __restrict__ wave,
+template <class T>
+__global__ void extract_forward_kernel(const T* __restrict__ spec, const float2* __restrict__ wave,
                                        const float2* __restrict__ wfac, float2* __restrict__ y, int N, long M,
                                        int first) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -826,7 +851,7 @@ __global__ void extract_forward_kernel(const float2* __restrict__ spec, const fl
         m = M - N + i;
     else
         m = half;
-    const float2 k = spec[row * M + m];
+    const float2 k = to_f2(spec[row * M + m]);
     const float2 w = __ldg(wave + i);
     const float2 f = __ldg(wfac + first + row);
     const float2 a = make_float2(w.x * k.x - w.y * k.y, w.x * k.y + w.y * k.x);
@@ -841,38 +866,53 @@ __global__ void weights_kernel(const float2* __restrict__ w, float2* wadj, float
     wadj[s] = conj_adjoint ? make_float2(v.x, -v.y) : v;
 }
 
-cudaError_t launch_pack_adjoint(const float2* y, const float2* wave, float2* spec, int N, long M, int rows,
+cudaError_t launch_pack_adjoint(const float2* y, const float2* wave, void* spec, int dbl, int N, long M, int rows,
                                 int first, cudaStream_t st) {
     const dim3 grid((unsigned)((M + 255) / 256), (unsigned)rows);
-    pack_adjoint_kernel<<<grid, 256, 0, st>>>(y, wave, spec, N, M, first);
+    if (dbl)
+        pack_adjoint_kernel<double2><<<grid, 256, 0, st>>>(y, wave, (double2*)spec, N, M, first);
+    else
+        pack_adjoint_kernel<float2><<<grid, 256, 0, st>>>(y, wave, (float2*)spec, N, M, first);
     return cudaGetLastError();
 }
 
-cudaError_t launch_unpack_pairs(const float2* spec, const float2* wfac, float4* pairs, long M, int Lg, long bg0,
-                                int rows, int first, int linear, cudaStream_t st) {
+cudaError_t launch_unpack_pairs(const void* spec, int dbl, const float2* wfac, float4* pairs, long M, int Lg,
+                                long bg0, int rows, int first, int linear, cudaStream_t st) {
     const dim3 grid((unsigned)((Lg + 255) / 256), (unsigned)rows);
-    unpack_pairs_kernel<<<grid, 256, 0, st>>>(spec, wfac, pairs, M, Lg, bg0, first, linear);
+    if (dbl)
+        unpack_pairs_kernel<double2><<<grid, 256, 0, st>>>((const double2*)spec, wfac, pairs, M, Lg, bg0, first, linear);
+    else
+        unpack_pairs_kernel<float2><<<grid, 256, 0, st>>>((const float2*)spec, wfac, pairs, M, Lg, bg0, first, linear);
     return cudaGetLastError();
 }
 
-cudaError_t launch_unpack_profiles(const float2* spec, float2* prof, long M, int Lg, long bg0, int rows, int first,
-                                   cudaStream_t st) {
+cudaError_t launch_unpack_profiles(const void* spec, int dbl, float2* prof, long M, int Lg, long bg0, int rows,
+                                   int first, cudaStream_t st) {
     const dim3 grid((unsigned)((Lg + 255) / 256), (unsigned)rows);
-    unpack_profiles_kernel<<<grid, 256, 0, st>>>(spec, prof, M, Lg, bg0, first);
+    if (dbl)
+        unpack_profiles_kernel<double2><<<grid, 256, 0, st>>>((const double2*)spec, prof, M, Lg, bg0, first);
+    else
+        unpack_profiles_kernel<float2><<<grid, 256, 0, st>>>((const float2*)spec, prof, M, Lg, bg0, first);
     return cudaGetLastError();
 }
 
-cudaError_t launch_pack_forward(const float2* acc, float2* spec, long M, int Lg, long bg0, int rows, int first,
+cudaError_t launch_pack_forward(const float2* acc, void* spec, int dbl, long M, int Lg, long bg0, int rows, int first,
                                 cudaStream_t st) {
     const dim3 grid((unsigned)((M + 255) / 256), (unsigned)rows);
-    pack_forward_kernel<<<grid, 256, 0, st>>>(acc, spec, M, Lg, bg0, first);
+    if (dbl)
+        pack_forward_kernel<double2><<<grid, 256, 0, st>>>(acc, (double2*)spec, M, Lg, bg0, first);
+    else
+        pack_forward_kernel<float2><<<grid, 256, 0, st>>>(acc, (float2*)spec, M, Lg, bg0, first);
     return cudaGetLastError();
 }
 
-cudaError_t launch_extract_forward(const float2* spec, const float2* wave, const float2* wfac, float2* y, int N,
-                                   long M, int rows, int first, cudaStream_t st) {
+cudaError_t launch_extract_forward(const void* spec, int dbl, const float2* wave, const float2* wfac, float2* y,
+                                   int N, long M, int rows, int first, cudaStream_t st) {
     const dim3 grid((unsigned)((N + 255) / 256), (unsigned)rows);
-    extract_forward_kernel<<<grid, 256, 0, st>>>(spec, wave, wfac, y, N, M, first);
+    if (dbl)
+        extract_forward_kernel<double2><<<grid, 256, 0, st>>>((const double2*)spec, wave, wfac, y, N, M, first);
+    else
+        extract_forward_kernel<float2><<<grid, 256, 0, st>>>((const float2*)spec, wave, wfac, y, N, M, first);
     return cudaGetLastError();
 }
 

@@ -74,17 +74,18 @@ cudaError_t launch_bp_points(const PointArgs& a, const float4* pairs, float2* x,
                              cudaStream_t st);
 cudaError_t launch_fp_points(const PointArgs& a, const float2* x, float2* acc, cudaStream_t st);
 
-// FFT-side kernels (K1 / K4).  y is [S][N] fftshifted along fast time; spec is [rows][M].
-cudaError_t launch_pack_adjoint(const float2* y, const float2* wave, float2* spec, int N, long M,
-                                int rows, int first, cudaStream_t st);
-cudaError_t launch_unpack_pairs(const float2* spec, const float2* wfac, float4* pairs, long M,
-                                int Lg, long bg0, int rows, int first, int linear, cudaStream_t st);
-cudaError_t launch_unpack_profiles(const float2* spec, float2* prof, long M, int Lg, long bg0,
-                                   int rows, int first, cudaStream_t st);
-cudaError_t launch_pack_forward(const float2* acc, float2* spec, long M, int Lg, long bg0, int rows,
+// FFT-side kernels (K1 / K4).  y is [S][N] fftshifted along fast time; spec is [rows][M] of
+// complex64, or complex128 when dbl != 0.
+cudaError_t launch_pack_adjoint(const float2* y, const float2* wave, void* spec, int dbl, int N, long M, int rows,
                                 int first, cudaStream_t st);
-cudaError_t launch_extract_forward(const float2* spec, const float2* wave, const float2* wfac,
-                                   float2* y, int N, long M, int rows, int first, cudaStream_t st);
+cudaError_t launch_unpack_pairs(const void* spec, int dbl, const float2* wfac, float4* pairs, long M, int Lg,
+                                long bg0, int rows, int first, int linear, cudaStream_t st);
+cudaError_t launch_unpack_profiles(const void* spec, int dbl, float2* prof, long M, int Lg, long bg0, int rows,
+                                   int first, cudaStream_t st);
+cudaError_t launch_pack_forward(const float2* acc, void* spec, int dbl, long M, int Lg, long bg0, int rows, int first,
+                                cudaStream_t st);
+cudaError_t launch_extract_forward(const void* spec, int dbl, const float2* wave, const float2* wfac, float2* y,
+                                   int N, long M, int rows, int first, cudaStream_t st);
 cudaError_t launch_weights(const float2* w, float2* wadj, float2* wfwd, int S, int conj_adjoint,
                            cudaStream_t st);
 

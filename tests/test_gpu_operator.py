@@ -144,6 +144,17 @@ def test_profiles_match_oracle_upsampling():
     assert rel_l2(prof, full[:, bins]) < 2.0e-6
 
 
+def test_profiles_prime_factor_length():
+    """Working length M = 251 * 128 (the reference's little case): the double-precision
+    transform keeps the upsampled profiles at FP32 accuracy."""
+    case = load_golden("little")
+    plan = SarPlan(case.scene, case.aperture, interp="linear")
+    prof = plan.profiles(torch.from_numpy(case.data["y"])).cpu().numpy()
+    full = oracle.upsample(case.problem(), case.data["y"], threads=8)
+    bins = (plan.profile_first_bin + np.arange(plan.profile_length)) % full.shape[1]
+    assert rel_l2(prof, full[:, bins]) < 1.0e-6
+
+
 def test_dropin_struct_entry_points():
     """forward_evaluate / adjoint_evaluate with the reference's SarCalculationInfo."""
     case = load_golden("spot_small")
