@@ -94,8 +94,12 @@ extern "C" int sar_geom_host_eval_points(const double* origin, size_t num_points
             r = df_add(r, pg.monostatic != 0.0f ? r : point_range(ar, ar2, pt));
             r = df_sub(r, df_make(pg.rref_hi, pg.rref_lo));
             phase_out[s * num_points + p] = df_frac(df_mul(kap, r));
+            // the kernel's two-step rounding (bin index n1 + n2, coordinate frac - n2)
             df v = df_mul(sr, r);
-            bin_out[s * num_points + p] = (double)v.hi + (double)v.lo + (double)bin_offset;
+            const float n1 = round_shift(v.hi);
+            const float frac = (v.hi - n1) + (v.lo + bin_offset);
+            const float n2 = round_shift(frac);
+            bin_out[s * num_points + p] = (double)n1 + (double)n2 + (double)(frac - n2);
         }
     }
     return 0;

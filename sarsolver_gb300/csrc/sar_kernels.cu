@@ -290,12 +290,14 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
                  "r"(bytes)
                  : "memory");
 }
+// try_wait with a suspend-time hint: the warp sleeps until the phase completes (or ~1 ms
+// passes) instead of spinning on issue slots the gathering warps need.
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     uint32_t done;
     asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(done)
-        : "r"(smem_addr(bar)), "r"(parity)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(1000000u)
         : "memory");
     return done != 0;
 }
@@ -643,10 +645,13 @@ __device__ __forceinline__ PointEval eval_point(const PointArgs& a, const PulseG
     PointEval e;
     e.f = df_frac(df_mul(a.kappa, r));
     const df V = df_sub(df_mul(a.s_r, r), df_make((float)a.bg0, 0.0f));
-    const float tail = V.lo + a.bin_offset;
-    const float n = round_shift(V.hi + tail);
-    e.sf = (V.hi - n) + tail;
-    e.gi = min(max((int)n, 0), a.Lg - 2);
+    // Round in two exact steps: the integer nearest V.hi, then the small remainder; rounding
+    // V.hi + tail directly in FP32 would decide the bin at the resolution of V.hi (1e-4 bins).
+    const float n1 = round_shift(V.hi);
+    const float frac = (V.hi - n1) + (V.lo + a.bin_offset);
+    const float n2 = round_shift(frac);
+    e.sf = frac - n2;
+    e.gi = min(max((int)n1 + (int)n2, 0), a.Lg - 2);
     return e;
 }
 

@@ -134,3 +134,32 @@ def test_precise_bins_match_fp64_rounding_at_short_range_and_fine_bins():
         assert err < max_err, (precise, err)
         if max_flips is not None:
             assert flips <= max_flips, flips
+
+
+def test_point_scheme_bins_match_fp64_rounding():
+    """Per-pixel double-float scheme on the reference's 'little' case: bin index and in-bin
+    coordinate recombined exactly as the kernel rounds them; no nearest-bin decision differs."""
+    lib = _lib.load_host()
+    case = load_golden("little")
+    ap = case.aperture
+    M = int(128 * ap.num_freqs)
+    s_r = ap.sample_bandwidth * M / (ap.num_freqs * ap.c_eff)
+    kappa = ap.centre_frequency / ap.c_eff
+    pos = np.ascontiguousarray(case.scene.positions)
+    S, P = ap.num_slow_times, pos.shape[0]
+    origin = 0.5 * (pos.min(0) + pos.max(0))
+    ph = np.zeros((S, P), np.float32)
+    bn = np.zeros((S, P))
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in
+            (origin, pos, ap.transmitter_positions, ap.receiver_positions, ap.stab_ref_posns)]
+    lib.sar_geom_host_eval_points(arrs[0].ctypes.data, P, arrs[1].ctypes.data, S, arrs[2].ctypes.data,
+                                  arrs[3].ctypes.data, arrs[4].ctypes.data, kappa, s_r, 0.5, ph.ctypes.data,
+                                  bn.ctypes.data)
+    flips = 0
+    for s in range(S):
+        _, tb = fp64_truth(ap.transmitter_positions[s], ap.receiver_positions[s], ap.stab_ref_posns[s], pos,
+                           kappa, s_r)
+        v = tb + 0.5
+        assert np.abs(bn[s] - v).max() < 1e-6
+        flips += int(np.sum(np.round(v) != np.round(bn[s])))
+    assert flips == 0
