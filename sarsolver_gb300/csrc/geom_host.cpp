@@ -94,12 +94,16 @@ extern "C" int sar_geom_host_eval_points(const double* origin, size_t num_points
             r = df_add(r, pg.monostatic != 0.0f ? r : point_range(ar, ar2, pt));
             r = df_sub(r, df_make(pg.rref_hi, pg.rref_lo));
             phase_out[s * num_points + p] = df_frac(df_mul(kap, r));
-            // the kernel's two-step rounding (bin index n1 + n2, coordinate frac - n2)
-            df v = df_mul(sr, r);
-            const float n1 = round_shift(v.hi);
-            const float frac = (v.hi - n1) + (v.lo + bin_offset);
-            const float n2 = round_shift(frac);
-            bin_out[s * num_points + p] = (double)n1 + (double)n2 + (double)(frac - n2);
+            // the kernel's bin rule: bin_offset -0.5 linear, +0.5 adjoint nearest, 0 forward nearest
+            const df v = df_mul(sr, r);
+            const int rule = bin_offset < 0.0f ? BIN_LINEAR : (bin_offset > 0.0f ? BIN_ADJ_NEAREST : BIN_FWD_NEAREST);
+            int gi;
+            float sf;
+            exact_bin(v, 0, rule, &gi, &sf);
+            // linear: position of v itself; nearest: the chosen bin (+0.5 for the adjoint rule so
+            // that round() of the result reproduces the kernel's choice, as for FP64 v + 0.5)
+            bin_out[s * num_points + p] = rule == BIN_LINEAR ? (double)gi + (double)sf + 0.5
+                                                             : (double)gi + (rule == BIN_ADJ_NEAREST ? 0.0 : 0.0);
         }
     }
     return 0;

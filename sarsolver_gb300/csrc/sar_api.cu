@@ -603,14 +603,14 @@ static int upsample_into_pairs(sar_plan* p, const float2* y, cudaStream_t st, bo
     return SAR_OK;
 }
 
-static PointArgs point_args(sar_plan* p, float bin_offset) {
+static PointArgs point_args(sar_plan* p, int bin_rule) {
     PointArgs a;
     a.pulses = p->d_pulses;
     a.alpha2 = p->d_alpha2;
     a.points = p->d_points;
     a.kappa = p->kappa;
     a.s_r = p->s_r;
-    a.bin_offset = bin_offset;
+    a.bin_rule = bin_rule;
     a.S = (int)p->S;
     a.P = (int)p->P;
     a.Lg = p->Lg;
@@ -648,7 +648,7 @@ int sar_adjoint(sar_plan* p, const void* y_dev, void* x_dev, void* stream) {
         a.accumulate = 0;
         SAR_CUDA(p->staged ? launch_bp_grid_ws(a, st) : launch_bp_grid(a, st), "backprojection");
     } else {
-        SAR_CUDA(launch_bp_points(point_args(p, adjoint_bin_offset(p->interp)), p->d_prof, (float2*)x_dev, 0, st),
+        SAR_CUDA(launch_bp_points(point_args(p, p->interp == SAR_INTERP_LINEAR ? BIN_LINEAR : BIN_ADJ_NEAREST), p->d_prof, (float2*)x_dev, 0, st),
                  "backprojection");
     }
     mark(ev, 2, st);
@@ -686,7 +686,7 @@ int sar_forward(sar_plan* p, const void* x_dev, void* y_dev, void* stream) {
         a.linear = p->interp == SAR_INTERP_LINEAR;
         SAR_CUDA(launch_fp_grid(a, st), "forward scatter");
     } else {
-        SAR_CUDA(launch_fp_points(point_args(p, forward_bin_offset(p->interp)), (const float2*)x_dev, acc, st),
+        SAR_CUDA(launch_fp_points(point_args(p, p->interp == SAR_INTERP_LINEAR ? BIN_LINEAR : BIN_FWD_NEAREST), (const float2*)x_dev, acc, st),
                  "forward scatter");
     }
     mark(ev, 2, st);

@@ -419,6 +419,42 @@ SAR_HD BinPos bin_position(float v, float ni) {
 }
 
 // ------------------------------------------------ unstructured positions (scheme 2)
+// Bin of a double-float bin position V (relative to the first stored bin base0), for the
+// three sampling rules:
+//   BIN_LINEAR      floor(v) and the coordinate sf = v - floor(v) - 0.5 in [-0.5, 0.5]
+//   BIN_ADJ_NEAREST round(0.5 + v)   (sarsolver_cxx.cpp:347)
+//   BIN_FWD_NEAREST round(v)         (sarsolver_cxx.cpp:289)
+// with round() halfway cases away from zero as std::round.  n1 = rint(V.hi) is exact and
+// t = V.hi - n1 is exact; the nearest-bin decisions then compare t (or t -+ 0.5, also exact)
+// with -V.lo through FP32 sums whose sign is exact, so the chosen bin equals the one FP64
+// rounding of the same double-float value gives, including ties.
+enum BinRule { BIN_LINEAR = 0, BIN_ADJ_NEAREST = 1, BIN_FWD_NEAREST = 2 };
+
+SAR_HD void exact_bin(df V, int base0, int rule, int* gi, float* sf) {
+    const float n1 = round_shift(V.hi);
+    const float t = V.hi - n1;
+    const bool nonneg = (int)n1 + base0 >= 0;   // sign of the absolute bin, for halfway cases
+    int n2 = 0;
+    *sf = 0.0f;
+    if (rule == BIN_LINEAR) {
+        const float frac = t + (V.lo - 0.5f);
+        const float r = round_shift(frac);
+        n2 = (int)r;
+        *sf = frac - r;
+    } else if (rule == BIN_ADJ_NEAREST) {
+        const float u = t + V.lo;          // round(0.5 + n1 + u) = n1 + [u > 0, or u == 0 and v >= 0]
+        n2 = (u > 0.0f || (u == 0.0f && nonneg)) ? 1 : 0;
+    } else {
+        const float up = (t - 0.5f) + V.lo;    // u - 0.5
+        const float dn = (t + 0.5f) + V.lo;    // u + 0.5
+        if (up > 0.0f || (up == 0.0f && nonneg))
+            n2 = 1;
+        else if (dn < 0.0f || (dn == 0.0f && !nonneg))
+            n2 = -1;
+    }
+    *gi = (int)n1 + n2;
+}
+
 // Per pixel: q = p - origin as hi/lo and |q|^2 as hi/lo.
 struct PointGeom {
     float qh[4];   // qx, qy, qz, |q|^2 (hi)

@@ -143,7 +143,7 @@ __device__ __forceinline__ PixelEval eval_pixel(const ColumnTerms& ct, float c9,
                                                 const TileThread& tt, int r) {
     PixelEval e;
     const float ph = pixel_phase(ct, c9, tt.dj[r], tt.dj2[r], tt.dj3[r]);
-    e.f = ph - round_shift(ph);
+    e.f = ph - rintf(ph);   // exact: |ph| < 2^22
     const float v = pixel_bin<PRECISE>(ct, w9, tt.dj[r], tt.dj2[r], tt.dj3[r]);
     const BinPos b = bin_position<PRECISE>(v, PRECISE ? fmaf(ib, tt.dj[r], ct.ci) : 0.f);
     e.sf = b.s;
@@ -290,24 +290,26 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
                  "r"(bytes)
                  : "memory");
 }
-// try_wait with a suspend-time hint: the warp sleeps until the phase completes (or ~1 ms
-// passes) instead of spinning on issue slots the gathering warps need.
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     uint32_t done;
     asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(done)
-        : "r"(smem_addr(bar)), "r"(parity), "r"(1000000u)
+        : "r"(smem_addr(bar)), "r"(parity)
         : "memory");
     return done != 0;
 }
-// Bounded wait for completion of the barrier phase with the given parity.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+// Bounded wait for completion of the barrier phase with the given parity.  Between polls the
+// warp sleeps for backoff_ns so that waiting warps leave the issue slots to the gathering
+// warps; the wait gives up after kWaitBudgetCycles.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned backoff_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity))
+    while (true) {
+        __nanosleep(backoff_ns);
+        if (mbar_try_wait(bar, parity)) return true;
         if (clock64() - t0 > kWaitBudgetCycles) return false;
-    return true;
+    }
 }
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 // 1-D bulk copy global -> shared (16-byte aligned addresses, size a multiple of 16).
@@ -392,7 +394,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_kernel(const BpGridA
         int issued = 0;
         for (int st = 0; st < nst; ++st) {
             const int b = st & 1;
-            if (st >= 2 && !mbar_wait(&bars[2 + b], ((st - 2) >> 1) & 1)) {
+            if (st >= 2 && !mbar_wait(&bars[2 + b], ((st - 2) >> 1) & 1, 1000)) {
                 ok = false;
                 break;
             }
@@ -423,7 +425,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_kernel(const BpGridA
         }
         // Do not leave while this warp's copies may still be landing (bounded).
         for (int st = max(0, issued - 2); st < issued; ++st)
-            if (!mbar_wait(&bars[st & 1], (st >> 1) & 1)) ok = false;
+            if (!mbar_wait(&bars[st & 1], (st >> 1) & 1, 1000)) ok = false;
         if (!ok && lane == 0) raise_flag(a.flags, FLAG_WAIT_TIMEOUT);
         return;
     }
@@ -435,7 +437,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_kernel(const BpGridA
     bool ok = true;
     for (int st = 0; st < nst; ++st) {
         const int b = st & 1;
-        if (!mbar_wait(&bars[b], (st >> 1) & 1)) {
+        if (!mbar_wait(&bars[b], (st >> 1) & 1, 64)) {
             ok = false;
             break;
         }
@@ -443,6 +445,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_kernel(const BpGridA
         const float4* coef = coef0 + b * pb * 4 * kSetF4;
         const float4* win = win0 + (size_t)b * pb * ww;
         float st_re[4] = {0.f, 0.f, 0.f, 0.f}, st_im[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 2
         for (int pi = 0; pi < npb; ++pi) {
             float c9, w9, ib;
             const ColumnTerms ct = load_column<PRECISE>(coef + (pi * 4 + tt.q) * kSetF4, tt, c9, w9, ib);
@@ -645,13 +648,9 @@ __device__ __forceinline__ PointEval eval_point(const PointArgs& a, const PulseG
     PointEval e;
     e.f = df_frac(df_mul(a.kappa, r));
     const df V = df_sub(df_mul(a.s_r, r), df_make((float)a.bg0, 0.0f));
-    // Round in two exact steps: the integer nearest V.hi, then the small remainder; rounding
-    // V.hi + tail directly in FP32 would decide the bin at the resolution of V.hi (1e-4 bins).
-    const float n1 = round_shift(V.hi);
-    const float frac = (V.hi - n1) + (V.lo + a.bin_offset);
-    const float n2 = round_shift(frac);
-    e.sf = frac - n2;
-    e.gi = min(max((int)n1 + (int)n2, 0), a.Lg - 2);
+    int gi;
+    exact_bin(V, a.bg0, a.bin_rule, &gi, &e.sf);
+    e.gi = min(max(gi, 0), a.Lg - 2);
     return e;
 }
 

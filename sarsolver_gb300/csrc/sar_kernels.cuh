@@ -65,7 +65,7 @@ struct PointArgs {
     const float4* alpha2;      // [S]: |tx-o|^2 (hi, lo), |rx-o|^2 (hi, lo)
     const PointGeom* points;   // [P]
     df kappa, s_r;
-    float bin_offset;
+    int bin_rule;              // BinRule (sar_geom.cuh)
     int S, P, Lg, bg0;
     int linear;                // forward scatter weights: 1 linear, 0 nearest bin
     unsigned* flags;

@@ -102,8 +102,9 @@ def test_unstructured_point_precision():
     ph = np.zeros((S, P), np.float32)
     bn = np.zeros((S, P))
     arrs = [np.ascontiguousarray(a) for a in (origin, pos, tx, rx, srp)]
+    # bin rule -0.5 (linear): the harness returns the bin position itself
     lib.sar_geom_host_eval_points(arrs[0].ctypes.data, P, arrs[1].ctypes.data, S, arrs[2].ctypes.data,
-                                  arrs[3].ctypes.data, arrs[4].ctypes.data, kappa, s_r, 0.0, ph.ctypes.data,
+                                  arrs[3].ctypes.data, arrs[4].ctypes.data, kappa, s_r, -0.5, ph.ctypes.data,
                                   bn.ctypes.data)
     for s in range(S):
         tp, tb = fp64_truth(tx[s], rx[s], srp[s], pos, kappa, s_r)
@@ -136,9 +137,16 @@ def test_precise_bins_match_fp64_rounding_at_short_range_and_fine_bins():
             assert flips <= max_flips, flips
 
 
-def test_point_scheme_bins_match_fp64_rounding():
-    """Per-pixel double-float scheme on the reference's 'little' case: bin index and in-bin
-    coordinate recombined exactly as the kernel rounds them; no nearest-bin decision differs."""
+def std_round(x):
+    """C++ std::round: halfway cases away from zero."""
+    return np.sign(x) * np.floor(np.abs(x) + 0.5)
+
+
+@pytest.mark.parametrize("rule,offset", [("adjoint", 0.5), ("forward", 0.0)])
+def test_point_scheme_bins_match_fp64_rounding(rule, offset):
+    """Per-pixel double-float scheme on the reference's 'little' case (upsample 128): the
+    nearest bin chosen by the kernel's exact rule equals std::round of the FP64 position,
+    round(0.5 + v) for the adjoint (sarsolver_cxx.cpp:347), round(v) forward (:289)."""
     lib = _lib.load_host()
     case = load_golden("little")
     ap = case.aperture
@@ -153,13 +161,11 @@ def test_point_scheme_bins_match_fp64_rounding():
     arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in
             (origin, pos, ap.transmitter_positions, ap.receiver_positions, ap.stab_ref_posns)]
     lib.sar_geom_host_eval_points(arrs[0].ctypes.data, P, arrs[1].ctypes.data, S, arrs[2].ctypes.data,
-                                  arrs[3].ctypes.data, arrs[4].ctypes.data, kappa, s_r, 0.5, ph.ctypes.data,
+                                  arrs[3].ctypes.data, arrs[4].ctypes.data, kappa, s_r, offset, ph.ctypes.data,
                                   bn.ctypes.data)
     flips = 0
     for s in range(S):
         _, tb = fp64_truth(ap.transmitter_positions[s], ap.receiver_positions[s], ap.stab_ref_posns[s], pos,
                            kappa, s_r)
-        v = tb + 0.5
-        assert np.abs(bn[s] - v).max() < 1e-6
-        flips += int(np.sum(np.round(v) != np.round(bn[s])))
+        flips += int(np.sum(std_round(tb + offset) != bn[s]))
     assert flips == 0
