@@ -300,15 +300,18 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return done != 0;
 }
 // Bounded wait for completion of the barrier phase with the given parity.  Between polls the
-// warp sleeps for backoff_ns so that waiting warps leave the issue slots to the gathering
-// warps; the wait gives up after kWaitBudgetCycles.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned backoff_ns) {
+// warp sleeps with exponential backoff (first_ns doubling up to max_ns), so waiting warps leave
+// the issue slots to the gathering warps and poll only a few times per wait; the wait gives up
+// after kWaitBudgetCycles.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned first_ns, unsigned max_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
+    unsigned ns = first_ns;
     while (true) {
-        __nanosleep(backoff_ns);
+        __nanosleep(ns);
         if (mbar_try_wait(bar, parity)) return true;
         if (clock64() - t0 > kWaitBudgetCycles) return false;
+        ns = min(2 * ns, max_ns);
     }
 }
 __device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
@@ -394,7 +397,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_kernel(const BpGridA
         int issued = 0;
         for (int st = 0; st < nst; ++st) {
             const int b = st & 1;
-            if (st >= 2 && !mbar_wait(&bars[2 + b], ((st - 2) >> 1) & 1, 1000)) {
+            if (st >= 2 && !mbar_wait(&bars[2 + b], ((st - 2) >> 1) & 1, 128, 2048)) {
                 ok = false;
                 break;
             }
@@ -425,7 +428,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_kernel(const BpGridA
         }
         // Do not leave while this warp's copies may still be landing (bounded).
         for (int st = max(0, issued - 2); st < issued; ++st)
-            if (!mbar_wait(&bars[st & 1], (st >> 1) & 1, 1000)) ok = false;
+            if (!mbar_wait(&bars[st & 1], (st >> 1) & 1, 128, 2048)) ok = false;
         if (!ok && lane == 0) raise_flag(a.flags, FLAG_WAIT_TIMEOUT);
         return;
     }
@@ -437,7 +440,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_kernel(const BpGridA
     bool ok = true;
     for (int st = 0; st < nst; ++st) {
         const int b = st & 1;
-        if (!mbar_wait(&bars[b], (st >> 1) & 1, 64)) {
+        if (!mbar_wait(&bars[b], (st >> 1) & 1, 32, 256)) {
             ok = false;
             break;
         }
