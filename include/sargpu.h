@@ -144,6 +144,28 @@ int sar_stage_times(sar_plan *plan, float *ms /* [3] */, int *calls);
 /* Synchronise the plan's last stream, return and clear the device check flags. */
 int sar_device_flags(sar_plan *plan, unsigned *flags);
 
+/* Backprojection x = A^H y from upsampled range profiles, without allocating device memory.
+ * No counterpart in the reference (its kernel allocates host buffers per call and has no GPU).
+ *
+ * For callers that cannot call cudaMalloc while they run: code running inside another
+ * runtime's memory pool or arena, real-time loops that must not allocate after start-up, and
+ * hosts whose device allocator belongs to another framework.  Everything else above allocates
+ * (plans hold FFT rows and profile buffers; cuFFT plans allocate work areas); this call does not.
+ *
+ * Inputs: the geometry on the host (a regular grid is required), the upsampled profiles on the
+ * device as complex64 [S][span], column w holding range bin first_bin + w -- exactly what
+ * sar_profiles() writes for a plan of the same geometry (profile_first_bin, profile_length).
+ * Output: x_dev, complex64 [P].  Asynchronous on `stream`.
+ *
+ * Scratch lives in one fixed 32 MiB device array inside the library (every GPU that loads the
+ * library holds it until exit): pulses x span x 16 bytes of profile pairs plus 72 bytes per pulse
+ * must fit, otherwise SAR_ERR_INVALID_ARGUMENT with a message (sar_last_error).  The array is
+ * shared by all calls and keeps the last call's contents; calls that overlap on the GPU race on
+ * it, so order them on one stream.  The first call on each device resolves the array's device
+ * address (cudaGetSymbolAddress, with that device current); make it before any stream capture. */
+int sar_adjoint_from_profiles_noalloc(const sar_geometry *geom, const void *prof_dev, long first_bin,
+                                      size_t span, void *x_dev, void *stream);
+
 /* Last error message of the calling thread (empty if none); returns its full length. */
 size_t sar_last_error(char *buf, size_t len);
 const char *sar_status_string(int status);

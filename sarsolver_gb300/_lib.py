@@ -29,6 +29,7 @@ EXPORTED = (
     "sar_set_slow_time_weighting", "sar_set_slow_time_weighting_device",
     "sar_device_flags", "sar_last_error", "sar_status_string",
     "sar_enable_stage_timing", "sar_stage_times",
+    "sar_adjoint_from_profiles_noalloc",
 )
 
 

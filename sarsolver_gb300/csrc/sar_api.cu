@@ -83,6 +83,8 @@ constexpr size_t kSpecBudget = (size_t)4 << 30;   // bytes of FFT work rows per 
 
 }  // namespace
 
+void sar::sar_internal_set_error(const char* msg) { g_last_error = msg ? msg : ""; }
+
 struct sar_plan {
     int device = 0;
     size_t N = 0, S = 0, P = 0, M = 0;

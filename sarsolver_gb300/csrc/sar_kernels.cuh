@@ -89,4 +89,7 @@ cudaError_t launch_extract_forward(const void* spec, int dbl, const float2* wave
 cudaError_t launch_weights(const float2* w, float2* wadj, float2* wfwd, int S, int conj_adjoint,
                            cudaStream_t st);
 
+// Sets the calling thread's sar_last_error() text (library-internal, not exported).
+__attribute__((visibility("hidden"))) void sar_internal_set_error(const char* msg);
+
 }  // namespace sar
