@@ -78,7 +78,7 @@ bool finite3(const double* v, size_t n) {
 
 // Shared-memory budgets: two tile CTAs per SM.
 constexpr size_t kBpSmemBudget = 110 * 1024;
-constexpr size_t kFpSmemBudget = 100 * 1024;
+constexpr size_t kFpSmemBudget = 110 * 1024;
 constexpr size_t kSpecBudget = (size_t)4 << 30;   // bytes of FFT work rows per chunk
 
 }  // namespace
@@ -386,7 +386,7 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
                             }
                         }
                 const int ws = (need + 31) & ~31;
-                if (fp_grid_smem_bytes(ws, pbf) <= kFpSmemBudget) {
+                if (fp_grid_ws_smem_bytes(ws, pbf) <= kFpSmemBudget) {
                     p->seg_tiles = seg;
                     p->segs_per_column = segs;
                     p->ws = ws;
@@ -686,7 +686,7 @@ int sar_forward(sar_plan* p, const void* x_dev, void* y_dev, void* stream) {
         a.ws = p->ws;
         a.pbf = p->pbf;
         a.linear = p->interp == SAR_INTERP_LINEAR;
-        SAR_CUDA(launch_fp_grid(a, st), "forward scatter");
+        SAR_CUDA(launch_fp_grid_ws(a, st), "forward scatter");
     } else {
         SAR_CUDA(launch_fp_points(point_args(p, p->interp == SAR_INTERP_LINEAR ? BIN_LINEAR : BIN_FWD_NEAREST), (const float2*)x_dev, acc, st),
                  "forward scatter");

@@ -622,6 +622,248 @@ cudaError_t launch_fp_grid(const FpGridArgs& a, cudaStream_t st) {
     return a.g.precise_bins ? launch_fp_grid_t<false, true>(a, st) : launch_fp_grid_t<false, false>(a, st);
 }
 
+// ------------------------------------------- K3 (grid, warp-specialised pipeline)
+// CTA = (strip segment of tiles along y, block of pbf pulses), 8 gathering warps + 2 producers,
+// pipelined per tile with two buffers.  Producers, per tile: load the tile's image values into
+// shared memory, compute the coefficient sets of every (pulse, sub-tile) and a per-pulse "fast"
+// flag, then arrive on the buffer's "full" mbarrier.  Gathering warp w owns pulses w, w+8, ...:
+// for each, lanes run along the tile's x axis and the warp walks the 32 rows; contributions go
+// to the pulse's shared-memory window, which only this warp touches.  When the bin rate along x
+// is at least 1.05 bins/pixel over the whole tile (checked by the producer from the quadratic
+// bin model, with margin for FP32 rounding), the 32 lanes of a row always hit 32 distinct bins,
+// so plain read-modify-writes are safe: first to bin n, then to bin n + 1, with __syncwarp in
+// between.  Otherwise shared-memory atomics are used.  After the strip the windows are merged
+// into the global accumulator with one atomic add per bin.
+constexpr float kFastBinRate = 1.05f;
+
+__device__ __forceinline__ size_t align_up(size_t n, size_t a) { return (n + a - 1) & ~(a - 1); }
+
+struct FpWsLayout {
+    size_t win, coef, xt, base, fast, wst, bars, anchors, total;
+};
+
+__host__ __device__ inline FpWsLayout fp_ws_layout(int ws, int pbf) {
+    FpWsLayout L;
+    L.win = 0;
+    L.coef = L.win + (size_t)pbf * ws * sizeof(float2);
+    L.coef = (L.coef + 15) & ~(size_t)15;
+    L.xt = L.coef + (size_t)2 * pbf * 4 * kSetF4 * sizeof(float4);
+    L.base = L.xt + (size_t)2 * kTile * kTile * sizeof(float2);
+    L.fast = L.base + (size_t)2 * pbf * sizeof(int);
+    L.wst = L.fast + (size_t)2 * pbf * sizeof(int);
+    L.bars = (L.wst + (size_t)pbf * sizeof(int) + 7) & ~(size_t)7;
+    L.anchors = L.bars + 4 * sizeof(uint64_t);
+    L.total = L.anchors + (size_t)kWsProducers * 4 * sizeof(df3);
+    return L;
+}
+
+size_t fp_grid_ws_smem_bytes(int ws, int pbf) { return fp_ws_layout(ws, pbf).total; }
+
+template <bool LINEAR, bool PRECISE>
+__global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridArgs a) {
+    extern __shared__ __align__(16) unsigned char fsm[];
+    const int pbf = a.pbf, ws = a.ws;
+    const FpWsLayout L = fp_ws_layout(ws, pbf);
+    float2* win = reinterpret_cast<float2*>(fsm + L.win);
+    float4* coef0 = reinterpret_cast<float4*>(fsm + L.coef);
+    float2* xt0 = reinterpret_cast<float2*>(fsm + L.xt);
+    int* base0 = reinterpret_cast<int*>(fsm + L.base);
+    int* fast0 = reinterpret_cast<int*>(fsm + L.fast);
+    int* wst = reinterpret_cast<int*>(fsm + L.wst);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(fsm + L.bars);   // full[0..1], empty[2..3]
+    df3* anchors_all = reinterpret_cast<df3*>(fsm + L.anchors);
+
+    const GridConst& g = a.g;
+    int bidx = blockIdx.x;
+    const int seg = bidx % a.segs_per_column;
+    bidx /= a.segs_per_column;
+    const int ti = bidx % g.tiles_x;
+    const int k = bidx / g.tiles_x;
+    const int strip = (k * g.tiles_x + ti) * a.segs_per_column + seg;
+    const int s0 = blockIdx.y * pbf;
+    const int npb = min(pbf, a.S - s0);
+    const int tj0 = seg * a.seg_tiles;
+    const int ntile = min(a.seg_tiles, g.tiles_y - tj0);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    for (int e = threadIdx.x; e < pbf * ws; e += blockDim.x) win[e] = make_float2(0.f, 0.f);
+    for (int e = threadIdx.x; e < npb; e += blockDim.x) wst[e] = a.strip_start[(size_t)strip * a.S + s0 + e];
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], kWsProducers);
+        mbar_init(&bars[1], kWsProducers);
+        mbar_init(&bars[2], kWsConsumers / 32);
+        mbar_init(&bars[3], kWsConsumers / 32);
+        mbar_fence_init();
+    }
+    __syncthreads();
+
+    if (warp >= kWsConsumers / 32) {
+        // ----------------------------------------------------------- producers
+        const int pw = warp - kWsConsumers / 32;
+        df3* anchors = anchors_all + 4 * pw;
+        for (int t = 0; t < ntile; ++t) {
+            const int b = t & 1;
+            if (t >= 2 && !mbar_wait(&bars[2 + b], ((t - 2) >> 1) & 1, 128, 2048)) {
+                if (lane == 0) raise_flag(a.flags, FLAG_WAIT_TIMEOUT);
+                return;   // the gathering warps time out on "full" and leave as well
+            }
+            const int tj = tj0 + t;
+            if (lane < 4) anchors[lane] = subtile_anchor(ti, tj, k, lane, g);
+            // this warp's half of the tile's image values (rows 16 pw .. 16 pw + 15)
+            float2* xt = xt0 + b * kTile * kTile;
+            const int i = ti * kTile + lane;
+            for (int r = 16 * pw; r < 16 * pw + 16; ++r) {
+                const int j = tj * kTile + r;
+                xt[r * kTile + lane] =
+                    (i < g.nx && j < g.ny) ? a.x[((size_t)k * g.ny + j) * g.nx + i] : make_float2(0.f, 0.f);
+            }
+            __syncwarp();
+            float4* coef = coef0 + b * pbf * 4 * kSetF4;
+            int* base = base0 + b * pbf;
+            int* fast = fast0 + b * pbf;
+            for (int pass = 8 * pw; pass < npb; pass += 8 * kWsProducers) {
+                producer_coeffs(g, a.pulses, s0, npb, pass, anchors, coef, base, lane);
+                __syncwarp();
+                // Distinct-bin guarantee along x for each pulse of the pass: the smallest
+                // |dv/di| over the sub-tile from the quadratic bin model (di, dj in [-8, 7]).
+                // The rate must also have one sign in all four sub-tiles, so that bins along a
+                // row are monotonic across the sub-tile boundary.
+                const int pi = pass + (lane >> 2), q = lane & 3;
+                bool ok_q = true, pos_q = true;
+                if (pi < npb) {
+                    const float4* cs = coef + (pi * 4 + q) * kSetF4;
+                    const float4 C = cs[2], D = cs[3], E = cs[4];
+                    const float r1 = C.w + E.x;                     // v1 (+ ia in precise mode)
+                    ok_q = fabsf(r1) - 16.0f * fabsf(D.y) - 8.0f * fabsf(D.z) >= kFastBinRate;
+                    pos_q = r1 > 0.0f;
+                }
+                const unsigned all4 = __ballot_sync(0xffffffffu, ok_q);
+                const unsigned pos4 = __ballot_sync(0xffffffffu, pos_q);
+                const unsigned grp = lane & ~3;
+                const unsigned sgn = (pos4 >> grp) & 0xFu;
+                if (pi < npb && q == 0) fast[pi] = ((all4 >> grp) & 0xFu) == 0xFu && (sgn == 0xFu || sgn == 0u);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&bars[b]);
+        }
+        return;
+    }
+
+    // ------------------------------------------------------------------ gathering warps
+    const int qx = lane >= 16;
+    const float di = (float)(lane - 8 - 16 * qx);
+    TileThread tt;
+    tt.q = qx;
+    tt.di = di;
+    tt.di2 = di * di;
+    tt.di3 = tt.di2 * di;
+    bool ok = true;
+    for (int t = 0; t < ntile; ++t) {
+        const int b = t & 1;
+        if (ok && !mbar_wait(&bars[b], (t >> 1) & 1, 32, 256)) ok = false;
+        if (ok) {
+            const float4* coef = coef0 + b * pbf * 4 * kSetF4;
+            const float2* xt = xt0 + b * kTile * kTile;
+            for (int p = warp; p < npb; p += kWsConsumers / 32) {
+                float2* wp = win + p * ws;
+                const int off = base0[b * pbf + p] - wst[p];
+                const bool fast = fast0[b * pbf + p] != 0;
+#pragma unroll
+                for (int half = 0; half < 2; ++half) {
+                    float c9, w9, ib;
+                    const ColumnTerms ct =
+                        load_column<PRECISE>(coef + (p * 4 + qx + 2 * half) * kSetF4, tt, c9, w9, ib);
+#pragma unroll 4
+                    for (int rr = 0; rr < 16; ++rr) {
+                        const float dj = (float)(rr - 8);
+                        const float ph = pixel_phase(ct, c9, dj, dj * dj, dj * dj * dj);
+                        const float f = ph - rintf(ph);
+                        const float v = pixel_bin<PRECISE>(ct, w9, dj, dj * dj, dj * dj * dj);
+                        const BinPos bp = bin_position<PRECISE>(v, PRECISE ? fmaf(ib, dj, ct.ci) : 0.f);
+                        const float2 xv = xt[(16 * half + rr) * kTile + lane];
+                        float sn, cn;
+                        __sincosf(SAR_TWO_PI * f, &sn, &cn);
+                        const float cr = xv.x * cn - xv.y * sn;
+                        const float ci = fmaf(xv.x, sn, xv.y * cn);
+                        const unsigned idx = min((unsigned)(bp.n + off), (unsigned)(ws - 2));
+                        if (fast) {
+                            if (LINEAR) {
+                                const float w0 = 0.5f - bp.s, w1 = 0.5f + bp.s;
+                                float2 u = wp[idx];
+                                u.x = fmaf(w0, cr, u.x);
+                                u.y = fmaf(w0, ci, u.y);
+                                wp[idx] = u;
+                                __syncwarp();
+                                float2 v2 = wp[idx + 1];
+                                v2.x = fmaf(w1, cr, v2.x);
+                                v2.y = fmaf(w1, ci, v2.y);
+                                wp[idx + 1] = v2;
+                                __syncwarp();
+                            } else {
+                                float2 u = wp[idx];
+                                u.x += cr;
+                                u.y += ci;
+                                wp[idx] = u;
+                                __syncwarp();
+                            }
+                        } else if (LINEAR) {
+                            const float w0 = 0.5f - bp.s, w1 = 0.5f + bp.s;
+                            atomicAdd(&wp[idx].x, w0 * cr);
+                            atomicAdd(&wp[idx].y, w0 * ci);
+                            atomicAdd(&wp[idx + 1].x, w1 * cr);
+                            atomicAdd(&wp[idx + 1].y, w1 * ci);
+                        } else {
+                            atomicAdd(&wp[idx].x, cr);
+                            atomicAdd(&wp[idx].y, ci);
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&bars[2 + b]);
+    }
+    if (!ok) {
+        if (lane == 0) raise_flag(a.flags, FLAG_WAIT_TIMEOUT);
+        return;
+    }
+    // merge this warp's windows into the global accumulator
+    __syncwarp();
+    for (int p = warp; p < npb; p += kWsConsumers / 32) {
+        const float2* wp = win + p * ws;
+        for (int w = lane; w < ws; w += 32) {
+            const float2 v = wp[w];
+            if (v.x == 0.f && v.y == 0.f) continue;
+            const long gi = (long)wst[p] + w - a.bg0;
+            if (gi < 0 || gi >= a.Lg) {
+                raise_flag(a.flags, FLAG_STRIP_WINDOW);
+                continue;
+            }
+            float2* dst = a.acc + (size_t)(s0 + p) * a.Lg + gi;
+            atomicAdd(&dst->x, v.x);
+            atomicAdd(&dst->y, v.y);
+        }
+    }
+}
+
+template <bool LINEAR, bool PRECISE>
+static cudaError_t launch_fp_grid_ws_t(const FpGridArgs& a, cudaStream_t st) {
+    const size_t smem = fp_grid_ws_smem_bytes(a.ws, a.pbf);
+    const dim3 grid((unsigned)(a.segs_per_column * a.g.tiles_x * a.g.nz), (unsigned)((a.S + a.pbf - 1) / a.pbf));
+    cudaError_t e = cudaFuncSetAttribute(fp_grid_ws_kernel<LINEAR, PRECISE>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    fp_grid_ws_kernel<LINEAR, PRECISE><<<grid, kWsThreads, smem, st>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fp_grid_ws(const FpGridArgs& a, cudaStream_t st) {
+    if (a.pbf < 8 || a.pbf > 32 || (a.pbf & 7) || a.ws < 32 || (a.ws & 31)) return cudaErrorInvalidValue;
+    if (a.linear)
+        return a.g.precise_bins ? launch_fp_grid_ws_t<true, true>(a, st) : launch_fp_grid_ws_t<true, false>(a, st);
+    return a.g.precise_bins ? launch_fp_grid_ws_t<false, true>(a, st) : launch_fp_grid_ws_t<false, false>(a, st);
+}
+
 // ------------------------------------------------------- K2 / K3 (points)
 constexpr int kPointThreads = 256;
 constexpr int kPointPulses = 64;
