@@ -729,19 +729,24 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                 // The rate must also have one sign in all four sub-tiles, so that bins along a
                 // row are monotonic across the sub-tile boundary.
                 const int pi = pass + (lane >> 2), q = lane & 3;
-                bool ok_q = true, pos_q = true;
+                bool ok_q = true, wide_q = true, pos_q = true;
                 if (pi < npb) {
                     const float4* cs = coef + (pi * 4 + q) * kSetF4;
                     const float4 C = cs[2], D = cs[3], E = cs[4];
                     const float r1 = C.w + E.x;                     // v1 (+ ia in precise mode)
-                    ok_q = fabsf(r1) - 16.0f * fabsf(D.y) - 8.0f * fabsf(D.z) >= kFastBinRate;
+                    const float rmin = fabsf(r1) - 16.0f * fabsf(D.y) - 8.0f * fabsf(D.z);
+                    ok_q = rmin >= kFastBinRate;
+                    wide_q = rmin >= kFastBinRate + 1.0f;
                     pos_q = r1 > 0.0f;
                 }
                 const unsigned all4 = __ballot_sync(0xffffffffu, ok_q);
+                const unsigned wide4 = __ballot_sync(0xffffffffu, wide_q);
                 const unsigned pos4 = __ballot_sync(0xffffffffu, pos_q);
                 const unsigned grp = lane & ~3;
                 const unsigned sgn = (pos4 >> grp) & 0xFu;
-                if (pi < npb && q == 0) fast[pi] = ((all4 >> grp) & 0xFu) == 0xFu && (sgn == 0xFu || sgn == 0u);
+                const bool mono = sgn == 0xFu || sgn == 0u;
+                if (pi < npb && q == 0)
+                    fast[pi] = !mono ? 0 : (((wide4 >> grp) & 0xFu) == 0xFu ? 2 : (((all4 >> grp) & 0xFu) == 0xFu ? 1 : 0));
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&bars[b]);
@@ -764,57 +769,103 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
         if (ok) {
             const float4* coef = coef0 + b * pbf * 4 * kSetF4;
             const float2* xt = xt0 + b * kTile * kTile;
-            for (int p = warp; p < npb; p += kWsConsumers / 32) {
+            // Pulses are processed in pairs (p, p + 8): both share each image value and give the
+            // warp two independent accumulation chains.
+            for (int p = warp; p < npb; p += 2 * (kWsConsumers / 32)) {
+                const int p2 = p + kWsConsumers / 32;
+                const bool two = p2 < npb;
+                const int pq = two ? p2 : p;   // second pulse (a repeat of the first when absent)
                 float2* wp = win + p * ws;
-                const int off = base0[b * pbf + p] - wst[p];
-                const bool fast = fast0[b * pbf + p] != 0;
+                float2* wq = win + pq * ws;
+                const int off_p = base0[b * pbf + p] - wst[p];
+                const int off_q = base0[b * pbf + pq] - wst[pq];
+                const int mode = two ? min(fast0[b * pbf + p], fast0[b * pbf + p2]) : fast0[b * pbf + p];
 #pragma unroll
                 for (int half = 0; half < 2; ++half) {
-                    float c9, w9, ib;
-                    const ColumnTerms ct =
-                        load_column<PRECISE>(coef + (p * 4 + qx + 2 * half) * kSetF4, tt, c9, w9, ib);
-#pragma unroll 4
+                    float c9p, w9p, ibp, c9q, w9q, ibq;
+                    const ColumnTerms ctp =
+                        load_column<PRECISE>(coef + (p * 4 + qx + 2 * half) * kSetF4, tt, c9p, w9p, ibp);
+                    const ColumnTerms ctq =
+                        load_column<PRECISE>(coef + (pq * 4 + qx + 2 * half) * kSetF4, tt, c9q, w9q, ibq);
+#pragma unroll 2
                     for (int rr = 0; rr < 16; ++rr) {
-                        const float dj = (float)(rr - 8);
-                        const float ph = pixel_phase(ct, c9, dj, dj * dj, dj * dj * dj);
-                        const float f = ph - rintf(ph);
-                        const float v = pixel_bin<PRECISE>(ct, w9, dj, dj * dj, dj * dj * dj);
-                        const BinPos bp = bin_position<PRECISE>(v, PRECISE ? fmaf(ib, dj, ct.ci) : 0.f);
+                        const float dj = (float)(rr - 8), dj2 = dj * dj, dj3 = dj2 * dj;
                         const float2 xv = xt[(16 * half + rr) * kTile + lane];
-                        float sn, cn;
-                        __sincosf(SAR_TWO_PI * f, &sn, &cn);
-                        const float cr = xv.x * cn - xv.y * sn;
-                        const float ci = fmaf(xv.x, sn, xv.y * cn);
-                        const unsigned idx = min((unsigned)(bp.n + off), (unsigned)(ws - 2));
-                        if (fast) {
-                            if (LINEAR) {
-                                const float w0 = 0.5f - bp.s, w1 = 0.5f + bp.s;
-                                float2 u = wp[idx];
-                                u.x = fmaf(w0, cr, u.x);
-                                u.y = fmaf(w0, ci, u.y);
-                                wp[idx] = u;
+                        // pulse p
+                        const float php = pixel_phase(ctp, c9p, dj, dj2, dj3);
+                        const float vp = pixel_bin<PRECISE>(ctp, w9p, dj, dj2, dj3);
+                        const BinPos bpp = bin_position<PRECISE>(vp, PRECISE ? fmaf(ibp, dj, ctp.ci) : 0.f);
+                        float snp, cnp;
+                        __sincosf(SAR_TWO_PI * (php - rintf(php)), &snp, &cnp);
+                        const float crp = xv.x * cnp - xv.y * snp, cip = fmaf(xv.x, snp, xv.y * cnp);
+                        const unsigned ip = min((unsigned)(bpp.n + off_p), (unsigned)(ws - 2));
+                        // pulse q
+                        const float phq = pixel_phase(ctq, c9q, dj, dj2, dj3);
+                        const float vq = pixel_bin<PRECISE>(ctq, w9q, dj, dj2, dj3);
+                        const BinPos bpq = bin_position<PRECISE>(vq, PRECISE ? fmaf(ibq, dj, ctq.ci) : 0.f);
+                        float snq, cnq;
+                        __sincosf(SAR_TWO_PI * (phq - rintf(phq)), &snq, &cnq);
+                        const float crq = xv.x * cnq - xv.y * snq, ciq = fmaf(xv.x, snq, xv.y * cnq);
+                        const unsigned iq = min((unsigned)(bpq.n + off_q), (unsigned)(ws - 2));
+                        if (LINEAR) {
+                            const float w0p = 0.5f - bpp.s, w1p = 0.5f + bpp.s;
+                            const float w0q = 0.5f - bpq.s, w1q = 0.5f + bpq.s;
+                            // (wq aliases wp when there is no second pulse: its update is skipped)
+                            if (mode == 2) {
+                                // bins n, n+1 of different lanes are disjoint: one phase per row
+                                float2 a0 = wp[ip], a1 = wp[ip + 1];
+                                a0.x = fmaf(w0p, crp, a0.x); a0.y = fmaf(w0p, cip, a0.y);
+                                a1.x = fmaf(w1p, crp, a1.x); a1.y = fmaf(w1p, cip, a1.y);
+                                wp[ip] = a0; wp[ip + 1] = a1;
+                                if (two) {
+                                    float2 b0 = wq[iq], b1 = wq[iq + 1];
+                                    b0.x = fmaf(w0q, crq, b0.x); b0.y = fmaf(w0q, ciq, b0.y);
+                                    b1.x = fmaf(w1q, crq, b1.x); b1.y = fmaf(w1q, ciq, b1.y);
+                                    wq[iq] = b0; wq[iq + 1] = b1;
+                                }
                                 __syncwarp();
-                                float2 v2 = wp[idx + 1];
-                                v2.x = fmaf(w1, cr, v2.x);
-                                v2.y = fmaf(w1, ci, v2.y);
-                                wp[idx + 1] = v2;
+                            } else if (mode == 1) {
+                                float2 a0 = wp[ip];
+                                a0.x = fmaf(w0p, crp, a0.x); a0.y = fmaf(w0p, cip, a0.y);
+                                wp[ip] = a0;
+                                if (two) {
+                                    float2 b0 = wq[iq];
+                                    b0.x = fmaf(w0q, crq, b0.x); b0.y = fmaf(w0q, ciq, b0.y);
+                                    wq[iq] = b0;
+                                }
+                                __syncwarp();
+                                float2 a1 = wp[ip + 1];
+                                a1.x = fmaf(w1p, crp, a1.x); a1.y = fmaf(w1p, cip, a1.y);
+                                wp[ip + 1] = a1;
+                                if (two) {
+                                    float2 b1 = wq[iq + 1];
+                                    b1.x = fmaf(w1q, crq, b1.x); b1.y = fmaf(w1q, ciq, b1.y);
+                                    wq[iq + 1] = b1;
+                                }
                                 __syncwarp();
                             } else {
-                                float2 u = wp[idx];
-                                u.x += cr;
-                                u.y += ci;
-                                wp[idx] = u;
-                                __syncwarp();
+                                atomicAdd(&wp[ip].x, w0p * crp); atomicAdd(&wp[ip].y, w0p * cip);
+                                atomicAdd(&wp[ip + 1].x, w1p * crp); atomicAdd(&wp[ip + 1].y, w1p * cip);
+                                if (two) {
+                                    atomicAdd(&wq[iq].x, w0q * crq); atomicAdd(&wq[iq].y, w0q * ciq);
+                                    atomicAdd(&wq[iq + 1].x, w1q * crq); atomicAdd(&wq[iq + 1].y, w1q * ciq);
+                                }
                             }
-                        } else if (LINEAR) {
-                            const float w0 = 0.5f - bp.s, w1 = 0.5f + bp.s;
-                            atomicAdd(&wp[idx].x, w0 * cr);
-                            atomicAdd(&wp[idx].y, w0 * ci);
-                            atomicAdd(&wp[idx + 1].x, w1 * cr);
-                            atomicAdd(&wp[idx + 1].y, w1 * ci);
                         } else {
-                            atomicAdd(&wp[idx].x, cr);
-                            atomicAdd(&wp[idx].y, ci);
+                            if (mode >= 1) {
+                                float2 a0 = wp[ip];
+                                a0.x += crp; a0.y += cip;
+                                wp[ip] = a0;
+                                if (two) {
+                                    float2 b0 = wq[iq];
+                                    b0.x += crq; b0.y += ciq;
+                                    wq[iq] = b0;
+                                }
+                                __syncwarp();
+                            } else {
+                                atomicAdd(&wp[ip].x, crp); atomicAdd(&wp[ip].y, cip);
+                                if (two) { atomicAdd(&wq[iq].x, crq); atomicAdd(&wq[iq].y, ciq); }
+                            }
                         }
                     }
                 }
