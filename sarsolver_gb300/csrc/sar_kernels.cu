@@ -638,6 +638,8 @@ constexpr float kFastBinRate = 1.05f;
 
 __device__ __forceinline__ size_t align_up(size_t n, size_t a) { return (n + a - 1) & ~(a - 1); }
 
+__host__ __device__ inline int window_slots(int ws) { return ws + (ws >> 4) + 1; }
+
 struct FpWsLayout {
     size_t win, coef, xt, base, fast, wst, bars, anchors, total;
 };
@@ -645,7 +647,7 @@ struct FpWsLayout {
 __host__ __device__ inline FpWsLayout fp_ws_layout(int ws, int pbf) {
     FpWsLayout L;
     L.win = 0;
-    L.coef = L.win + (size_t)pbf * ws * sizeof(float2);
+    L.coef = L.win + (size_t)pbf * window_slots(ws) * sizeof(float2);
     L.coef = (L.coef + 15) & ~(size_t)15;
     L.xt = L.coef + (size_t)2 * pbf * 4 * kSetF4 * sizeof(float4);
     L.base = L.xt + (size_t)2 * kTile * kTile * sizeof(float2);
@@ -659,10 +661,122 @@ __host__ __device__ inline FpWsLayout fp_ws_layout(int ws, int pbf) {
 
 size_t fp_grid_ws_smem_bytes(int ws, int pbf) { return fp_ws_layout(ws, pbf).total; }
 
+// Window slot of bin w: one padding slot every 16 bins, so lanes whose bins differ by a
+// multiple of 16 do not share a shared-memory bank pair.
+__device__ __forceinline__ int wslot(int w) { return w + (w >> 4); }
+
+template <bool PRECISE>
+struct RowEval {
+    BinPos bp;
+    float cr, ci;
+};
+
+template <bool PRECISE>
+__device__ __forceinline__ RowEval<PRECISE> scatter_eval(const ColumnTerms& ct, float c9, float w9, float ib, float dj,
+                                                         float2 xv) {
+    RowEval<PRECISE> e;
+    const float dj2 = dj * dj, dj3 = dj2 * dj;
+    const float ph = pixel_phase(ct, c9, dj, dj2, dj3);
+    const float v = pixel_bin<PRECISE>(ct, w9, dj, dj2, dj3);
+    e.bp = bin_position<PRECISE>(v, PRECISE ? fmaf(ib, dj, ct.ci) : 0.f);
+    float sn, cn;
+    __sincosf(SAR_TWO_PI * (ph - rintf(ph)), &sn, &cn);
+    e.cr = xv.x * cn - xv.y * sn;   // x * exp(+2 pi i f)
+    e.ci = fmaf(xv.x, sn, xv.y * cn);
+    return e;
+}
+
+__device__ __forceinline__ void rmw_add(float2* wp, int idx, float w, float cr, float ci) {
+    float2* q = wp + wslot(idx);
+    float2 u = *q;
+    u.x = fmaf(w, cr, u.x);
+    u.y = fmaf(w, ci, u.y);
+    *q = u;
+}
+
+// 16 rows of one half tile for the pulse pair (p, q).  MODE 2: bins n, n+1 of different lanes
+// disjoint (one phase per row); MODE 1: bins n distinct (two phases); MODE 0: atomics.
+template <bool LINEAR, bool PRECISE, int MODE, bool TWO>
+__device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, float w9p, float ibp,
+                                             const ColumnTerms& ctq, float c9q, float w9q, float ibq,
+                                             const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
+                                             int ws, int lane) {
+#pragma unroll
+    for (int rr = 0; rr < 16; ++rr) {
+        const float dj = (float)(rr - 8);
+        const float2 xv = xrow[rr * kTile + lane];
+        const RowEval<PRECISE> ep = scatter_eval<PRECISE>(ctp, c9p, w9p, ibp, dj, xv);
+        const int ip = (int)min((unsigned)(ep.bp.n + off_p), (unsigned)(ws - 2));
+        RowEval<PRECISE> eq;
+        int iq = 0;
+        if (TWO) {
+            eq = scatter_eval<PRECISE>(ctq, c9q, w9q, ibq, dj, xv);
+            iq = (int)min((unsigned)(eq.bp.n + off_q), (unsigned)(ws - 2));
+        }
+        if (LINEAR) {
+            const float w0p = 0.5f - ep.bp.s, w1p = 0.5f + ep.bp.s;
+            const float w0q = TWO ? 0.5f - eq.bp.s : 0.f, w1q = TWO ? 0.5f + eq.bp.s : 0.f;
+            if (MODE == 2) {
+                rmw_add(wp, ip, w0p, ep.cr, ep.ci);
+                rmw_add(wp, ip + 1, w1p, ep.cr, ep.ci);
+                if (TWO) {
+                    rmw_add(wq, iq, w0q, eq.cr, eq.ci);
+                    rmw_add(wq, iq + 1, w1q, eq.cr, eq.ci);
+                }
+                __syncwarp();
+            } else if (MODE == 1) {
+                rmw_add(wp, ip, w0p, ep.cr, ep.ci);
+                if (TWO) rmw_add(wq, iq, w0q, eq.cr, eq.ci);
+                __syncwarp();
+                rmw_add(wp, ip + 1, w1p, ep.cr, ep.ci);
+                if (TWO) rmw_add(wq, iq + 1, w1q, eq.cr, eq.ci);
+                __syncwarp();
+            } else {
+                float2* a0 = wp + wslot(ip);
+                float2* a1 = wp + wslot(ip + 1);
+                atomicAdd(&a0->x, w0p * ep.cr); atomicAdd(&a0->y, w0p * ep.ci);
+                atomicAdd(&a1->x, w1p * ep.cr); atomicAdd(&a1->y, w1p * ep.ci);
+                if (TWO) {
+                    float2* b0 = wq + wslot(iq);
+                    float2* b1 = wq + wslot(iq + 1);
+                    atomicAdd(&b0->x, w0q * eq.cr); atomicAdd(&b0->y, w0q * eq.ci);
+                    atomicAdd(&b1->x, w1q * eq.cr); atomicAdd(&b1->y, w1q * eq.ci);
+                }
+            }
+        } else {
+            if (MODE >= 1) {
+                rmw_add(wp, ip, 1.0f, ep.cr, ep.ci);
+                if (TWO) rmw_add(wq, iq, 1.0f, eq.cr, eq.ci);
+                __syncwarp();
+            } else {
+                float2* a0 = wp + wslot(ip);
+                atomicAdd(&a0->x, ep.cr); atomicAdd(&a0->y, ep.ci);
+                if (TWO) {
+                    float2* b0 = wq + wslot(iq);
+                    atomicAdd(&b0->x, eq.cr); atomicAdd(&b0->y, eq.ci);
+                }
+            }
+        }
+    }
+}
+
+template <bool LINEAR, bool PRECISE, bool TWO>
+__device__ __forceinline__ void scatter_half(int mode, const ColumnTerms& ctp, float c9p, float w9p, float ibp,
+                                             const ColumnTerms& ctq, float c9q, float w9q, float ibq,
+                                             const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
+                                             int ws, int lane) {
+    if (mode == 2)
+        scatter_rows<LINEAR, PRECISE, 2, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane);
+    else if (mode == 1)
+        scatter_rows<LINEAR, PRECISE, 1, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane);
+    else
+        scatter_rows<LINEAR, PRECISE, 0, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane);
+}
+
 template <bool LINEAR, bool PRECISE>
 __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridArgs a) {
     extern __shared__ __align__(16) unsigned char fsm[];
-    const int pbf = a.pbf, ws = a.ws;
+    const int pbf = a.pbf, ws = a.ws, wslots = window_slots(ws);
     const FpWsLayout L = fp_ws_layout(ws, pbf);
     float2* win = reinterpret_cast<float2*>(fsm + L.win);
     float4* coef0 = reinterpret_cast<float4*>(fsm + L.coef);
@@ -686,7 +800,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
     const int ntile = min(a.seg_tiles, g.tiles_y - tj0);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    for (int e = threadIdx.x; e < pbf * ws; e += blockDim.x) win[e] = make_float2(0.f, 0.f);
+    for (int e = threadIdx.x; e < pbf * wslots; e += blockDim.x) win[e] = make_float2(0.f, 0.f);
     for (int e = threadIdx.x; e < npb; e += blockDim.x) wst[e] = a.strip_start[(size_t)strip * a.S + s0 + e];
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], kWsProducers);
@@ -774,9 +888,9 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
             for (int p = warp; p < npb; p += 2 * (kWsConsumers / 32)) {
                 const int p2 = p + kWsConsumers / 32;
                 const bool two = p2 < npb;
-                const int pq = two ? p2 : p;   // second pulse (a repeat of the first when absent)
-                float2* wp = win + p * ws;
-                float2* wq = win + pq * ws;
+                const int pq = two ? p2 : p;
+                float2* wp = win + p * wslots;
+                float2* wq = win + pq * wslots;
                 const int off_p = base0[b * pbf + p] - wst[p];
                 const int off_q = base0[b * pbf + pq] - wst[pq];
                 const int mode = two ? min(fast0[b * pbf + p], fast0[b * pbf + p2]) : fast0[b * pbf + p];
@@ -787,87 +901,13 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                         load_column<PRECISE>(coef + (p * 4 + qx + 2 * half) * kSetF4, tt, c9p, w9p, ibp);
                     const ColumnTerms ctq =
                         load_column<PRECISE>(coef + (pq * 4 + qx + 2 * half) * kSetF4, tt, c9q, w9q, ibq);
-#pragma unroll 2
-                    for (int rr = 0; rr < 16; ++rr) {
-                        const float dj = (float)(rr - 8), dj2 = dj * dj, dj3 = dj2 * dj;
-                        const float2 xv = xt[(16 * half + rr) * kTile + lane];
-                        // pulse p
-                        const float php = pixel_phase(ctp, c9p, dj, dj2, dj3);
-                        const float vp = pixel_bin<PRECISE>(ctp, w9p, dj, dj2, dj3);
-                        const BinPos bpp = bin_position<PRECISE>(vp, PRECISE ? fmaf(ibp, dj, ctp.ci) : 0.f);
-                        float snp, cnp;
-                        __sincosf(SAR_TWO_PI * (php - rintf(php)), &snp, &cnp);
-                        const float crp = xv.x * cnp - xv.y * snp, cip = fmaf(xv.x, snp, xv.y * cnp);
-                        const unsigned ip = min((unsigned)(bpp.n + off_p), (unsigned)(ws - 2));
-                        // pulse q
-                        const float phq = pixel_phase(ctq, c9q, dj, dj2, dj3);
-                        const float vq = pixel_bin<PRECISE>(ctq, w9q, dj, dj2, dj3);
-                        const BinPos bpq = bin_position<PRECISE>(vq, PRECISE ? fmaf(ibq, dj, ctq.ci) : 0.f);
-                        float snq, cnq;
-                        __sincosf(SAR_TWO_PI * (phq - rintf(phq)), &snq, &cnq);
-                        const float crq = xv.x * cnq - xv.y * snq, ciq = fmaf(xv.x, snq, xv.y * cnq);
-                        const unsigned iq = min((unsigned)(bpq.n + off_q), (unsigned)(ws - 2));
-                        if (LINEAR) {
-                            const float w0p = 0.5f - bpp.s, w1p = 0.5f + bpp.s;
-                            const float w0q = 0.5f - bpq.s, w1q = 0.5f + bpq.s;
-                            // (wq aliases wp when there is no second pulse: its update is skipped)
-                            if (mode == 2) {
-                                // bins n, n+1 of different lanes are disjoint: one phase per row
-                                float2 a0 = wp[ip], a1 = wp[ip + 1];
-                                a0.x = fmaf(w0p, crp, a0.x); a0.y = fmaf(w0p, cip, a0.y);
-                                a1.x = fmaf(w1p, crp, a1.x); a1.y = fmaf(w1p, cip, a1.y);
-                                wp[ip] = a0; wp[ip + 1] = a1;
-                                if (two) {
-                                    float2 b0 = wq[iq], b1 = wq[iq + 1];
-                                    b0.x = fmaf(w0q, crq, b0.x); b0.y = fmaf(w0q, ciq, b0.y);
-                                    b1.x = fmaf(w1q, crq, b1.x); b1.y = fmaf(w1q, ciq, b1.y);
-                                    wq[iq] = b0; wq[iq + 1] = b1;
-                                }
-                                __syncwarp();
-                            } else if (mode == 1) {
-                                float2 a0 = wp[ip];
-                                a0.x = fmaf(w0p, crp, a0.x); a0.y = fmaf(w0p, cip, a0.y);
-                                wp[ip] = a0;
-                                if (two) {
-                                    float2 b0 = wq[iq];
-                                    b0.x = fmaf(w0q, crq, b0.x); b0.y = fmaf(w0q, ciq, b0.y);
-                                    wq[iq] = b0;
-                                }
-                                __syncwarp();
-                                float2 a1 = wp[ip + 1];
-                                a1.x = fmaf(w1p, crp, a1.x); a1.y = fmaf(w1p, cip, a1.y);
-                                wp[ip + 1] = a1;
-                                if (two) {
-                                    float2 b1 = wq[iq + 1];
-                                    b1.x = fmaf(w1q, crq, b1.x); b1.y = fmaf(w1q, ciq, b1.y);
-                                    wq[iq + 1] = b1;
-                                }
-                                __syncwarp();
-                            } else {
-                                atomicAdd(&wp[ip].x, w0p * crp); atomicAdd(&wp[ip].y, w0p * cip);
-                                atomicAdd(&wp[ip + 1].x, w1p * crp); atomicAdd(&wp[ip + 1].y, w1p * cip);
-                                if (two) {
-                                    atomicAdd(&wq[iq].x, w0q * crq); atomicAdd(&wq[iq].y, w0q * ciq);
-                                    atomicAdd(&wq[iq + 1].x, w1q * crq); atomicAdd(&wq[iq + 1].y, w1q * ciq);
-                                }
-                            }
-                        } else {
-                            if (mode >= 1) {
-                                float2 a0 = wp[ip];
-                                a0.x += crp; a0.y += cip;
-                                wp[ip] = a0;
-                                if (two) {
-                                    float2 b0 = wq[iq];
-                                    b0.x += crq; b0.y += ciq;
-                                    wq[iq] = b0;
-                                }
-                                __syncwarp();
-                            } else {
-                                atomicAdd(&wp[ip].x, crp); atomicAdd(&wp[ip].y, cip);
-                                if (two) { atomicAdd(&wq[iq].x, crq); atomicAdd(&wq[iq].y, ciq); }
-                            }
-                        }
-                    }
+                    const float2* xrow = xt + 16 * half * kTile;
+                    if (two)
+                        scatter_half<LINEAR, PRECISE, true>(mode, ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq,
+                                                            off_p, off_q, ws, lane);
+                    else
+                        scatter_half<LINEAR, PRECISE, false>(mode, ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp,
+                                                             wq, off_p, off_q, ws, lane);
                 }
             }
         }
@@ -881,9 +921,9 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
     // merge this warp's windows into the global accumulator
     __syncwarp();
     for (int p = warp; p < npb; p += kWsConsumers / 32) {
-        const float2* wp = win + p * ws;
+        const float2* wp = win + p * wslots;
         for (int w = lane; w < ws; w += 32) {
-            const float2 v = wp[w];
+            const float2 v = wp[wslot(w)];
             if (v.x == 0.f && v.y == 0.f) continue;
             const long gi = (long)wst[p] + w - a.bg0;
             if (gi < 0 || gi >= a.Lg) {
