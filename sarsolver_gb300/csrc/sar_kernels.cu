@@ -701,7 +701,7 @@ __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, 
                                              const ColumnTerms& ctq, float c9q, float w9q, float ibq,
                                              const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
                                              int ws, int lane) {
-#pragma unroll
+#pragma unroll 2
     for (int rr = 0; rr < 16; ++rr) {
         const float dj = (float)(rr - 8);
         const float2 xv = xrow[rr * kTile + lane];
