@@ -112,6 +112,9 @@ typedef struct sar_plan_info {
     size_t strip_window;        /* forward strip window (bins); 0 on the unstructured path */
     size_t device_bytes;        /* device memory held by the plan */
     int grid;                   /* 1 regular-grid path, 0 unstructured path */
+    int interp;                 /* SAR_INTERP_* of the plan */
+    size_t num_fast_times, num_slow_times, num_scatterers;   /* N, S, P */
+    int device;                 /* CUDA device of the plan */
 } sar_plan_info;
 
 /* Create a plan on `device` (-1: the current device).  Copies all host inputs. */
@@ -131,6 +134,40 @@ int sar_profiles(sar_plan *plan, const void *y_dev, void *prof_dev, void *stream
 int sar_set_slow_time_weighting(sar_plan *plan, const double *w_host /* [S][2] */);
 int sar_set_slow_time_weighting_device(sar_plan *plan, const void *w_dev /* complex64 [S] */,
                                        void *stream);
+
+/* Per-pulse phase-error gradient (autofocus).  g[s] = scale * Im( sum_f conj(ag[s][f]) y[s][f] ),
+ * ag and y complex64 [S][N] on the device, g float32 [S].  With ag = A_phi G, G = |I|^2 I,
+ * I = A_phi^H y and scale = 4 this is d(sum|I|^4)/d phi_s for slow-time weights exp(i phi_s).
+ * New (no counterpart in the reference, which exposes only slow_time_weighting,
+ * sarsolver_cxx.cpp:288, :349). */
+int sar_phase_gradient(const void *ag_dev, const void *y_dev, void *g_dev, size_t num_slow_times,
+                       size_t num_fast_times, float scale, void *stream);
+
+/* Image sharpness sum |I|^4 (FP64, written to *sum_dev on the device) and, when g_dev is not
+ * NULL, G = |I|^2 I, complex64 [P] -- the image-side factor of the autofocus gradient above.
+ * Buffers 16-byte aligned.  New (no counterpart in the reference). */
+int sar_sharpness(const void *img_dev, void *g_dev, double *sum_dev, size_t num_pixels, void *stream);
+
+/* CGLS on the normal equations A^H A x = A^H y with the plan's operator pair (replaces the CIL
+ * CGLS the reference runs on its operator, tests/test_cil.py:18-22).  x_dev holds the start on
+ * entry (ignored and zeroed when zero_start != 0) and the solution on return.  Stops when the
+ * normal-equations residual ||A^H (y - A x)|| / ||A^H y|| <= tolerance or after max_iterations.
+ * history (host, may be NULL) receives that residual before each iteration and after the last
+ * ([max_iterations + 1]).  Each iteration is one sar_forward and one sar_adjoint plus fused vector
+ * updates; the host waits on `stream` once per iteration to test the residual.  Work vectors
+ * (2 x S*N + 2 x P complex64) are taken from the stream-ordered allocator for the call.  Exact
+ * convergence theory needs SAR_INTERP_LINEAR (an exact adjoint pair).  Non-finite data returns
+ * SAR_ERR_INVALID_ARGUMENT; ||A p|| = 0 before convergence sets result->breakdown. */
+typedef struct sar_cgls_result {
+    int iterations;   /* iterations run */
+    int converged;    /* residual <= tolerance reached */
+    int breakdown;    /* stopped on ||A p|| = 0 */
+    double residual;  /* final ||A^H (y - A x)|| / ||A^H y|| */
+    double norm_ahy;  /* ||A^H y|| */
+} sar_cgls_result;
+
+int sar_cgls(sar_plan *plan, const void *y_dev, void *x_dev, int zero_start, int max_iterations,
+             double tolerance, double *history, sar_cgls_result *result, void *stream);
 
 /* Stage timing.  While enabled, every sar_forward / sar_adjoint call records CUDA events on
  * its stream around its stages: [0] range-profile FFT side before the main kernel (adjoint:

@@ -29,7 +29,7 @@ EXPORTED = (
     "sar_set_slow_time_weighting", "sar_set_slow_time_weighting_device",
     "sar_device_flags", "sar_last_error", "sar_status_string",
     "sar_enable_stage_timing", "sar_stage_times",
-    "sar_adjoint_from_profiles_noalloc",
+    "sar_adjoint_from_profiles_noalloc", "sar_phase_gradient", "sar_sharpness", "sar_cgls",
 )
 
 
@@ -49,12 +49,21 @@ class SarGeometry(ctypes.Structure):
     ]
 
 
+class SarCglsResult(ctypes.Structure):
+    """Mirror of ``sar_cgls_result``."""
+
+    _fields_ = [("iterations", c_int), ("converged", c_int), ("breakdown", c_int), ("residual", c_double),
+                ("norm_ahy", c_double)]
+
+
 class SarPlanInfo(ctypes.Structure):
     """Mirror of ``sar_plan_info``."""
 
     _fields_ = [
         ("working_length", c_size_t), ("profile_first_bin", c_long), ("profile_length", c_size_t),
         ("tile_window", c_size_t), ("strip_window", c_size_t), ("device_bytes", c_size_t), ("grid", c_int),
+        ("interp", c_int), ("num_fast_times", c_size_t), ("num_slow_times", c_size_t), ("num_scatterers", c_size_t),
+        ("device", c_int),
     ]
 
 
@@ -95,6 +104,13 @@ def load() -> ctypes.CDLL:
     lib.sar_set_slow_time_weighting_device.argtypes = [c_void_p, c_void_p, c_void_p]
     lib.sar_device_flags.argtypes = [c_void_p, POINTER(c_uint)]
     lib.sar_enable_stage_timing.argtypes = [c_void_p, c_int]
+    lib.sar_phase_gradient.argtypes = [c_void_p, c_void_p, c_void_p, c_size_t, c_size_t, ctypes.c_float, c_void_p]
+    lib.sar_phase_gradient.restype = c_int
+    lib.sar_sharpness.argtypes = [c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]
+    lib.sar_sharpness.restype = c_int
+    lib.sar_cgls.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_int, c_double, c_void_p,
+                             POINTER(SarCglsResult), c_void_p]
+    lib.sar_cgls.restype = c_int
     lib.sar_stage_times.argtypes = [c_void_p, POINTER(ctypes.c_float), POINTER(c_int)]
     for name in ("sar_plan_create", "sar_plan_destroy", "sar_plan_get_info", "sar_forward", "sar_adjoint",
                  "sar_profiles", "sar_set_slow_time_weighting", "sar_set_slow_time_weighting_device",

@@ -13,6 +13,7 @@
 #include <complex>
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -584,6 +585,11 @@ int sar_plan_get_info(const sar_plan* p, sar_plan_info* info) {
     info->strip_window = (p->grid && !p->forward_points) ? (size_t)p->ws : 0;
     info->device_bytes = p->device_bytes;
     info->grid = p->grid ? 1 : 0;
+    info->interp = p->interp;
+    info->num_fast_times = p->N;
+    info->num_slow_times = p->S;
+    info->num_scatterers = p->P;
+    info->device = p->device;
     return SAR_OK;
 }
 
@@ -732,6 +738,31 @@ int sar_set_slow_time_weighting_device(sar_plan* p, const void* w_dev, void* str
     p->last_stream = st;
     SAR_CUDA(launch_weights((const float2*)w_dev, p->d_wadj, p->d_wfwd, (int)p->S, p->interp == SAR_INTERP_LINEAR, st),
              "weights kernel");
+    return SAR_OK;
+}
+
+int sar_phase_gradient(const void* ag_dev, const void* y_dev, void* g_dev, size_t num_slow_times,
+                       size_t num_fast_times, float scale, void* stream) {
+    if (!ag_dev || !y_dev || !g_dev) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    if (!num_slow_times || !num_fast_times || num_slow_times > (size_t)1 << 31 || num_fast_times > (size_t)1 << 30)
+        return fail(SAR_ERR_INVALID_ARGUMENT, "bad sizes");
+    SAR_CUDA(launch_phase_grad((const float2*)ag_dev, (const float2*)y_dev, (float*)g_dev, (int)num_slow_times,
+                               (int)num_fast_times, scale, (cudaStream_t)stream),
+             "phase gradient");
+    return SAR_OK;
+}
+
+int sar_sharpness(const void* img_dev, void* g_dev, double* sum_dev, size_t num_pixels, void* stream) {
+    if (!img_dev || !sum_dev) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    if (((uintptr_t)img_dev & 15) || ((uintptr_t)g_dev & 15))
+        return fail(SAR_ERR_INVALID_ARGUMENT, "image buffers must be 16-byte aligned");
+    cudaStream_t st = (cudaStream_t)stream;
+    int dev = 0, sms = 0;
+    SAR_CUDA(cudaGetDevice(&dev), "get device");
+    SAR_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "device attribute");
+    SAR_CUDA(cudaMemsetAsync(sum_dev, 0, sizeof(double), st), "clear sum");
+    if (!num_pixels) return SAR_OK;
+    SAR_CUDA(launch_sharpness((const float2*)img_dev, (float2*)g_dev, sum_dev, num_pixels, sms, st), "sharpness");
     return SAR_OK;
 }
 

@@ -1198,6 +1198,78 @@ __global__ void extract_forward_kernel(const T* __restrict__ spec, const float2*
     y[(size_t)(first + row) * N + (i + half) % N] = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
 }
 
+// K6: per-pulse phase-error gradient of an image-domain objective.  For the sharpness
+// S = sum |I|^4 of I = A_phi^H y (slow-time weights w_s = exp(i phi_s)), dS/dphi_s =
+// 4 Im( sum_f conj((A_phi G)_{s,f}) y_{s,f} ) with G = |I|^2 I.  One CTA per pulse row: a
+// strided FP32 dot product per thread (a few terms each), then FP64 warp shuffles and a
+// shared-memory reduction across warps.
+__global__ void phase_grad_kernel(const float2* __restrict__ ag, const float2* __restrict__ y, float* __restrict__ g,
+                                  int N, float scale) {
+    __shared__ double part[32];
+    const size_t row = blockIdx.x;
+    const float2* a = ag + row * N;
+    const float2* b = y + row * N;
+    float acc = 0.f;
+    for (int f = threadIdx.x; f < N; f += blockDim.x) {
+        const float2 u = __ldg(a + f), v = __ldg(b + f);
+        acc = fmaf(u.x, v.y, fmaf(-u.y, v.x, acc));   // Im(conj(u) v)
+    }
+    double d = acc;
+    for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = d;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        d = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.0;
+        for (int o = 16; o; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        if (threadIdx.x == 0) g[row] = (float)(scale * d);
+    }
+}
+
+cudaError_t launch_phase_grad(const float2* ag, const float2* y, float* g, int S, int N, float scale, cudaStream_t st) {
+    phase_grad_kernel<<<S, 256, 0, st>>>(ag, y, g, N, scale);
+    return cudaGetLastError();
+}
+
+// Image sharpness: G = |I|^2 I (optional) and sum |I|^4 accumulated in FP64 (one atomic per CTA;
+// the caller zeroes *sum).  Grid-stride over pixel pairs with 16-byte loads; an odd tail pixel
+// is taken by thread 0 of CTA 0.
+__global__ void sharpness_kernel(const float2* __restrict__ img, float2* __restrict__ G, double* __restrict__ sum,
+                                 size_t P) {
+    __shared__ double part[32];
+    double acc = 0.0;
+    const size_t pairs = P >> 1;
+    const float4* in4 = reinterpret_cast<const float4*>(img);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < pairs; i += (size_t)gridDim.x * blockDim.x) {
+        const float4 v = __ldg(in4 + i);
+        const float m0 = fmaf(v.x, v.x, v.y * v.y), m1 = fmaf(v.z, v.z, v.w * v.w);
+        acc += (double)(m0 * m0) + (double)(m1 * m1);
+        if (G) reinterpret_cast<float4*>(G)[i] = make_float4(m0 * v.x, m0 * v.y, m1 * v.z, m1 * v.w);
+    }
+    if ((P & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        const float2 v = img[P - 1];
+        const float m = fmaf(v.x, v.x, v.y * v.y);
+        acc += (double)(m * m);
+        if (G) G[P - 1] = make_float2(m * v.x, m * v.y);
+    }
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        acc = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.0;
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (threadIdx.x == 0) atomicAdd(sum, acc);
+    }
+}
+
+cudaError_t launch_sharpness(const float2* img, float2* G, double* sum, size_t P, int num_sms, cudaStream_t st) {
+    const size_t pairs = (P >> 1) ? (P >> 1) : 1;
+    size_t blocks = (pairs + 255) / 256;
+    const size_t cap = (size_t)(num_sms > 0 ? num_sms : 152) * 8;
+    if (blocks > cap) blocks = cap;
+    sharpness_kernel<<<(unsigned)blocks, 256, 0, st>>>(img, G, sum, P);
+    return cudaGetLastError();
+}
+
 __global__ void weights_kernel(const float2* __restrict__ w, float2* wadj, float2* wfwd, int S, int conj_adjoint) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= S) return;

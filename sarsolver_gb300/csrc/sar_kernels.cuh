@@ -91,6 +91,9 @@ cudaError_t launch_pack_forward(const float2* acc, void* spec, int dbl, long M, 
                                 cudaStream_t st);
 cudaError_t launch_extract_forward(const void* spec, int dbl, const float2* wave, const float2* wfac, float2* y,
                                    int N, long M, int rows, int first, cudaStream_t st);
+cudaError_t launch_phase_grad(const float2* ag, const float2* y, float* g, int S, int N, float scale,
+                              cudaStream_t st);
+cudaError_t launch_sharpness(const float2* img, float2* G, double* sum, size_t P, int num_sms, cudaStream_t st);
 cudaError_t launch_weights(const float2* w, float2* wadj, float2* wfwd, int S, int conj_adjoint,
                            cudaStream_t st);
 
