@@ -169,6 +169,51 @@ typedef struct sar_cgls_result {
 int sar_cgls(sar_plan *plan, const void *y_dev, void *x_dev, int zero_start, int max_iterations,
              double tolerance, double *history, sar_cgls_result *result, void *stream);
 
+/* ------------------------------------------------ 3. learned warm start (U-Net)
+ *
+ * New (no counterpart in the reference): the network that maps a backprojected image A^H y to a
+ * CGLS warm start.  4-level U-Net in bf16 with FP32 accumulation on the tensor cores (layer list
+ * in sar_unet_layer order: enc0 a/b, enc1 a/b, enc2 a/b, bottleneck a/b, dec2 a/b, dec1 a/b,
+ * dec0 a/b, 1x1 output).  Images are complex64 [batch][height][width] (channels re, im);
+ * width / 8 must be a power of two >= 16 and height a multiple of 8 * 128 / min(width / 8, 128).
+ * Parameters are one flat FP32 vector: for each layer its filter [cout][taps][cin0 + cin1]
+ * (tap = 3 * (dy + 1) + (dx + 1)) followed by its bias [cout]. */
+#define SAR_UNET_LAYERS 15
+typedef struct sar_unet sar_unet;
+typedef struct sar_unet_layer {
+    size_t weight_offset, bias_offset;   /* into the flat parameter vector */
+    int cin0, cin1, cout, taps, relu, level;
+} sar_unet_layer;
+
+int sar_unet_create(int base_channels /* 32 or 64 */, int device, sar_unet **net_out);
+int sar_unet_destroy(sar_unet *net);
+int sar_unet_info(const sar_unet *net, size_t *num_params, sar_unet_layer *layers /* [SAR_UNET_LAYERS] or NULL */);
+/* Copy parameters in (resets the Adam moments) / out, gradients out; device FP32 buffers. */
+int sar_unet_set_params(sar_unet *net, const float *params_dev, void *stream);
+int sar_unet_get_params(const sar_unet *net, float *params_dev, void *stream);
+int sar_unet_get_grads(const sar_unet *net, float *grads_dev, void *stream);
+int sar_unet_zero_grad(sar_unet *net, void *stream);
+/* out = U(in_scale * in); keeps the activations for sar_unet_backward. */
+int sar_unet_forward(sar_unet *net, const void *in_dev, float in_scale, int batch, int height, int width,
+                     void *out_dev, void *stream);
+/* Adds d(loss)/d(parameters) for grad_out = d(loss)/d(out) (complex64, PyTorch's conjugate
+ * convention, i.e. d/d(re) + i d/d(im)) of the last forward call. */
+int sar_unet_backward(sar_unet *net, const void *grad_out_dev, void *stream);
+int sar_unet_adam_step(sar_unet *net, float lr, float beta1, float beta2, float eps, int step, void *stream);
+/* Synchronise the device, return and clear the kernels' check flags (SAR_FLAG_WAIT_TIMEOUT). */
+int sar_unet_flags(sar_unet *net, unsigned *flags);
+
+/* Building blocks (the network's own kernels): bf16 NHWC convolution over the channel
+ * concatenation of x0 [c0] and x1 [c1] (x1 may be NULL), filter w [cout][taps][c0 + c1] bf16,
+ * taps 9 (3x3, zero padding 1) or 1; y bf16 NHWC [cout] with optional FP32 bias and ReLU.  The
+ * weight gradient adds sum_pixels dz[p][co] * x[p + tap][ci] into dw (FP32, same layout as w).
+ * Channel counts multiples of 32; flags_dev a device word receiving SAR_FLAG_WAIT_TIMEOUT. */
+int sar_conv2d_forward_bf16(const void *x0, int c0, const void *x1, int c1, int batch, int height, int width,
+                            int taps, const void *w, const float *bias, int cout, int relu, void *y,
+                            unsigned *flags_dev, void *stream);
+int sar_conv2d_wgrad_bf16(const void *x0, int c0, const void *x1, int c1, const void *dz, int cout, int batch,
+                          int height, int width, int taps, float *dw, unsigned *flags_dev, void *stream);
+
 /* Stage timing.  While enabled, every sar_forward / sar_adjoint call records CUDA events on
  * its stream around its stages: [0] range-profile FFT side before the main kernel (adjoint:
  * pack + inverse FFT + unpack; forward: accumulator clear), [1] the main gather / scatter

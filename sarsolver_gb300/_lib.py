@@ -30,7 +30,12 @@ EXPORTED = (
     "sar_device_flags", "sar_last_error", "sar_status_string",
     "sar_enable_stage_timing", "sar_stage_times",
     "sar_adjoint_from_profiles_noalloc", "sar_phase_gradient", "sar_sharpness", "sar_cgls",
+    "sar_unet_create", "sar_unet_destroy", "sar_unet_info", "sar_unet_set_params", "sar_unet_get_params",
+    "sar_unet_get_grads", "sar_unet_zero_grad", "sar_unet_forward", "sar_unet_backward", "sar_unet_adam_step",
+    "sar_unet_flags", "sar_conv2d_forward_bf16", "sar_conv2d_wgrad_bf16",
 )
+
+SAR_UNET_LAYERS = 15
 
 
 class SarGeometry(ctypes.Structure):
@@ -47,6 +52,13 @@ class SarGeometry(ctypes.Structure):
         ("grid_step_y", c_double * 3), ("grid_step_z", c_double * 3),
         ("path", c_int),
     ]
+
+
+class SarUnetLayer(ctypes.Structure):
+    """Mirror of ``sar_unet_layer``."""
+
+    _fields_ = [("weight_offset", c_size_t), ("bias_offset", c_size_t), ("cin0", c_int), ("cin1", c_int),
+                ("cout", c_int), ("taps", c_int), ("relu", c_int), ("level", c_int)]
 
 
 class SarCglsResult(ctypes.Structure):
@@ -111,6 +123,26 @@ def load() -> ctypes.CDLL:
     lib.sar_cgls.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_int, c_double, c_void_p,
                              POINTER(SarCglsResult), c_void_p]
     lib.sar_cgls.restype = c_int
+    P = c_void_p
+    unet_sigs = {
+        "sar_unet_create": [c_int, c_int, P],
+        "sar_unet_destroy": [P],
+        "sar_unet_info": [P, P, P],
+        "sar_unet_set_params": [P, P, P],
+        "sar_unet_get_params": [P, P, P],
+        "sar_unet_get_grads": [P, P, P],
+        "sar_unet_zero_grad": [P, P],
+        "sar_unet_forward": [P, P, ctypes.c_float, c_int, c_int, c_int, P, P],
+        "sar_unet_backward": [P, P, P],
+        "sar_unet_adam_step": [P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float, c_int, P],
+        "sar_unet_flags": [P, P],
+        "sar_conv2d_forward_bf16": [P, c_int, P, c_int, c_int, c_int, c_int, c_int, P, P, c_int, c_int, P, P, P],
+        "sar_conv2d_wgrad_bf16": [P, c_int, P, c_int, P, c_int, c_int, c_int, c_int, c_int, P, P, P],
+    }
+    for name, args in unet_sigs.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = c_int
     lib.sar_stage_times.argtypes = [c_void_p, POINTER(ctypes.c_float), POINTER(c_int)]
     for name in ("sar_plan_create", "sar_plan_destroy", "sar_plan_get_info", "sar_forward", "sar_adjoint",
                  "sar_profiles", "sar_set_slow_time_weighting", "sar_set_slow_time_weighting_device",

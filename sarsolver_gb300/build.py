@@ -21,8 +21,8 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math"]
-CUDA_UNITS = ["sar_kernels.cu", "sar_api.cu", "sar_noalloc.cu", "sar_cgls.cu"]
-HEADERS = ["sar_geom.cuh", "sar_host_prep.h", "sar_kernels.cuh"]
+CUDA_UNITS = ["sar_kernels.cu", "sar_api.cu", "sar_noalloc.cu", "sar_cgls.cu", "sar_unet.cu"]
+HEADERS = ["sar_geom.cuh", "sar_host_prep.h", "sar_kernels.cuh", "unet_tc.cuh"]
 
 GPU_LIB = os.path.join(BUILD, "libsargpu.so")
 HOST_LIB = os.path.join(BUILD, "libsargeom_host.so")
