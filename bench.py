@@ -40,6 +40,8 @@ def parse():
     ap.add_argument("--case", default="config2")
     ap.add_argument("--cpu-pulses", type=int, default=96, help="pulse sample of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-cgls", action="store_true", help="skip the learned-vs-plain CGLS timing")
+    ap.add_argument("--cgls-scenes", type=int, default=8)
     return ap.parse_args()
 
 
@@ -239,11 +241,55 @@ def run_ours(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(aperture, scene, upsample, y, args.cpu_pulses, steps=1)
+    if rank == 0 and not args.no_cgls:
+        result["cgls"] = learned_vs_plain(args.cgls_scenes)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(result))
+
+
+def learned_vs_plain(scenes: int) -> dict:
+    """Second half of the metric: wall time of CGLS to ||A^H (y - A x)|| / ||A^H y|| <= 1e-3, plain
+    (from zero) vs learned (U-Net warm start, then CGLS), on held-out generated scenes of the
+    learned-solver workload (512^2 image, 1024 pulses x 1024 samples, aperture 2-6 deg, SNR
+    10-30 dB).  Each solve is timed whole, host clock with device synchronisation around it."""
+    import torch
+    from sarsolver_gb300.learned import SceneSource, compare
+    from sarsolver_gb300.train_warmstart import DEFAULT_WEIGHTS, load_warm_start, summary
+
+    if not os.path.exists(DEFAULT_WEIGHTS):
+        return {"unavailable": "no trained warm-start weights at " + os.path.relpath(DEFAULT_WEIGHTS, HERE)}
+    warm, cfg = load_warm_start(DEFAULT_WEIGHTS)
+    src = SceneSource(cfg, seed=424242, continuous=True)
+    compare(warm, src, 1)                       # warm-up: plans, cuFFT plans, module loads
+    recs = compare(warm, src, scenes, repeats=2)
+    # component times on the last scene's plan: one operator pair and one U-Net inference
+    plan, y, _, _, _ = src.sample()
+    b = plan.adjoint(y)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    timings = {}
+    for name, fn in (("forward_ms", lambda: plan.forward(b)), ("adjoint_ms", lambda: plan.adjoint(y)),
+                     ("unet_inference_ms", lambda: warm.direction(b))):
+        for _ in range(3):
+            fn()
+        e0.record()
+        for _ in range(10):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        timings[name] = e0.elapsed_time(e1) / 10
+    src.close()
+    out = summary(recs)
+    out["component_ms"] = timings
+    out.update({"metric": "CGLS wall time to normal-equations residual 1e-3", "unit": "ms",
+                "higher_is_better": False, "learned_over_plain_time": out["learned_ms"] / out["plain_ms"],
+                "workload": f"{cfg.n}^2 at {cfg.spacing} m, {cfg.num_pulses} pulses x {cfg.num_freqs} samples, "
+                            f"U={cfg.upsample:g}, aperture U[{cfg.aperture_min:g},{cfg.aperture_max:g}] deg, "
+                            f"SNR U[{cfg.snr_min:g},{cfg.snr_max:g}] dB",
+                "weights": os.path.relpath(DEFAULT_WEIGHTS, HERE)})
+    return out
 
 
 def plan_chunk(plan) -> int:

@@ -169,6 +169,16 @@ typedef struct sar_cgls_result {
 int sar_cgls(sar_plan *plan, const void *y_dev, void *x_dev, int zero_start, int max_iterations,
              double tolerance, double *history, sar_cgls_result *result, void *stream);
 
+/* As sar_cgls with a choice of start and an optional precomputed A^H y (complex64 [P] on the
+ * device; NULL: computed here).  SAR_CGLS_START_SCALED takes x_dev as a direction z and starts
+ * from x0 = c z with c = Re<z, A^H y> / ||A z||^2 (the best multiple of z), which costs one
+ * forward projection -- the same as a given start. */
+#define SAR_CGLS_START_GIVEN 0
+#define SAR_CGLS_START_ZERO 1
+#define SAR_CGLS_START_SCALED 2
+int sar_cgls_ex(sar_plan *plan, const void *y_dev, void *x_dev, int start, const void *ahy_dev,
+                int max_iterations, double tolerance, double *history, sar_cgls_result *result, void *stream);
+
 /* ------------------------------------------------ 3. learned warm start (U-Net)
  *
  * New (no counterpart in the reference): the network that maps a backprojected image A^H y to a

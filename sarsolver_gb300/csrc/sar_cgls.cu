@@ -86,6 +86,45 @@ __global__ void update_p_kernel(float2* __restrict__ p, const float2* __restrict
     }
 }
 
+// Re<a, b> = sum Re(conj(a) b) accumulated in FP64 into *out (zeroed by the caller).
+__global__ void dot_re_kernel(const float2* __restrict__ a, const float2* __restrict__ b, size_t n,
+                              double* __restrict__ out) {
+    __shared__ double part[kThreads / 32];
+    double acc = 0.0;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 u = __ldg(a + i), v = __ldg(b + i);
+        acc += (double)fmaf(u.x, v.x, u.y * v.y);
+    }
+    for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        acc = threadIdx.x < kThreads / 32 ? part[threadIdx.x] : 0.0;
+        for (int o = 16; o; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (threadIdx.x == 0) atomicAdd(out, acc);
+    }
+}
+
+// Scaled start: c = sc[inum] / sc[iden]; x = c x over P entries, r = y - c r over NS entries
+// (x holds the direction z and r holds A z on entry).
+__global__ void scale_start_kernel(float2* __restrict__ x, size_t P, float2* __restrict__ r,
+                                   const float2* __restrict__ y, size_t NS, const double* __restrict__ sc, int inum,
+                                   int iden) {
+    const double den = sc[iden];
+    const float c = den > 0.0 ? (float)(sc[inum] / den) : 0.f;
+    const size_t total = P + NS;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        if (i < P) {
+            const float2 a = x[i];
+            x[i] = make_float2(c * a.x, c * a.y);
+        } else {
+            const size_t j = i - P;
+            const float2 a = r[j], b = __ldg(y + j);
+            r[j] = make_float2(fmaf(-c, a.x, b.x), fmaf(-c, a.y, b.y));
+        }
+    }
+}
+
 // r = y - r (r holds A x0 on entry).
 __global__ void residual_kernel(float2* __restrict__ r, const float2* __restrict__ y, size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
@@ -150,11 +189,14 @@ int arg_error(const char* msg) {
 }  // namespace
 
 // Scalar slots on the device: 0 and 1 hold gamma of alternate iterations, 2 holds ||A p||^2,
-// 3 holds ||A^H y||^2.
-extern "C" int sar_cgls(sar_plan* plan, const void* y_dev, void* x_dev, int zero_start, int max_iterations,
-                        double tolerance, double* history, sar_cgls_result* result, void* stream) {
+// 3 holds ||A^H y||^2, 4 and 5 hold <z, A^H y> and ||A z||^2 of a scaled start.
+extern "C" int sar_cgls_ex(sar_plan* plan, const void* y_dev, void* x_dev, int start, const void* ahy_dev,
+                           int max_iterations, double tolerance, double* history, sar_cgls_result* result,
+                           void* stream) {
     if (!plan || !y_dev || !x_dev || !result) return arg_error("null argument");
     if (max_iterations < 0 || !(tolerance >= 0.0)) return arg_error("max_iterations >= 0 and tolerance >= 0 required");
+    if (start != SAR_CGLS_START_GIVEN && start != SAR_CGLS_START_ZERO && start != SAR_CGLS_START_SCALED)
+        return arg_error("unknown CGLS start mode");
     sar_plan_info info;
     CG_CALL(sar_plan_get_info(plan, &info));
     const size_t P = info.num_scatterers, NS = info.num_slow_times * info.num_fast_times;
@@ -171,17 +213,27 @@ extern "C" int sar_cgls(sar_plan* plan, const void* y_dev, void* x_dev, int zero
     CG_CUDA(cudaMallocAsync((void**)&w.q, sizeof(float2) * NS, st), "CGLS work q");
     CG_CUDA(cudaMallocAsync((void**)&w.s, sizeof(float2) * P, st), "CGLS work s");
     CG_CUDA(cudaMallocAsync((void**)&w.p, sizeof(float2) * P, st), "CGLS work p");
-    CG_CUDA(cudaMallocAsync((void**)&w.sc, sizeof(double) * 4, st), "CGLS scalars");
-    CG_CUDA(cudaMemsetAsync(w.sc, 0, sizeof(double) * 4, st), "clear scalars");
+    CG_CUDA(cudaMallocAsync((void**)&w.sc, sizeof(double) * 6, st), "CGLS scalars");
+    CG_CUDA(cudaMemsetAsync(w.sc, 0, sizeof(double) * 6, st), "clear scalars");
     float2* x = (float2*)x_dev;
     const float2* y = (const float2*)y_dev;
 
-    // ||A^H y|| (the residual's denominator) and the initial s = A^H (y - A x0).
-    CG_CALL(sar_adjoint(plan, y, w.s, st));
+    // ||A^H y|| (the residual's denominator), then the initial r = y - A x0 and s = A^H r.
+    if (ahy_dev)
+        CG_CUDA(cudaMemcpyAsync(w.s, ahy_dev, sizeof(float2) * P, cudaMemcpyDeviceToDevice, st), "A^H y");
+    else
+        CG_CALL(sar_adjoint(plan, y, w.s, st));
     norm2_kernel<<<grid_for(P, sms), kThreads, 0, st>>>(w.s, P, w.sc + 3);
-    if (zero_start) {
+    if (start == SAR_CGLS_START_ZERO) {
         CG_CUDA(cudaMemsetAsync(x, 0, sizeof(float2) * P, st), "zero x");
         CG_CUDA(cudaMemcpyAsync(w.r, y, sizeof(float2) * NS, cudaMemcpyDeviceToDevice, st), "r = y");
+    } else if (start == SAR_CGLS_START_SCALED) {
+        // x0 = c z with c = Re<z, A^H y> / ||A z||^2, the minimiser of ||y - c A z||.
+        CG_CALL(sar_forward(plan, x, w.r, st));
+        dot_re_kernel<<<grid_for(P, sms), kThreads, 0, st>>>(x, w.s, P, w.sc + 4);
+        norm2_kernel<<<grid_for(NS, sms), kThreads, 0, st>>>(w.r, NS, w.sc + 5);
+        scale_start_kernel<<<grid_for(P + NS, sms), kThreads, 0, st>>>(x, P, w.r, y, NS, w.sc, 4, 5);
+        CG_CALL(sar_adjoint(plan, w.r, w.s, st));
     } else {
         CG_CALL(sar_forward(plan, x, w.r, st));
         residual_kernel<<<grid_for(NS, sms), kThreads, 0, st>>>(w.r, y, NS);
@@ -191,7 +243,7 @@ extern "C" int sar_cgls(sar_plan* plan, const void* y_dev, void* x_dev, int zero
     CG_CUDA(cudaMemcpyAsync(w.p, w.s, sizeof(float2) * P, cudaMemcpyDeviceToDevice, st), "p = s");
     CG_CUDA(cudaGetLastError(), "CGLS set-up kernels");
 
-    double host_sc[4];
+    double host_sc[6];
     CG_CUDA(cudaMemcpyAsync(host_sc, w.sc, sizeof host_sc, cudaMemcpyDeviceToHost, st), "read scalars");
     CG_CUDA(cudaStreamSynchronize(st), "CGLS set-up");
     const double norm_ahy = std::sqrt(host_sc[3]);
@@ -237,4 +289,10 @@ extern "C" int sar_cgls(sar_plan* plan, const void* y_dev, void* x_dev, int zero
     }
     CG_CUDA(cudaGetLastError(), "CGLS kernels");
     return SAR_OK;
+}
+
+extern "C" int sar_cgls(sar_plan* plan, const void* y_dev, void* x_dev, int zero_start, int max_iterations,
+                        double tolerance, double* history, sar_cgls_result* result, void* stream) {
+    return sar_cgls_ex(plan, y_dev, x_dev, zero_start ? SAR_CGLS_START_ZERO : SAR_CGLS_START_GIVEN, nullptr,
+                       max_iterations, tolerance, history, result, stream);
 }

@@ -108,3 +108,20 @@ def test_cgls_rejects_non_finite_data():
     # The plan stays usable.
     x, info = cgls(plan, torch.from_numpy(y.astype(np.complex64)), tol=1e-2, max_iterations=50)
     assert info.converged
+
+
+def test_cgls_scaled_start_and_precomputed_ahy():
+    case, prob, y = noisy_case(seed=4)
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp="linear")
+    yt = torch.from_numpy(y.astype(np.complex64)).cuda()
+    b = plan.adjoint(yt)
+    z = 3.7 * b   # a direction of arbitrary scale
+    _, given = cgls(plan, yt, x0=z, tol=1e-3, max_iterations=300)
+    xs, scaled = cgls(plan, yt, x0=z, tol=1e-3, max_iterations=300, start="scaled")
+    xs2, scaled2 = cgls(plan, yt, x0=z, tol=1e-3, max_iterations=300, start="scaled", ahy=b)
+    # The scaled start is the best multiple of z: its residual is that of one steepest-descent step.
+    _, plain = cgls(plan, yt, tol=0.0, max_iterations=1)
+    assert scaled.history[0] < given.history[0]
+    assert abs(scaled.history[0] - plain.history[1]) < 1e-3 * plain.history[1] + 1e-6
+    assert scaled.converged and scaled2.converged and scaled2.iterations == scaled.iterations
+    assert float((xs - xs2).abs().max()) <= 1e-6 * float(xs.abs().max())
