@@ -123,12 +123,15 @@ class SarPlan:
         t = t.to(device=self.device, non_blocking=True)
         if t.dtype != torch.complex64:
             t = t.to(torch.complex64)
-        return t.contiguous()
+        # Kernels read raw memory: materialise PyTorch's lazy conjugate / negative views
+        # (autograd hands such views to backward functions).
+        return t.resolve_conj().resolve_neg().contiguous()
 
     def _check_out(self, out: Optional[torch.Tensor], shape, name: str) -> torch.Tensor:
         if out is None:
             return torch.empty(shape, dtype=torch.complex64, device=self.device)
-        if out.dtype != torch.complex64 or out.device != self.device or not out.is_contiguous():
+        if (out.dtype != torch.complex64 or out.device != self.device or not out.is_contiguous()
+                or out.is_conj() or out.is_neg()):
             raise ValueError(f"{name} must be a contiguous complex64 tensor on {self.device}")
         if out.numel() != int(np.prod(shape)):
             raise ValueError(f"{name} has the wrong size")

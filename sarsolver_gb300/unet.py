@@ -117,7 +117,7 @@ class UNet:
         """``U(in_scale * x)`` for complex64 ``x`` of shape ``[B, H, W]`` (or ``[H, W]``)."""
         squeeze = x.dim() == 2
         xx = x.reshape(1, *x.shape) if squeeze else x
-        xx = xx.to(device=self.device, dtype=torch.complex64).contiguous()
+        xx = xx.to(device=self.device, dtype=torch.complex64).resolve_conj().resolve_neg().contiguous()
         B, H, W = xx.shape
         out = torch.empty_like(xx)
         with torch.cuda.device(self.device):
@@ -128,7 +128,7 @@ class UNet:
 
     def backward(self, grad_out: torch.Tensor) -> None:
         """Accumulate parameter gradients for ``grad_out`` of the last forward call."""
-        g = grad_out.to(device=self.device, dtype=torch.complex64).contiguous()
+        g = grad_out.to(device=self.device, dtype=torch.complex64).resolve_conj().resolve_neg().contiguous()
         if g.numel() != int(np.prod(self._last_shape)):
             raise ValueError("grad_out does not match the last forward call")
         with torch.cuda.device(self.device):

@@ -238,3 +238,15 @@ def test_sharpness_autofocus_recovers_smooth_phase_error():
     after = np.sqrt(np.mean(detrended(phi_err - phi.cpu().numpy()) ** 2))
     assert after < 0.5 * before
     assert plan.device_flags() == 0
+
+
+def test_lazy_conjugate_gradients_are_materialised():
+    """Autograd passes lazily conjugated views to backward; the kernels must see the values."""
+    case = small_case()
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp="linear")
+    rng = np.random.default_rng(21)
+    x = torch.from_numpy(crandn(rng, plan.num_scatterers).astype(np.complex64)).cuda().requires_grad_(True)
+    v = torch.from_numpy(crandn(rng, plan.num_slow_times, plan.num_freqs).astype(np.complex64)).cuda()
+    (sar_forward(plan, x).conj() * v).sum().real.backward()      # grad_y arrives as a conj view
+    assert torch.allclose(x.grad, plan.adjoint(v), rtol=1e-6, atol=0)
+    assert torch.equal(plan.adjoint(v.conj()), plan.adjoint(v.conj().resolve_conj()))
