@@ -373,15 +373,21 @@ __global__ void pool_bwd_add_mask_kernel(const bf16* __restrict__ gpool, const b
     }
 }
 
-// db[c] += sum_p dz[p][c].
+// db[c] += sum_p dz[p][c].  256 threads = (256 / C) pixel lanes x C channels (C divides 256),
+// grid-stride over pixels with coalesced rows, a shared-memory sum over the pixel lanes and one
+// atomic per channel per CTA.
 __global__ void bias_grad_kernel(const bf16* __restrict__ dz, size_t P, int C, float* __restrict__ db) {
-    const int c = threadIdx.x;
-    if (c >= C) return;
-    const size_t per = (P + gridDim.x - 1) / gridDim.x;
-    const size_t p0 = blockIdx.x * per, p1 = min(P, p0 + per);
+    __shared__ float part[256];
+    const int lanes = blockDim.x / C, c = threadIdx.x % C, pl = threadIdx.x / C;
     float acc = 0.f;
-    for (size_t p = p0; p < p1; ++p) acc += bf(dz[p * C + c]);
-    atomicAdd(db + c, acc);
+    for (size_t p = (size_t)blockIdx.x * lanes + pl; p < P; p += (size_t)gridDim.x * lanes) acc += bf(dz[p * C + c]);
+    part[threadIdx.x] = acc;
+    __syncthreads();
+    if (threadIdx.x < C) {
+        float sum = 0.f;
+        for (int l = 0; l < lanes; ++l) sum += part[l * C + threadIdx.x];
+        atomicAdd(db + threadIdx.x, sum);
+    }
 }
 
 // FP32 master -> bf16 forward [Cout][tap][Cin] and backward-data [Cin][8 - tap][Cout] copies.
@@ -529,8 +535,9 @@ int layer_backward(sar_unet* n, int i, cudaStream_t st) {
     const int h = n->H >> l.level, w = n->W >> l.level;
     const size_t P = n->pixels(l.level);
     U_CALL(conv_wgrad(s0, s1, n->dz[i], l.cout, n->B, h, w, l.taps, n->grads + n->w_off[i], n->flags, st));
-    bias_grad_kernel<<<(unsigned)std::max<size_t>(1, std::min<size_t>(2048, P / 64)), l.cout, 0, st>>>(
-        n->dz[i], P, l.cout, n->grads + n->b_off[i]);
+    const size_t lanes = 256 / l.cout;
+    bias_grad_kernel<<<(unsigned)std::max<size_t>(1, std::min<size_t>((size_t)device_sms() * 4, P / (lanes * 16))), 256,
+                       0, st>>>(n->dz[i], P, l.cout, n->grads + n->b_off[i]);
     U_CUDA(cudaGetLastError(), "bias gradient");
     if (i == 0) return SAR_OK;
     Dst d0, d1;
