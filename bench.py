@@ -52,6 +52,22 @@ def dist_info():
     return rank, world, local
 
 
+def reduce_max(value: float, world: int, device=None) -> float:
+    """Max of a per-rank value over all ranks (the job's clock is its slowest rank)."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_rank: float, world: int, ms_max: float) -> float:
+    """Whole-job units/s: every rank runs the full workload (replicas), timed by the slowest rank."""
+    return world * units_per_rank / (ms_max * 1e-3)
+
+
 def measured_peaks():
     path = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -162,12 +178,8 @@ def run_ours(args):
     ms = e0.elapsed_time(e1) / args.steps
     stage_ms, calls = plan.stage_times()
     plan.enable_stage_timing(False)
-    ms_t = torch.tensor([ms], device=dev)
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms = float(ms_t.item())
-    value = world * P * S / (ms * 1e-3)
+    ms = reduce_max(ms, world, dev)
+    value = job_throughput(P * S, world, ms)
 
     # ---- forward projection y = A x (same workload), device-resident, stage-timed
     y_out = torch.empty((S, N), dtype=torch.complex64, device=dev)
@@ -195,12 +207,7 @@ def run_ours(args):
         x_host.copy_(op.backproject(y_host), non_blocking=True)
     e1.record(stream)
     barrier()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    et = torch.tensor([e2e_ms], device=dev)
-    if world > 1:
-        import torch.distributed as dist
-        dist.all_reduce(et, op=dist.ReduceOp.MAX)
-    e2e_ms = float(et.item())
+    e2e_ms = reduce_max(e0.elapsed_time(e1) / args.steps, world, dev)
 
     # ---- roofline of the gather kernel (SFU bound: 3 MUFU per pixel-pulse, 16 MUFU/clk/SM)
     props = torch.cuda.get_device_properties(dev)
@@ -232,7 +239,7 @@ def run_ours(args):
                      "unit": "px*pulse/s", "frac": achieved / r_roof, "traffic": traffic,
                      "peak_basis": f"{props.multi_processor_count} SMs x {sm_max:.0f} MHz x 16 MUFU/clk/SM / "
                                    "3 MUFU per px*pulse (sm_max_mhz of MEASURED_PEAKS.json)"},
-        "e2e": {"value": world * P * S / (e2e_ms * 1e-3), "unit": UNIT, "ms_per_step": e2e_ms,
+        "e2e": {"value": job_throughput(P * S, world, e2e_ms), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": S * N * 8, "d2h_bytes_per_step": P * 8,
                 "api": "NumpySimpleSarOperator.backproject(pinned host complex64 tensor) -> pinned host copy"},
         # our kernels per call: pack + unpack per FFT chunk, then the gather (cuFFT's own excluded)
