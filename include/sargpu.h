@@ -126,6 +126,14 @@ int sar_plan_get_info(const sar_plan *plan, sar_plan_info *info);
 int sar_forward(sar_plan *plan, const void *x_dev, void *y_dev, void *stream);
 /* x[P] = A^H y[S][N].  Device complex64 buffers; asynchronous on `stream`. */
 int sar_adjoint(sar_plan *plan, const void *y_dev, void *x_dev, void *stream);
+/* Backprojection of one block of pulses, for streaming a phase history through the device:
+ * y_block_dev holds rows first_pulse .. first_pulse + count - 1 (complex64 [count][N], fftshifted
+ * like y); x_dev = (accumulate ? x_dev : 0) + contribution of those pulses.  Summing the blocks of a
+ * partition of [0, S) in order reproduces sar_adjoint (up to FP32 summation order).  Regular-grid
+ * plans only.  Replaces the reference's slow-time blocking (num_calculation_blocks,
+ * cxx_binding/adjoint.py:66-94) with device-side accumulation. */
+int sar_adjoint_pulse_block(sar_plan *plan, const void *y_block_dev, size_t first_pulse, size_t count,
+                            void *x_dev, int accumulate, void *stream);
 /* Upsampled range profiles over the stored span, prof[S][profile_length] complex64,
  * bin profile_first_bin + w at column w, no slow-time weight (test and inspection aid). */
 int sar_profiles(sar_plan *plan, const void *y_dev, void *prof_dev, void *stream);

@@ -29,7 +29,7 @@ EXPORTED = (
     "sar_set_slow_time_weighting", "sar_set_slow_time_weighting_device",
     "sar_device_flags", "sar_last_error", "sar_status_string",
     "sar_enable_stage_timing", "sar_stage_times",
-    "sar_adjoint_from_profiles_noalloc", "sar_phase_gradient", "sar_sharpness", "sar_cgls", "sar_cgls_ex",
+    "sar_adjoint_from_profiles_noalloc", "sar_phase_gradient", "sar_sharpness", "sar_cgls", "sar_cgls_ex", "sar_adjoint_pulse_block",
     "sar_unet_create", "sar_unet_destroy", "sar_unet_info", "sar_unet_set_params", "sar_unet_get_params",
     "sar_unet_get_grads", "sar_unet_zero_grad", "sar_unet_forward", "sar_unet_backward", "sar_unet_adam_step",
     "sar_unet_flags", "sar_conv2d_forward_bf16", "sar_conv2d_wgrad_bf16",
@@ -126,6 +126,8 @@ def load() -> ctypes.CDLL:
     lib.sar_cgls_ex.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_void_p, c_int, c_double, c_void_p,
                                 POINTER(SarCglsResult), c_void_p]
     lib.sar_cgls_ex.restype = c_int
+    lib.sar_adjoint_pulse_block.argtypes = [c_void_p, c_void_p, c_size_t, c_size_t, c_void_p, c_int, c_void_p]
+    lib.sar_adjoint_pulse_block.restype = c_int
     P = c_void_p
     unet_sigs = {
         "sar_unet_create": [c_int, c_int, P],

@@ -118,6 +118,8 @@ struct sar_plan {
     size_t device_bytes = 0;
     cufftHandle fft_full = 0, fft_tail = 0;
     bool have_full = false, have_tail = false;
+    int tail_rows = 0;
+    std::vector<std::pair<int, cufftHandle>> fft_other;   // other batch sizes (pulse blocks), made on first use
     cudaStream_t last_stream = nullptr;
     std::mutex mu;
     // stage timing: 4 events per recorded call (start, pre-kernel done, kernel done, end)
@@ -160,6 +162,7 @@ struct sar_plan {
         cudaFree(d_flags);
         if (have_full) cufftDestroy(fft_full);
         if (have_tail) cufftDestroy(fft_tail);
+        for (auto& e : fft_other) cufftDestroy(e.second);
         for (auto& ev : events)
             for (auto e : ev) cudaEventDestroy(e);
     }
@@ -204,7 +207,20 @@ int make_fft(cufftHandle* h, long M, int batch, bool dbl) {
 }
 
 int run_fft(sar_plan* p, void* data, int rows, int direction, cudaStream_t st) {
-    cufftHandle h = (rows == p->chunk) ? p->fft_full : p->fft_tail;
+    cufftHandle h = 0;
+    if (rows == p->chunk) {
+        h = p->fft_full;
+    } else if (p->have_tail && rows == p->tail_rows) {
+        h = p->fft_tail;
+    } else {
+        for (auto& e : p->fft_other)
+            if (e.first == rows) h = e.second;
+        if (!h) {
+            int rc = make_fft(&h, (long)p->M, rows, p->fft_double);
+            if (rc) return rc;
+            p->fft_other.emplace_back(rows, h);
+        }
+    }
     SAR_CUFFT(cufftSetStream(h, st), "cufftSetStream");
     if (p->fft_double)
         SAR_CUFFT(cufftExecZ2Z(h, reinterpret_cast<cufftDoubleComplex*>(data),
@@ -520,6 +536,7 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
     if (tail) {
         if ((rc = make_fft(&p->fft_tail, (long)M, tail, p->fft_double))) return rc;
         p->have_tail = true;
+        p->tail_rows = tail;
     }
     return SAR_OK;
 }
@@ -593,9 +610,11 @@ int sar_plan_get_info(const sar_plan* p, sar_plan_info* info) {
     return SAR_OK;
 }
 
-static int upsample_into_pairs(sar_plan* p, const float2* y, cudaStream_t st, bool pairs_out, float2* prof) {
-    for (size_t first = 0; first < p->S; first += (size_t)p->chunk) {
-        const int rows = (int)std::min<size_t>(p->chunk, p->S - first);
+// Upsampled profiles of pulses [begin, end): y row s is read at y + s * N.
+static int upsample_rows(sar_plan* p, const float2* y, size_t begin, size_t end, cudaStream_t st, bool pairs_out,
+                         float2* prof) {
+    for (size_t first = begin; first < end; first += (size_t)p->chunk) {
+        const int rows = (int)std::min<size_t>(p->chunk, end - first);
         const int dbl = p->fft_double;
         SAR_CUDA(launch_pack_adjoint(y, p->d_wave, p->d_spec, dbl, (int)p->N, (long)p->M, rows, (int)first, st), "pack");
         int rc = run_fft(p, p->d_spec, rows, CUFFT_INVERSE, st);
@@ -609,6 +628,10 @@ static int upsample_into_pairs(sar_plan* p, const float2* y, cudaStream_t st, bo
                      "unpack");
     }
     return SAR_OK;
+}
+
+static int upsample_into_pairs(sar_plan* p, const float2* y, cudaStream_t st, bool pairs_out, float2* prof) {
+    return upsample_rows(p, y, 0, p->S, st, pairs_out, prof);
 }
 
 static PointArgs point_args(sar_plan* p, int bin_rule) {
@@ -709,6 +732,40 @@ int sar_forward(sar_plan* p, const void* x_dev, void* y_dev, void* stream) {
                  "extract");
     }
     mark(ev, 3, st);
+    return SAR_OK;
+}
+
+int sar_adjoint_pulse_block(sar_plan* p, const void* y_block_dev, size_t first_pulse, size_t count, void* x_dev,
+                            int accumulate, void* stream) {
+    if (!p || !y_block_dev || !x_dev) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    if (!count || first_pulse >= p->S || count > p->S - first_pulse)
+        return fail(SAR_ERR_INVALID_ARGUMENT, "pulse block [%zu, %zu) outside [0, %zu)", first_pulse,
+                    first_pulse + count, p->S);
+    if (!p->grid) return fail(SAR_ERR_NOT_SUPPORTED, "pulse blocks need a regular-grid plan");
+    std::lock_guard<std::mutex> lock(p->mu);
+    DeviceGuard guard(p->device);
+    if (guard.status != cudaSuccess) return cuda_fail(guard.status, "select device");
+    cudaStream_t st = (cudaStream_t)stream;
+    p->last_stream = st;
+    // The block holds rows first_pulse .. first_pulse + count - 1; the pack kernel addresses row s
+    // at y + s * N, so the base is moved back by first_pulse rows (only rows of the block are read).
+    const float2* y = reinterpret_cast<const float2*>(y_block_dev) - first_pulse * p->N;
+    int rc = upsample_rows(p, y, first_pulse, first_pulse + count, st, true, nullptr);
+    if (rc) return rc;
+    BpGridArgs a;
+    a.g = p->gc_adj;
+    a.pulses = p->d_pulses + first_pulse;
+    a.pairs = p->d_prof + first_pulse * (size_t)p->Lg;
+    a.x = (float2*)x_dev;
+    a.flags = p->d_flags;
+    a.S = (int)count;
+    a.Lg = p->Lg;
+    a.bg0 = (int)p->bg0;
+    a.wwin = p->wwin;
+    a.pb = p->pb;
+    a.staged = p->staged;
+    a.accumulate = accumulate ? 1 : 0;
+    SAR_CUDA(p->staged ? launch_bp_grid_ws(a, st) : launch_bp_grid(a, st), "backprojection");
     return SAR_OK;
 }
 

@@ -156,6 +156,44 @@ class SarPlan:
                                              ctypes.c_void_p(x.data_ptr()), self._stream()), "sar_adjoint")
         return x
 
+    def adjoint_streamed(self, y_host: torch.Tensor, block: int = 512, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """x = A^H y with y in host memory (pin it for overlap), streamed through the device in
+        blocks of ``block`` pulses: block b + 1 is copied on a side stream while block b is
+        backprojected on the current stream into the resident image (``sar_adjoint_pulse_block``
+        with accumulation).  Device memory for y is two blocks."""
+        if not self.is_grid:
+            raise ValueError("streamed backprojection needs a regular-grid scene")
+        S, N = self.num_slow_times, self.num_freqs
+        yh = torch.as_tensor(y_host).reshape(S, N)
+        if yh.dtype != torch.complex64:
+            yh = yh.to(torch.complex64)
+        yh = yh.resolve_conj().resolve_neg().contiguous()
+        x = self._check_out(out, (self.num_scatterers,), "out")
+        block = max(1, min(int(block), S))
+        compute = torch.cuda.current_stream(self.device)
+        side = torch.cuda.Stream(self.device)
+        bufs = [torch.empty((block, N), dtype=torch.complex64, device=self.device) for _ in range(2)]
+        copied = [torch.cuda.Event() for _ in range(2)]
+        consumed = [torch.cuda.Event() for _ in range(2)]
+        nblk = (S + block - 1) // block
+        with torch.cuda.device(self.device):
+            for k in range(nblk):
+                b, first = k % 2, k * block
+                count = min(block, S - first)
+                with torch.cuda.stream(side):
+                    if k >= 2:
+                        side.wait_event(consumed[b])
+                    bufs[b][:count].copy_(yh[first:first + count], non_blocking=True)
+                    copied[b].record(side)
+                bufs[b].record_stream(side)
+                compute.wait_event(copied[b])
+                _lib.check(self._lib.sar_adjoint_pulse_block(self._handle, ctypes.c_void_p(bufs[b].data_ptr()), first,
+                                                             count, ctypes.c_void_p(x.data_ptr()), int(k > 0),
+                                                             ctypes.c_void_p(compute.cuda_stream)),
+                           "sar_adjoint_pulse_block")
+                consumed[b].record(compute)
+        return x
+
     def profiles(self, y: torch.Tensor) -> torch.Tensor:
         """Upsampled range profiles over the stored span, complex64 [S, profile_length]."""
         y = self._as_input(y, self.num_slow_times * self.num_freqs, "y")

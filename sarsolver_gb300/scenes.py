@@ -97,4 +97,7 @@ def config_workload(name: str):
     if name == "config3":
         return (spotlight_aperture(2048, 2048, 3.0), grid_scene(1024, 0.25), 8.0,
                 "2048 pulses x 2048 samples, U=8, 1024^2 at 0.25 m")
+    if name == "config5":
+        return (spotlight_aperture(16384, 8192, 5.0), grid_scene(8192, 0.125), 8.0,
+                "16384 pulses x 8192 samples, U=8, 8192^2 at 0.125 m, 5 deg")
     raise ValueError(name)
