@@ -115,6 +115,7 @@ typedef struct sar_plan_info {
     int interp;                 /* SAR_INTERP_* of the plan */
     size_t num_fast_times, num_slow_times, num_scatterers;   /* N, S, P */
     int device;                 /* CUDA device of the plan */
+    int fft_callbacks;          /* 1: range-profile FFTs run with cuFFT load/store callbacks */
 } sar_plan_info;
 
 /* Create a plan on `device` (-1: the current device).  Copies all host inputs. */

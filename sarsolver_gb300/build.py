@@ -22,7 +22,11 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math"]
 CUDA_UNITS = ["sar_kernels.cu", "sar_api.cu", "sar_noalloc.cu", "sar_cgls.cu", "sar_unet.cu"]
-HEADERS = ["sar_geom.cuh", "sar_host_prep.h", "sar_kernels.cuh", "unet_tc.cuh"]
+HEADERS = ["sar_geom.cuh", "sar_host_prep.h", "sar_kernels.cuh", "unet_tc.cuh", "sar_fft_cb.h"]
+# cuFFT load/store callbacks: compiled to LTO-IR, embedded in the library as a byte array and
+# handed to cufftXtSetJITCallback at plan creation.
+CALLBACK_UNIT = "sar_fft_callbacks.cu"
+CALLBACK_ARCH = ["-gencode", "arch=compute_103a,code=lto_103a"]
 
 GPU_LIB = os.path.join(BUILD, "libsargpu.so")
 HOST_LIB = os.path.join(BUILD, "libsargeom_host.so")
@@ -64,6 +68,10 @@ def build(verbose: bool = False) -> dict:
         objs.append(obj)
         if _stale(obj, [src] + headers):
             cmds.append([nvcc] + ARCH + NVCC_FLAGS + ["-c", src, "-o", obj])
+    cb_src = os.path.join(CSRC, CALLBACK_UNIT)
+    cb_fatbin = os.path.join(BUILD, "sar_fft_callbacks.fatbin")
+    if _stale(cb_fatbin, [cb_src, os.path.join(CSRC, "sar_fft_cb.h")]):
+        cmds.append([nvcc] + CALLBACK_ARCH + ["-O3", "-std=c++17", "-rdc=true", "-fatbin", "-o", cb_fatbin, cb_src])
     host_src = os.path.join(CSRC, "geom_host.cpp")
     if _stale(HOST_LIB, [host_src] + headers):
         cmds.append(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", "-fno-fast-math", "-ffp-contract=off",
@@ -73,8 +81,20 @@ def build(verbose: bool = False) -> dict:
             for c in cmds:
                 print(" ".join(c))
         _run_parallel(cmds)
+    blob_src = os.path.join(BUILD, "sar_fft_callbacks_blob.cpp")
+    blob_obj = os.path.join(BUILD, "sar_fft_callbacks_blob.o")
+    if _stale(blob_obj, [cb_fatbin]):
+        data = open(cb_fatbin, "rb").read()
+        body = ",".join(str(b) for b in data)
+        with open(blob_src, "w") as f:
+            f.write("#include <cstddef>\n"
+                    f"extern \"C\" const unsigned char sar_fft_cb_fatbin[{len(data)}] = {{{body}}};\n"
+                    f"extern \"C\" const size_t sar_fft_cb_fatbin_size = {len(data)};\n")
+        _run_parallel([["g++", "-O1", "-fPIC", "-c", blob_src, "-o", blob_obj]])
+    objs.append(blob_obj)
     if _stale(GPU_LIB, objs):
-        _run_parallel([[nvcc] + ARCH + ["-shared", "-o", GPU_LIB] + objs + ["-cudart", "shared", "-lcufft"]])
+        _run_parallel([[nvcc] + ARCH + ["-shared", "-o", GPU_LIB] + objs +
+                       ["-cudart", "shared", "-lcufft", "-lnvJitLink"]])
     return {"gpu": GPU_LIB, "host": HOST_LIB}
 
 

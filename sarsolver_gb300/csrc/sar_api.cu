@@ -23,6 +23,12 @@
 #include "../../include/sargpu.h"
 #include "sar_host_prep.h"
 #include "sar_kernels.cuh"
+#include "sar_fft_cb.h"
+
+#include <cufftXt.h>
+
+extern "C" const unsigned char sar_fft_cb_fatbin[];
+extern "C" const size_t sar_fft_cb_fatbin_size;
 
 using namespace sar;
 
@@ -120,6 +126,14 @@ struct sar_plan {
     bool have_full = false, have_tail = false;
     int tail_rows = 0;
     std::vector<std::pair<int, cufftHandle>> fft_other;   // other batch sizes (pulse blocks), made on first use
+    // cuFFT callback path (single precision, large problems): plans per direction and batch size
+    // with the load/store callbacks of sar_fft_callbacks.cu linked in, their parameter block, and
+    // the compact adjoint output [chunk][Lc].
+    bool fft_cb = false;
+    SarFftCbInfo* d_cb = nullptr;
+    float2* d_compact = nullptr;
+    int Lc = 0;
+    std::vector<std::pair<int, cufftHandle>> cb_adj, cb_fwd;
     cudaStream_t last_stream = nullptr;
     std::mutex mu;
     // stage timing: 4 events per recorded call (start, pre-kernel done, kernel done, end)
@@ -163,6 +177,10 @@ struct sar_plan {
         if (have_full) cufftDestroy(fft_full);
         if (have_tail) cufftDestroy(fft_tail);
         for (auto& e : fft_other) cufftDestroy(e.second);
+        for (auto& e : cb_adj) cufftDestroy(e.second);
+        for (auto& e : cb_fwd) cufftDestroy(e.second);
+        cudaFree(d_cb);
+        cudaFree(d_compact);
         for (auto& ev : events)
             for (auto e : ev) cudaEventDestroy(e);
     }
@@ -230,6 +248,68 @@ int run_fft(sar_plan* p, void* data, int rows, int direction, cudaStream_t st) {
         SAR_CUFFT(cufftExecC2C(h, reinterpret_cast<cufftComplex*>(data), reinterpret_cast<cufftComplex*>(data),
                                direction),
                   "cufftExecC2C");
+    return SAR_OK;
+}
+
+// A C2C plan of `batch` rows of length M with the adjoint (inverse) or forward callbacks linked in.
+int make_cb_fft(sar_plan* p, cufftHandle* h, int batch, bool adjoint) {
+    SAR_CUFFT(cufftCreate(h), "cufftCreate");
+    void* info = p->d_cb;
+    cufftResult r = cufftXtSetJITCallback(*h, adjoint ? "sar_cb_adjoint_load" : "sar_cb_forward_load", sar_fft_cb_fatbin,
+                                          sar_fft_cb_fatbin_size, CUFFT_CB_LD_COMPLEX, &info);
+    if (r == CUFFT_SUCCESS)
+        r = cufftXtSetJITCallback(*h, adjoint ? "sar_cb_adjoint_store" : "sar_cb_forward_store", sar_fft_cb_fatbin,
+                                  sar_fft_cb_fatbin_size, CUFFT_CB_ST_COMPLEX, &info);
+    size_t work = 0;
+    int n[1] = {(int)p->M};
+    if (r == CUFFT_SUCCESS)
+        r = cufftMakePlanMany(*h, 1, n, nullptr, 1, (int)p->M, nullptr, 1, (int)p->M, CUFFT_C2C, batch, &work);
+    if (r != CUFFT_SUCCESS) {
+        cufftDestroy(*h);
+        *h = 0;
+        return fail(SAR_ERR_CUFFT, "callback FFT plan (batch %d): cufft error %d", batch, (int)r);
+    }
+    return SAR_OK;
+}
+
+int cb_plan(sar_plan* p, int rows, bool adjoint, cufftHandle* h) {
+    auto& list = adjoint ? p->cb_adj : p->cb_fwd;
+    for (auto& e : list)
+        if (e.first == rows) {
+            *h = e.second;
+            return SAR_OK;
+        }
+    int rc = make_cb_fft(p, h, rows, adjoint);
+    if (rc) return rc;
+    list.emplace_back(rows, *h);
+    return SAR_OK;
+}
+
+// Parameters of one callback transform (rows first .. first + rows - 1), stream-ordered.
+int set_cb_info(sar_plan* p, const float2* y, float2* yout, int first, cudaStream_t st) {
+    SarFftCbInfo c{};
+    c.y = y;
+    c.yout = yout;
+    c.wave = p->d_wave;
+    c.wfac = p->d_wfwd;
+    c.acc = reinterpret_cast<const float2*>(p->d_prof);
+    c.compact = p->d_compact;
+    c.M = (long long)p->M;
+    long long nb0 = -(long long)p->bg0 % (long long)p->M;
+    if (nb0 < 0) nb0 += (long long)p->M;
+    c.nb0 = nb0;
+    const bool pow2 = (p->M & (p->M - 1)) == 0;
+    c.mask = pow2 ? (unsigned)(p->M - 1) : 0u;
+    int sh = 0;
+    while (pow2 && ((size_t)1 << sh) < p->M) ++sh;
+    c.shift = sh;
+    c.N = (int)p->N;
+    c.half = (int)(p->N / 2);
+    c.Lg = p->Lg;
+    c.Lc = p->Lc;
+    c.first = first;
+    // pageable source: the copy is staged before the call returns, so `c` may go out of scope
+    SAR_CUDA(cudaMemcpyAsync(p->d_cb, &c, sizeof c, cudaMemcpyHostToDevice, st), "callback parameters");
     return SAR_OK;
 }
 
@@ -538,6 +618,30 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
         p->have_tail = true;
         p->tail_rows = tail;
     }
+    // Callback transforms (single precision): opt-in with SAR_FFT_CALLBACKS=1.  On GB300 with the
+    // cuFFT of CUDA 13.0, plans with JIT (LTO) callbacks fail to build (CUFFT_INTERNAL_ERROR from
+    // cufftMakePlanMany for LTO-IR of compute_90 .. compute_103a alike), so the packing kernels are
+    // the default; when forced on, a plan that cannot link the callbacks reports why.
+    {
+        const char* env = getenv("SAR_FFT_CALLBACKS");
+        const bool want = !p->fft_double && env && env[0] == '1';
+        if (want) {
+            p->Lc = (int)std::min<size_t>((size_t)p->Lg + 1, M);
+            cufftHandle h = 0;
+            int crc = p->alloc(&p->d_cb, 1, "callback parameters");
+            if (!crc) crc = p->alloc(&p->d_compact, (size_t)p->chunk * p->Lc, "compact profiles");
+            if (!crc) crc = cb_plan(p, p->chunk, true, &h);
+            if (!crc) crc = cb_plan(p, p->chunk, false, &h);
+            if (!crc) {
+                p->fft_cb = true;
+            } else if (env && env[0] == '1') {
+                return crc;   // forced on: report why the callbacks could not be linked
+            } else {
+                cudaGetLastError();
+                g_last_error.clear();
+            }
+        }
+    }
     return SAR_OK;
 }
 
@@ -607,6 +711,7 @@ int sar_plan_get_info(const sar_plan* p, sar_plan_info* info) {
     info->num_slow_times = p->S;
     info->num_scatterers = p->P;
     info->device = p->device;
+    info->fft_callbacks = p->fft_cb ? 1 : 0;
     return SAR_OK;
 }
 
@@ -616,6 +721,21 @@ static int upsample_rows(sar_plan* p, const float2* y, size_t begin, size_t end,
     for (size_t first = begin; first < end; first += (size_t)p->chunk) {
         const int rows = (int)std::min<size_t>(p->chunk, end - first);
         const int dbl = p->fft_double;
+        if (p->fft_cb) {
+            cufftHandle h = 0;
+            int rc = cb_plan(p, rows, true, &h);
+            if (rc) return rc;
+            if ((rc = set_cb_info(p, y, nullptr, (int)first, st))) return rc;
+            SAR_CUFFT(cufftSetStream(h, st), "cufftSetStream");
+            SAR_CUFFT(cufftExecC2C(h, reinterpret_cast<cufftComplex*>(p->d_spec), reinterpret_cast<cufftComplex*>(p->d_spec),
+                                   CUFFT_INVERSE),
+                      "cufftExecC2C (callbacks)");
+            SAR_CUDA(launch_unpack_compact(p->d_compact, p->Lc, p->d_wadj, pairs_out ? p->d_prof : nullptr,
+                                           pairs_out ? nullptr : prof, (long)p->M, p->Lg, rows, (int)first,
+                                           p->interp == SAR_INTERP_LINEAR, st),
+                     "unpack");
+            continue;
+        }
         SAR_CUDA(launch_pack_adjoint(y, p->d_wave, p->d_spec, dbl, (int)p->N, (long)p->M, rows, (int)first, st), "pack");
         int rc = run_fft(p, p->d_spec, rows, CUFFT_INVERSE, st);
         if (rc) return rc;
@@ -723,6 +843,17 @@ int sar_forward(sar_plan* p, const void* x_dev, void* y_dev, void* stream) {
     mark(ev, 2, st);
     for (size_t first = 0; first < p->S; first += (size_t)p->chunk) {
         const int rows = (int)std::min<size_t>(p->chunk, p->S - first);
+        if (p->fft_cb) {
+            cufftHandle h = 0;
+            int rc = cb_plan(p, rows, false, &h);
+            if (rc) return rc;
+            if ((rc = set_cb_info(p, nullptr, (float2*)y_dev, (int)first, st))) return rc;
+            SAR_CUFFT(cufftSetStream(h, st), "cufftSetStream");
+            SAR_CUFFT(cufftExecC2C(h, reinterpret_cast<cufftComplex*>(p->d_spec), reinterpret_cast<cufftComplex*>(p->d_spec),
+                                   CUFFT_FORWARD),
+                      "cufftExecC2C (callbacks)");
+            continue;
+        }
         SAR_CUDA(launch_pack_forward(acc, p->d_spec, p->fft_double, (long)p->M, p->Lg, p->bg0, rows, (int)first, st),
                  "pack");
         int rc = run_fft(p, p->d_spec, rows, CUFFT_FORWARD, st);

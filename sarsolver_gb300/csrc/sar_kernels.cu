@@ -1149,6 +1149,44 @@ __global__ void unpack_pairs_kernel(const T* __restrict__ spec, const float2* __
     pairs[(size_t)(first + row) * Lg + w] = out;
 }
 
+// Stored span from the callback transform's compact output compact[row][w] (w = bin - bg0;
+// Lc = min(Lg + 1, M) columns, taken modulo M when the span wraps): pairs as unpack_pairs_kernel,
+// or plain profiles when `pairs` is null.
+__global__ void unpack_compact_kernel(const float2* __restrict__ compact, int Lc, const float2* __restrict__ wfac,
+                                      float4* __restrict__ pairs, float2* __restrict__ prof, long M, int Lg, int first,
+                                      int linear) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= Lg) return;
+    const long row = blockIdx.y;
+    const float2* c = compact + (size_t)row * Lc;
+    const int w0 = (Lc == M) ? (int)(w % M) : w;
+    if (!pairs) {
+        prof[(size_t)(first + row) * Lg + w] = c[w0];
+        return;
+    }
+    const int w1 = (Lc == M) ? (int)((w + 1) % M) : w + 1;
+    const float2 f = __ldg(wfac + first + row);
+    const float2 a = c[w0];
+    const float2 p0 = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
+    float4 out;
+    if (linear) {
+        const float2 b = c[w1];
+        const float2 p1 = make_float2(b.x * f.x - b.y * f.y, b.x * f.y + b.y * f.x);
+        const float dx = p1.x - p0.x, dy = p1.y - p0.y;
+        out = make_float4(fmaf(0.5f, dx, p0.x), fmaf(0.5f, dy, p0.y), dx, dy);
+    } else {
+        out = make_float4(p0.x, p0.y, 0.f, 0.f);
+    }
+    pairs[(size_t)(first + row) * Lg + w] = out;
+}
+
+cudaError_t launch_unpack_compact(const float2* compact, int Lc, const float2* wfac, float4* pairs, float2* prof,
+                                  long M, int Lg, int rows, int first, int linear, cudaStream_t st) {
+    const dim3 grid((unsigned)((Lg + 255) / 256), (unsigned)rows);
+    unpack_compact_kernel<<<grid, 256, 0, st>>>(compact, Lc, wfac, pairs, prof, M, Lg, first, linear);
+    return cudaGetLastError();
+}
+
 template <class T>
 __global__ void unpack_profiles_kernel(const T* __restrict__ spec, float2* __restrict__ prof, long M, int Lg,
                                        long bg0, int first) {

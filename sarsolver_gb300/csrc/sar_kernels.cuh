@@ -83,6 +83,8 @@ cudaError_t launch_fp_points(const PointArgs& a, const float2* x, float2* acc, c
 // complex64, or complex128 when dbl != 0.
 cudaError_t launch_pack_adjoint(const float2* y, const float2* wave, void* spec, int dbl, int N, long M, int rows,
                                 int first, cudaStream_t st);
+cudaError_t launch_unpack_compact(const float2* compact, int Lc, const float2* wfac, float4* pairs, float2* prof,
+                                  long M, int Lg, int rows, int first, int linear, cudaStream_t st);
 cudaError_t launch_unpack_pairs(const void* spec, int dbl, const float2* wfac, float4* pairs, long M, int Lg,
                                 long bg0, int rows, int first, int linear, cudaStream_t st);
 cudaError_t launch_unpack_profiles(const void* spec, int dbl, float2* prof, long M, int Lg, long bg0, int rows,
