@@ -373,11 +373,13 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_kernel(const BpGridA
     df3* anchors = reinterpret_cast<df3*>(bars + 4);
 
     const GridConst& g = a.g;
+    // Consecutive CTAs walk a tile column (y fastest): tiles stacked along y see nearly the same
+    // range windows when range runs along x, so concurrent CTAs share profile rows in L2.
     int tile = blockIdx.x;
-    const int ti = tile % g.tiles_x;
-    tile /= g.tiles_x;
     const int tj = tile % g.tiles_y;
-    const int k = tile / g.tiles_y;
+    tile /= g.tiles_y;
+    const int ti = tile % g.tiles_x;
+    const int k = tile / g.tiles_x;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x < 4) anchors[threadIdx.x] = subtile_anchor(ti, tj, k, threadIdx.x, g);
     if (threadIdx.x == 0) {
