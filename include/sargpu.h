@@ -233,6 +233,28 @@ int sar_conv2d_forward_bf16(const void *x0, int c0, const void *x1, int c1, int 
 int sar_conv2d_wgrad_bf16(const void *x0, int c0, const void *x1, int c1, const void *dz, int cout, int batch,
                           int height, int width, int taps, float *dw, unsigned *flags_dev, void *stream);
 
+/* ------------------------------------------------ 4. dataset resampling (before the operator)
+ * Device phase histories complex64 [S][N], fast time fftshifted; small parameters on the host.
+ *
+ * sar_move_srps: out = ph * exp(i kb_f dR_s) * exp(-2 pi i sign fc dR_s / c), kb_f = 2 pi bb_f / c,
+ *   bb_f = (f - N/2) fs / N, dR_s = change of the pulse's bistatic SRP range (host FP64 [S]).
+ *   Replaces utils.move_srps (src/sarsolver/utils/geodesy.py:33-73).
+ * sar_fast_freq_downsample: out [S][new_N] = fftshift(FFT(window * crop(IFFT(ifftshift(ph))))),
+ *   window = the fftshifted Tukey window (host [new_N]).  Replaces utils.fast_freq_downsample
+ *   (src/sarsolver/utils/signal.py:45-77).
+ * sar_resample_phase_history: both of the above on every pulse (delta_range may be NULL: no SRP
+ *   move), then out[t][f] = sum_k kernel[k] X[row0[t] + k][f] (kernel host complex [L][2], row0
+ *   host [T]).  The phase-history part of NumpySimpleSarDataset.from_resampling
+ *   (src/sarsolver/numpy/measurement.py:342-458). */
+int sar_move_srps(const void *ph_dev, void *out_dev, size_t S, size_t N, const double *delta_range,
+                  double centre_freq, double sample_bandwidth, double sign_multiplier, double c_eff, void *stream);
+int sar_fast_freq_downsample(const void *ph_dev, void *out_dev, size_t S, size_t N, size_t new_N,
+                             const double *window, void *stream);
+int sar_resample_phase_history(const void *ph_dev, size_t S, size_t N, const double *delta_range,
+                               double centre_freq, double sample_bandwidth, double sign_multiplier, double c_eff,
+                               size_t new_N, const double *window, const double *kernel, size_t kernel_length,
+                               const int *row0, size_t num_rows, void *out_dev, void *stream);
+
 /* Stage timing.  While enabled, every sar_forward / sar_adjoint call records CUDA events on
  * its stream around its stages: [0] range-profile FFT side before the main kernel (adjoint:
  * pack + inverse FFT + unpack; forward: accumulator clear), [1] the main gather / scatter

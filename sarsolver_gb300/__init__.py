@@ -7,6 +7,7 @@ Public API (drop-in names of the reference where one exists):
   SarPlan                                   device-tensor plan under both
   cxx_binding                               single_/multi_{forward,adjoint}_evaluate
   autodiff                                  autograd Functions, phase-error gradient, autofocus
+  resample                                  SRP moves and dataset downsampling on the GPU
 """
 from .geometry import GridSarScene, NumpySimpleSarAperture, NumpySimpleSarDataset, SimpleSarScene, grid_axes
 from .plan import SarPlan

@@ -6,6 +6,8 @@
   (oracle/_ref, present only where the reference checkout exists);
 * the exact-transpose property of the linear mode.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -88,3 +90,30 @@ def test_reference_conventions_are_not_an_adjoint_pair():
     lhs = np.vdot(y, oracle.forward(p, x, "nearest_ref"))
     rhs = np.vdot(oracle.adjoint(p, y, "nearest_ref"), x)
     assert abs(lhs - rhs) / abs(lhs) > 1e-3
+
+
+# ------------------------------------------------------------------ dataset resampling oracle
+@pytest.mark.parametrize("name", ["a", "b", "c"])
+def test_resample_oracle_matches_reference_golden(name):
+    from oracle import resample as rs
+    d = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", f"resample_{name}.npz")))
+    fc, fs, sign = float(d["centre_frequency"]), float(d["sample_frequency"]), float(d["sign_multiplier"])
+    moved = rs.move_srps(d["ph"], d["srps"], d["new_srp"], d["tx"], d["rx"], fc, fs, sign)
+    ok = np.isfinite(d["moved"]).all(axis=1)
+    np.testing.assert_allclose(moved[ok], d["moved"][ok], rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(rs.fast_freq_downsample(d["ph"], int(d["n_new"]), 1.2), d["ffd"], rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(rs.downsample_kernel(max(int(d["slow_factor"]), 1)), d["kernel"], rtol=1e-6, atol=1e-7)
+    fast, slow = float(d["fast_factor"]), int(d["slow_factor"])
+    if float(d["range_amb"]) > 0:
+        S, N = d["ph"].shape
+        fast, slow = rs.factors_from_ambiguities(d["tx"], d["rx"], d["new_srp"], fc, fs, S, N, float(d["range_amb"]),
+                                                 float(d["cross_range_amb"]))
+    tx, rx, srps, wt, wave, ph = rs.resample(d["tx"], d["rx"], d["srps"], d["ph"], d["wave"], d["wt"], fc, fs, sign,
+                                              fast, slow, d["new_srp"])
+    np.testing.assert_array_equal(tx, d["out_tx"])
+    np.testing.assert_array_equal(rx, d["out_rx"])
+    np.testing.assert_allclose(srps, d["out_srps"])
+    np.testing.assert_allclose(wt, d["out_wt"], rtol=1e-6)
+    np.testing.assert_allclose(wave, d["out_wave"], rtol=1e-10, atol=1e-12)
+    assert ph.shape == d["out_ph"].shape
+    np.testing.assert_allclose(ph, d["out_ph"], rtol=1e-6, atol=1e-9)
