@@ -5,8 +5,8 @@ These mirror the reference's concrete classes so code written against sarsolver 
   NumpySimpleSarAperture           src/sarsolver/numpy/measurement.py:13-241
   NumpySimpleSarDataset            src/sarsolver/numpy/measurement.py:244-290
 The operator also accepts the reference's own objects (duck typing on the same attributes).
-Grid sizing from k-space (``GridSarScene.from_aperture``) and dataset resampling are not part of
-this package.
+Grid sizing from k-space (``GridSarScene.from_aperture``, ``scene_params_classic_sar``) is host-side
+geometry here too; dataset resampling lives in ``sarsolver_gb300.resample``.
 """
 from __future__ import annotations
 
@@ -15,6 +15,62 @@ from typing import List, Optional, Sequence, Tuple
 import numpy as np
 
 C = 299792458.0
+
+
+# ------------------------------------------------------------------ k-space geometry (host, FP64)
+WGS84_A = 6378137.0
+WGS84_F = 1.0 / 298.257223563
+
+
+def wgs84_up(p_ecef: np.ndarray) -> np.ndarray:
+    """Unit normal of the WGS84 ellipsoid at the geodetic position of an ECEF point (the local
+    'up' the reference takes from pymap3d's enu2ecef at the point's geodetic coordinates)."""
+    x, y, z = (float(v) for v in p_ecef)
+    e2 = WGS84_F * (2.0 - WGS84_F)
+    lon = np.arctan2(y, x)
+    r = np.hypot(x, y)
+    lat = np.arctan2(z, r * (1.0 - e2))
+    for _ in range(8):   # fixed-point iteration on the geodetic latitude
+        n = WGS84_A / np.sqrt(1.0 - e2 * np.sin(lat) ** 2)
+        h = r / np.cos(lat) - n if abs(np.cos(lat)) > 1e-12 else abs(z) - n * (1.0 - e2)
+        lat = np.arctan2(z, r * (1.0 - e2 * n / (n + h)))
+    return np.array([np.cos(lat) * np.cos(lon), np.cos(lat) * np.sin(lon), np.sin(lat)])
+
+
+def kspace_box(points: np.ndarray):
+    """Box around the finite rows of ``points`` aligned with their principal axes
+    (utils/k_space.py:9-80).  Returns (basis, spans, range_index, cross_range_index,
+    out_of_plane_index): range is the axis along which the box centre lies furthest, cross range
+    the widest other axis (the middle one when range is the widest)."""
+    x = points[np.isfinite(points).all(axis=1)]
+    z = x - x.mean(axis=0, keepdims=True)
+    _, basis = np.linalg.eigh(z.T @ z)
+    if np.linalg.det(basis) < 0.0:
+        basis = -basis
+    y = (basis.T @ x.T).T
+    lo, hi = y.min(axis=0), y.max(axis=0)
+    spans = np.abs(hi - lo)
+    r = int(np.argmax(np.abs(0.5 * (lo + hi))))
+    cr = int(np.argmax(spans)) if spans[r] < spans.max() else int(np.argsort(spans)[1])
+    oop = [i for i in range(3) if i not in (r, cr)][0]
+    return basis, spans, r, cr, oop
+
+
+def scene_params_classic_sar(scene_centre_ecef: np.ndarray, aperture, tol: float = 1.0e-6):
+    """(rotation matrix with columns range / cross range / out of plane, Nyquist sample rates in
+    1/m per box axis, ground cosines) for a scene at ``scene_centre_ecef`` (utils/geodesy.py:124-172)."""
+    c = np.asarray(scene_centre_ecef, np.float64)
+    up = wgs84_up(c) if np.linalg.norm(c) > tol else np.array([0.0, 0.0, 1.0])
+    up = up / np.linalg.norm(up)
+    basis, spans, r, cr, oop = kspace_box(aperture.edge_k_vecs())
+    unit = lambda v: v / np.linalg.norm(v)
+    rng, crs, out = unit(basis.T[r]), unit(basis.T[cr]), unit(basis.T[oop])
+    if np.dot(out, up) < 0.0:
+        out, crs = -out, -crs
+    rot = np.stack([rng, crs, out], axis=0)
+    cosines = np.array([np.sqrt(1.0 - np.dot(rng, up) ** 2), np.sqrt(1.0 - np.dot(crs, up) ** 2),
+                        np.dot(out, up)]) / (2.0 * np.pi)
+    return rot.T, spans / (2.0 * np.pi), cosines
 
 
 class SimpleSarScene:
@@ -57,6 +113,18 @@ class GridSarScene:
         self._rotation_matrix = np.identity(3) if rotation_matrix is None else np.asarray(rotation_matrix, np.float64)
         self._grid_shape = [int(v) for v in grid_shape]
         self._grid_dimensions = [float(v) for v in grid_dimensions]
+
+    @staticmethod
+    def from_aperture(aperture, scene_centre_ecef: np.ndarray, grid_dimensions: Sequence[float],
+                      grid_shape: Optional[Sequence[int]] = None, safety_factor: float = 1.2) -> "GridSarScene":
+        """Grid aligned with the aperture's range / cross-range / out-of-plane axes at the scene
+        centre; without ``grid_shape`` the point counts follow the Nyquist sample rates of the
+        aperture's k-space support times ``safety_factor`` (numpy/hypothesis.py:236-267)."""
+        rot, rates, _ = scene_params_classic_sar(scene_centre_ecef, aperture)
+        if grid_shape is None:
+            grid_shape = np.rint(np.clip(np.asarray(grid_dimensions, np.float64) * rates * safety_factor, 1.0, None))
+            grid_shape = grid_shape.astype(int).tolist()
+        return GridSarScene(grid_shape, grid_dimensions, scene_centre_ecef, rot)
 
     @property
     def num_scatterers(self) -> int:
@@ -186,6 +254,18 @@ class NumpySimpleSarAperture:
     @property
     def c_eff(self) -> float:
         return self._c_eff
+
+    def edge_k_vecs(self, real_space_origin: Optional[np.ndarray] = None) -> np.ndarray:
+        """Band-edge k-vectors of every pulse at ``real_space_origin`` (each pulse's SRP when None):
+        bistatic direction (unit vector towards the receiver minus unit vector from the transmitter)
+        times the lowest, then the highest wavenumber, [2S, 3] (base/measurement.py:250-321)."""
+        o = self.stab_ref_posns if real_space_origin is None else np.asarray(real_space_origin)[None, :]
+        unit = lambda v: v / np.linalg.norm(v, axis=-1, keepdims=True)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            d = unit(self.receiver_positions - o) - unit(o - self.transmitter_positions)
+        k = 2.0 * np.pi / self.c_eff
+        return np.concatenate([d * k * (self.centre_frequency - 0.5 * self.sample_bandwidth),
+                               d * k * (self.centre_frequency + 0.5 * self.sample_bandwidth)], axis=0)
 
     @property
     def bad_slow_times(self) -> List[int]:

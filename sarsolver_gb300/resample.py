@@ -21,7 +21,7 @@ import torch
 from scipy.signal.windows import hann, tukey
 
 from . import _lib
-from .geometry import C, NumpySimpleSarAperture, NumpySimpleSarDataset
+from .geometry import C, NumpySimpleSarAperture, NumpySimpleSarDataset, kspace_box
 
 
 def _device_rows(ph, device) -> torch.Tensor:
@@ -106,32 +106,17 @@ def bad_slow_times(aperture) -> np.ndarray:
 
 
 def edge_k_vecs(aperture, origin) -> np.ndarray:
-    """k-space support at ``origin``: per pulse the bistatic direction (unit vector towards the
-    receiver minus unit vector from the transmitter) times the lowest and the highest wavenumber
-    of the band ([2S, 3]; base/measurement.py:250-321)."""
-    o = np.asarray(origin, np.float64)[None, :]
-    unit = lambda v: v / np.linalg.norm(v, axis=-1, keepdims=True)
-    with np.errstate(invalid="ignore", divide="ignore"):
-        d = unit(np.asarray(aperture.receiver_positions) - o) - unit(o - np.asarray(aperture.transmitter_positions))
-    k = 2.0 * np.pi / aperture.c_eff
-    return np.concatenate([d * k * (aperture.centre_frequency - 0.5 * aperture.sample_bandwidth),
-                           d * k * (aperture.centre_frequency + 0.5 * aperture.sample_bandwidth)], axis=0)
+    """k-space support of ``aperture`` at ``origin`` ([2S, 3]; base/measurement.py:250-321)."""
+    if hasattr(aperture, "edge_k_vecs"):
+        return aperture.edge_k_vecs(np.asarray(origin, np.float64))
+    return NumpySimpleSarAperture(aperture.transmitter_positions, aperture.receiver_positions,
+                                  aperture.stab_ref_posns, aperture.centre_frequency, aperture.sample_bandwidth,
+                                  num_freqs=aperture.num_freqs, c_eff=aperture.c_eff).edge_k_vecs(origin)
 
 
 def kspace_spans(points: np.ndarray):
-    """(range span, cross-range span) of the box around ``points`` aligned with their principal
-    axes (utils/k_space.py:9-80): range is the axis the box centre lies furthest along, cross range
-    the widest remaining axis (the middle one when range is the widest)."""
-    x = points[np.isfinite(points).all(axis=1)]
-    z = x - x.mean(axis=0, keepdims=True)
-    _, basis = np.linalg.eigh(z.T @ z)
-    if np.linalg.det(basis) < 0.0:
-        basis = -basis
-    y = x @ basis
-    lo, hi = y.min(axis=0), y.max(axis=0)
-    spans = np.abs(hi - lo)
-    r = int(np.argmax(np.abs(0.5 * (lo + hi))))
-    cr = int(np.argmax(spans)) if spans[r] < spans.max() else int(np.argsort(spans)[1])
+    """(range span, cross-range span) of the principal-axes box around ``points``."""
+    _, spans, r, cr, _ = kspace_box(points)
     return float(spans[r]), float(spans[cr])
 
 

@@ -169,3 +169,26 @@ def test_point_scheme_bins_match_fp64_rounding(rule, offset):
                            kappa, s_r)
         flips += int(np.sum(std_round(tb + offset) != bn[s]))
     assert flips == 0
+
+
+def test_grid_from_aperture_reproduces_the_reference_little_grid():
+    """GridSarScene.from_aperture on the reference's 'little' aperture (tests/conftest.py:46-73:
+    origin centre, 0 x 40 x 40 m, safety factor 3) gives the grid the reference built."""
+    import numpy as np
+    from cases import load_golden
+    from sarsolver_gb300.geometry import GridSarScene
+    case = load_golden("little")
+    scene = GridSarScene.from_aperture(case.aperture, np.zeros(3), np.array([0.0, 40.0, 40.0]), safety_factor=3.0)
+    assert list(scene.grid_shape) == case.data["grid_shape"].tolist()
+    np.testing.assert_allclose(scene.rotation_matrix, case.data["rotation_matrix"], atol=1e-12)
+    np.testing.assert_allclose(scene.positions, case.scene.positions, atol=1e-9)
+
+
+def test_wgs84_up_is_the_ellipsoid_normal():
+    import numpy as np
+    from sarsolver_gb300.geometry import WGS84_A, WGS84_F, wgs84_up
+    lat, lon, h = np.deg2rad(-17.7), np.deg2rad(168.3), 120.0
+    e2 = WGS84_F * (2 - WGS84_F)
+    n = WGS84_A / np.sqrt(1 - e2 * np.sin(lat) ** 2)
+    p = np.array([(n + h) * np.cos(lat) * np.cos(lon), (n + h) * np.cos(lat) * np.sin(lon), (n * (1 - e2) + h) * np.sin(lat)])
+    np.testing.assert_allclose(wgs84_up(p), [np.cos(lat) * np.cos(lon), np.cos(lat) * np.sin(lon), np.sin(lat)], atol=1e-12)
