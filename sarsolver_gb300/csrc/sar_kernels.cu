@@ -151,18 +151,20 @@ __device__ __forceinline__ PixelEval eval_pixel(const ColumnTerms& ct, float c9,
     return e;
 }
 
-// ------------------------------------------------------------------- K2 (grid)
+// ------------------------------------------------------------------- K2 (grid, wide windows)
+// Fallback for tiles whose range window is too wide to stage in shared memory: coefficient sets
+// per block of pulses in shared memory, profile pairs read straight from global memory (L2).
 size_t bp_grid_smem_bytes(int wwin, int pb, int staged) {
-    size_t f4 = (staged ? (size_t)pb * wwin : 0) + (size_t)pb * 4 * kSetF4 + (size_t)((pb + 3) / 4) + 6;
-    return f4 * sizeof(float4);
+    (void)wwin;
+    (void)staged;
+    return ((size_t)pb * 4 * kSetF4 + (size_t)((pb + 3) / 4) + 6) * sizeof(float4);
 }
 
-template <bool STAGED, bool PRECISE>
+template <bool PRECISE>
 __global__ void __launch_bounds__(kThreads, 2) bp_grid_kernel(const BpGridArgs a) {
     extern __shared__ float4 smem[];
     const int pb = a.pb;
-    float4* win = smem;
-    float4* coef = smem + (STAGED ? pb * a.wwin : 0);
+    float4* coef = smem;
     int* base = reinterpret_cast<int*>(coef + pb * 4 * kSetF4);
     df3* anchors = reinterpret_cast<df3*>(base + ((pb + 3) & ~3));
 
@@ -176,43 +178,22 @@ __global__ void __launch_bounds__(kThreads, 2) bp_grid_kernel(const BpGridArgs a
     if (threadIdx.x < 4) anchors[threadIdx.x] = subtile_anchor(ti, tj, k, threadIdx.x, g);
 
     float acc_re[4] = {0.f, 0.f, 0.f, 0.f}, acc_im[4] = {0.f, 0.f, 0.f, 0.f};
-    const int half_w = a.wwin / 2;
     for (int s0 = 0; s0 < a.S; s0 += pb) {
         const int npb = min(pb, a.S - s0);
         __syncthreads();
         coeff_stage(g, a.pulses, s0, npb, pb, anchors, coef, base);
         __syncthreads();
-        if (STAGED) {
-            for (int e = threadIdx.x; e < npb * a.wwin; e += kThreads) {
-                const int pi = e / a.wwin;
-                const int w = e - pi * a.wwin;
-                long gi = (long)base[pi] - half_w - a.bg0 + w;
-                if (gi < 0 || gi >= a.Lg) {
-                    raise_flag(a.flags, FLAG_TILE_WINDOW);
-                    gi = gi < 0 ? 0 : a.Lg - 1;
-                }
-                win[e] = __ldg(a.pairs + (size_t)(s0 + pi) * a.Lg + gi);
-            }
-            __syncthreads();
-        }
         float st_re[4] = {0.f, 0.f, 0.f, 0.f}, st_im[4] = {0.f, 0.f, 0.f, 0.f};
         for (int pi = 0; pi < npb; ++pi) {
             float c9, w9, ib;
             const ColumnTerms ct = load_column<PRECISE>(coef + (pi * 4 + tt.q) * kSetF4, tt, c9, w9, ib);
-            const float4* wp = win + pi * a.wwin;
             const float4* gp = a.pairs + (size_t)(s0 + pi) * a.Lg;
             const int bb = base[pi] - a.bg0;
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
                 const PixelEval e = eval_pixel<PRECISE>(ct, c9, w9, ib, tt, r);
-                float4 pv;
-                if (STAGED) {
-                    const unsigned idx = min((unsigned)(e.n + half_w), (unsigned)(a.wwin - 1));
-                    pv = wp[idx];
-                } else {
-                    const int gi = min(max(bb + e.n, 0), a.Lg - 1);
-                    pv = __ldg(gp + gi);
-                }
+                const int gi = min(max(bb + e.n, 0), a.Lg - 1);
+                const float4 pv = __ldg(gp + gi);
                 const float re = fmaf(e.sf, pv.z, pv.x);
                 const float im = fmaf(e.sf, pv.w, pv.y);
                 float sn, cn;
@@ -245,20 +226,18 @@ __global__ void __launch_bounds__(kThreads, 2) bp_grid_kernel(const BpGridArgs a
     }
 }
 
-template <bool STAGED, bool PRECISE>
+template <bool PRECISE>
 static cudaError_t launch_bp_grid_t(const BpGridArgs& a, cudaStream_t st) {
-    const size_t smem = bp_grid_smem_bytes(a.wwin, a.pb, a.staged);
+    const size_t smem = bp_grid_smem_bytes(a.wwin, a.pb, 0);
     const unsigned blocks = (unsigned)(a.g.tiles_x * a.g.tiles_y * a.g.nz);
-    cudaError_t e = cudaFuncSetAttribute(bp_grid_kernel<STAGED, PRECISE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(bp_grid_kernel<PRECISE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    bp_grid_kernel<STAGED, PRECISE><<<blocks, kThreads, smem, st>>>(a);
+    bp_grid_kernel<PRECISE><<<blocks, kThreads, smem, st>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st) {
-    if (a.staged) return a.g.precise_bins ? launch_bp_grid_t<true, true>(a, st) : launch_bp_grid_t<true, false>(a, st);
-    return a.g.precise_bins ? launch_bp_grid_t<false, true>(a, st) : launch_bp_grid_t<false, false>(a, st);
+    return a.g.precise_bins ? launch_bp_grid_t<true>(a, st) : launch_bp_grid_t<false>(a, st);
 }
 
 // ------------------------------------------- K2 (grid, warp-specialised pipeline)
@@ -512,116 +491,6 @@ cudaError_t launch_bp_grid_ws(const BpGridArgs& a, cudaStream_t st) {
         bp_grid_ws_kernel<false><<<blocks, kWsThreads, smem, st>>>(a);
     }
     return cudaGetLastError();
-}
-
-// ------------------------------------------------------------------- K3 (grid)
-// CTA = (strip segment of tiles along y, block of pbf pulses).  Contributions of the
-// segment's tiles are accumulated in a shared-memory window per pulse that covers the
-// segment's whole range extent, then merged into the global profile accumulator with one
-// atomic add per bin.  Each pixel uses the identical coefficient sets, bin and weights as
-// K2, so the pair is an exact transpose up to FP32 summation order.
-size_t fp_grid_smem_bytes(int ws, int pbf) {
-    size_t f4 = (size_t)pbf * ws / 2 + (size_t)pbf * 4 * kSetF4 + (size_t)((2 * pbf + 3) / 4) + 6;
-    return f4 * sizeof(float4);
-}
-
-template <bool LINEAR, bool PRECISE>
-__global__ void __launch_bounds__(kThreads, 2) fp_grid_kernel(const FpGridArgs a) {
-    extern __shared__ float4 smem[];
-    const int pbf = a.pbf;
-    float2* win = reinterpret_cast<float2*>(smem);
-    float4* coef = smem + (pbf * a.ws) / 2;
-    int* base = reinterpret_cast<int*>(coef + pbf * 4 * kSetF4);
-    int* wst = base + pbf;
-    df3* anchors = reinterpret_cast<df3*>(base + ((2 * pbf + 3) & ~3));
-
-    const GridConst& g = a.g;
-    int b = blockIdx.x;
-    const int seg = b % a.segs_per_column;
-    b /= a.segs_per_column;
-    const int ti = b % g.tiles_x;
-    const int k = b / g.tiles_x;
-    const int strip = (k * g.tiles_x + ti) * a.segs_per_column + seg;
-    const int s0 = blockIdx.y * pbf;
-    const int npb = min(pbf, a.S - s0);
-    const int tj0 = seg * a.seg_tiles;
-    const int tj1 = min(tj0 + a.seg_tiles, g.tiles_y);
-    const TileThread tt = tile_thread();
-
-    for (int e = threadIdx.x; e < pbf * a.ws; e += kThreads) win[e] = make_float2(0.f, 0.f);
-    if (threadIdx.x < npb) wst[threadIdx.x] = a.strip_start[(size_t)strip * a.S + s0 + threadIdx.x];
-    const int i = ti * kTile + (threadIdx.x & 31);
-
-    for (int tj = tj0; tj < tj1; ++tj) {
-        __syncthreads();
-        if (threadIdx.x < 4) anchors[threadIdx.x] = subtile_anchor(ti, tj, k, threadIdx.x, g);
-        float2 xv[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            const int j = tj * kTile + 4 * (threadIdx.x >> 5) + r;
-            xv[r] = (i < g.nx && j < g.ny) ? a.x[((size_t)k * g.ny + j) * g.nx + i] : make_float2(0.f, 0.f);
-        }
-        __syncthreads();
-        coeff_stage(g, a.pulses, s0, npb, pbf, anchors, coef, base);
-        __syncthreads();
-        for (int pi = 0; pi < npb; ++pi) {
-            float c9, w9, ib;
-            const ColumnTerms ct = load_column<PRECISE>(coef + (pi * 4 + tt.q) * kSetF4, tt, c9, w9, ib);
-            float2* wp = win + pi * a.ws;
-            const int off = base[pi] - wst[pi];
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                const PixelEval e = eval_pixel<PRECISE>(ct, c9, w9, ib, tt, r);
-                float sn, cn;
-                __sincosf(SAR_TWO_PI * e.f, &sn, &cn);
-                // contribution x * exp(+2 pi i f)
-                const float cr = xv[r].x * cn - xv[r].y * sn;
-                const float ci = fmaf(xv[r].x, sn, xv[r].y * cn);
-                const unsigned idx = min((unsigned)(e.n + off), (unsigned)(a.ws - 2));
-                if (LINEAR) {
-                    const float w0 = 0.5f - e.sf, w1 = 0.5f + e.sf;
-                    atomicAdd(&wp[idx].x, w0 * cr);
-                    atomicAdd(&wp[idx].y, w0 * ci);
-                    atomicAdd(&wp[idx + 1].x, w1 * cr);
-                    atomicAdd(&wp[idx + 1].y, w1 * ci);
-                } else {
-                    atomicAdd(&wp[idx].x, cr);
-                    atomicAdd(&wp[idx].y, ci);
-                }
-            }
-        }
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < npb * a.ws; e += kThreads) {
-        const int pi = e / a.ws;
-        const int w = e - pi * a.ws;
-        const float2 v = win[e];
-        if (v.x == 0.f && v.y == 0.f) continue;
-        const long gi = (long)wst[pi] + w - a.bg0;
-        if (gi < 0 || gi >= a.Lg) {
-            raise_flag(a.flags, FLAG_STRIP_WINDOW);
-            continue;
-        }
-        float2* dst = a.acc + (size_t)(s0 + pi) * a.Lg + gi;
-        atomicAdd(&dst->x, v.x);
-        atomicAdd(&dst->y, v.y);
-    }
-}
-
-template <bool LINEAR, bool PRECISE>
-static cudaError_t launch_fp_grid_t(const FpGridArgs& a, cudaStream_t st) {
-    const size_t smem = fp_grid_smem_bytes(a.ws, a.pbf);
-    const dim3 grid((unsigned)(a.segs_per_column * a.g.tiles_x * a.g.nz), (unsigned)((a.S + a.pbf - 1) / a.pbf));
-    cudaError_t e = cudaFuncSetAttribute(fp_grid_kernel<LINEAR, PRECISE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    fp_grid_kernel<LINEAR, PRECISE><<<grid, kThreads, smem, st>>>(a);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_fp_grid(const FpGridArgs& a, cudaStream_t st) {
-    if (a.linear) return a.g.precise_bins ? launch_fp_grid_t<true, true>(a, st) : launch_fp_grid_t<true, false>(a, st);
-    return a.g.precise_bins ? launch_fp_grid_t<false, true>(a, st) : launch_fp_grid_t<false, false>(a, st);
 }
 
 // ------------------------------------------- K3 (grid, warp-specialised pipeline)

@@ -56,8 +56,6 @@ struct FpGridArgs {
     int pbf;                   // pulses per CTA (multiple of 8, <= 32)
     int linear;                // 1: linear interpolation weights; 0: nearest bin
 };
-size_t fp_grid_smem_bytes(int ws, int pbf);
-cudaError_t launch_fp_grid(const FpGridArgs& a, cudaStream_t st);
 // Warp-specialised variant: producer warps stage image tiles and coefficient sets; each
 // gathering warp owns whole pulses, so its windows need no atomics when bins along a row of
 // the tile are provably distinct (pbf <= 32, multiple of 8).
