@@ -234,7 +234,7 @@ def run_ours(args):
                     "stages_ms": {"accumulator_clear": fstage[0] / max(fcalls, 1),
                                   "scatter_kernel": fstage[1] / max(fcalls, 1),
                                   "downsample_fft_side": fstage[2] / max(fcalls, 1)},
-                    "note": "y = A x on the same workload (fp_grid_kernel + FFT downsampling), not the headline"},
+                    "note": "y = A x on the same workload (fp_grid_ws_kernel + FFT downsampling), not the headline"},
         "roofline": {"bound": "sfu", "kernel": "bp_grid_ws_kernel", "achieved": achieved, "peak": r_roof,
                      "unit": "px*pulse/s", "frac": achieved / r_roof, "traffic": traffic,
                      "peak_basis": f"{props.multi_processor_count} SMs x {sm_max:.0f} MHz x 16 MUFU/clk/SM / "
