@@ -94,3 +94,28 @@ def test_null_arguments_and_status_strings():
     assert lib.sar_plan_destroy(None) == 0
     assert lib.sar_status_string(0) == b"ok"
     assert lib.sar_status_string(4) == b"out of device memory"
+
+
+def test_new_entry_points_validate_arguments_without_gpu():
+    lib = _lib.load()
+    null = ctypes.c_void_p(0)
+    res = _lib.SarCglsResult()
+    assert lib.sar_cgls_ex(null, null, null, 0, null, 10, 1e-3, null, ctypes.byref(res), null) == _lib.SAR_ERR_INVALID_ARGUMENT
+    assert "null" in _lib.last_error()
+    assert lib.sar_phase_gradient(null, null, null, 4, 4, 4.0, null) == _lib.SAR_ERR_INVALID_ARGUMENT
+    assert lib.sar_sharpness(null, null, null, 4, null) == _lib.SAR_ERR_INVALID_ARGUMENT
+    h = ctypes.c_void_p()
+    assert lib.sar_unet_create(48, 0, ctypes.byref(h)) == _lib.SAR_ERR_NOT_SUPPORTED
+    assert "base_channels" in _lib.last_error()
+    win = np.ones(8)
+    dummy = ctypes.c_void_p(16)   # never dereferenced: the size check fails first
+    assert lib.sar_fast_freq_downsample(dummy, dummy, 4, 4, 9, win.ctypes.data_as(ctypes.c_void_p), null) == \
+        _lib.SAR_ERR_INVALID_ARGUMENT
+    assert "new_N" in _lib.last_error()
+    rows = np.array([0, 3], dtype=np.int32)
+    kern = np.zeros((4, 2))
+    assert lib.sar_resample_phase_history(dummy, 6, 4, null, 1e9, 1e8, 1.0, 3e8, 4, win.ctypes.data_as(ctypes.c_void_p),
+                                          kern.ctypes.data_as(ctypes.c_void_p), 4, rows.ctypes.data_as(ctypes.c_void_p),
+                                          2, dummy, null) == _lib.SAR_ERR_INVALID_ARGUMENT
+    assert "window" in _lib.last_error()
+    assert lib.sar_adjoint_pulse_block(null, null, 0, 1, null, 0, null) == _lib.SAR_ERR_INVALID_ARGUMENT
