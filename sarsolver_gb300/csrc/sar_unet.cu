@@ -197,8 +197,18 @@ int conv_forward(Src s0, Src s1, int images, int H, int W, int taps, const bf16*
     a.out_f32 = out_f32;
     a.f32_keep = f32_keep;
     a.flags = flags;
-    const size_t smem = 1024 + (size_t)a.stages * stage + (2 * a.stages + 2) * 8 + 16;
-    dim3 grid((unsigned)(images * a.tiles_x * a.tiles_y), (unsigned)(Nout / BN));
+    size_t smem = 1024 + (size_t)a.stages * stage + (2 * a.stages + 4) * 8 + 16;
+    // Persistent grid: as many CTAs as fit on the SMs, by shared memory and by TMEM (two
+    // accumulators each).  When TMEM is the tighter limit the shared-memory request is raised so
+    // that no more CTAs than that share an SM (a CTA beyond it would wait in tcgen05.alloc).
+    a.images = images;
+    const int items = images * a.tiles_x * a.tiles_y * (Nout / BN);
+    const size_t sm_smem = 227u * 1024u;
+    const int by_smem = std::max(1, (int)(sm_smem / smem));
+    const int by_tmem = std::max(1, (int)(512u / (2u * tmem_cols(BN))));
+    const int per_sm = std::max(1, std::min(by_smem, by_tmem));
+    if (by_tmem < by_smem) smem = std::max(smem, sm_smem / (size_t)(per_sm + 1) + 1024);
+    dim3 grid((unsigned)std::min(items, device_sms() * per_sm));
     if (bk64) {
         U_CUDA(cudaFuncSetAttribute(conv_fwd_kernel<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem), "smem attr");
         conv_fwd_kernel<64><<<grid, kThreads, smem, st>>>(maps, a);

@@ -46,6 +46,9 @@ __device__ __forceinline__ void bar_init(uint64_t* b, uint32_t n) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(n) : "memory");
 }
 __device__ __forceinline__ void bar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void bar_try_arrive(uint64_t* b) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(su32(b)) : "memory");
+}
 __device__ __forceinline__ void bar_expect_tx(uint64_t* b, uint32_t bytes) {
     asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(su32(b)),
                  "r"(bytes)
@@ -158,7 +161,7 @@ struct ConvMaps {
 };
 
 struct ConvArgs {
-    int nsrc, C0, C1, Ctot, taps;
+    int nsrc, C0, C1, Ctot, taps, images;
     int W, H, BW, BH, tiles_x, tiles_y;
     int BN, Nout, stages;
     const float* bias;                 // [Nout] or null
@@ -172,6 +175,67 @@ struct ConvArgs {
     unsigned* flags;
 };
 
+// Epilogue of one output tile: 32 columns at a time from this warp's TMEM lanes.
+template <int BK>
+__device__ __forceinline__ void conv_epilogue(const ConvArgs& a, uint32_t tacc, int q, int lane, int img, int x0,
+                                              int y0, int n0) {
+    const int row = 32 * q + lane;
+    const int px = x0 + row % a.BW, py = y0 + row / a.BW;
+    const size_t pix = ((size_t)img * a.H + py) * a.W + px;
+    for (int c0 = 0; c0 < a.BN; c0 += 32) {
+        float v[32];
+        tmem_ld32(tacc + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
+        const int n = n0 + c0;
+        if (a.bias) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) v[i] += __ldg(a.bias + n + i);
+        }
+        if (a.relu) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i], 0.f);
+        }
+        if (a.out_f32) {
+#pragma unroll
+            for (int i = 0; i < 32; ++i)
+                if (n + i < a.f32_keep) a.out_f32[pix * a.f32_keep + n + i] = v[i];
+            continue;
+        }
+        const int d = n >= a.outc[0] ? 1 : 0;
+        const int ch = d ? n - a.outc[0] : n;
+        __nv_bfloat16* dst = a.out[d] + pix * a.outc[d] + ch;
+        if (a.mask[d]) {
+            const uint4* m4 = reinterpret_cast<const uint4*>(a.mask[d] + pix * a.outc[d] + ch);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const uint4 mm = m4[j];
+                const __nv_bfloat16* mb = reinterpret_cast<const __nv_bfloat16*>(&mm);
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    if (!(__bfloat162float(mb[i]) > 0.f)) v[8 * j + i] = 0.f;
+            }
+        }
+        uint4* d4 = reinterpret_cast<uint4*>(dst);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (a.accumulate[d]) {
+                const uint4 old = d4[j];
+                const __nv_bfloat16* ob = reinterpret_cast<const __nv_bfloat16*>(&old);
+#pragma unroll
+                for (int i = 0; i < 8; ++i) v[8 * j + i] += __bfloat162float(ob[i]);
+            }
+            uint4 pk;
+            __nv_bfloat162* pb = reinterpret_cast<__nv_bfloat162*>(&pk);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) pb[i] = __floats2bfloat162_rn(v[8 * j + 2 * i], v[8 * j + 2 * i + 1]);
+            d4[j] = pk;
+        }
+    }
+}
+
+// Persistent: CTA c handles work items c, c + gridDim.x, ... (item = M tile x N tile).  The TMA
+// ring runs on across items, and two TMEM accumulators alternate so that the epilogue of one
+// item overlaps the MMAs of the next ("tfull[b]" committed by the MMA lane when accumulator b
+// holds a finished item, "tempty[b]" arrived at by the four epilogue warps once they have read it).
 template <int BK>
 __global__ void __launch_bounds__(kThreads, 1) conv_fwd_kernel(const __grid_constant__ ConvMaps maps, const ConvArgs a) {
     extern __shared__ uint8_t smem_raw[];
@@ -179,15 +243,15 @@ __global__ void __launch_bounds__(kThreads, 1) conv_fwd_kernel(const __grid_cons
     const int a_bytes = 128 * BK * 2, b_bytes = a.BN * BK * 2, stage_bytes = a_bytes + b_bytes;
     uint64_t* full = (uint64_t*)(smem + a.stages * stage_bytes);
     uint64_t* empty = full + a.stages;
-    uint64_t* done = empty + a.stages;
-    uint32_t* tslot = (uint32_t*)(done + 1);
+    uint64_t* tfull = empty + a.stages;   // [2]
+    uint64_t* tempty = tfull + 2;         // [2]
+    uint32_t* tslot = (uint32_t*)(tempty + 2);
     __shared__ int timed_out;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int per_img = a.tiles_x * a.tiles_y;
-    const int img = blockIdx.x / per_img, rem = blockIdx.x % per_img;
-    const int x0 = (rem % a.tiles_x) * a.BW, y0 = (rem / a.tiles_x) * a.BH;
-    const int n0 = blockIdx.y * a.BN;
+    const int ntn = a.Nout / a.BN;
+    const int items = a.images * per_img * ntn;
     const uint32_t ncols = tmem_cols(a.BN);
 
     if (threadIdx.x == 0) {
@@ -195,12 +259,15 @@ __global__ void __launch_bounds__(kThreads, 1) conv_fwd_kernel(const __grid_cons
             bar_init(&full[s], 1);
             bar_init(&empty[s], 1);
         }
-        bar_init(done, 1);
+        for (int b = 0; b < 2; ++b) {
+            bar_init(&tfull[b], 1);
+            bar_init(&tempty[b], 4);
+        }
         bar_fence_init();
         timed_out = 0;
     }
     if (warp == 1) {
-        tmem_alloc(tslot, ncols);
+        tmem_alloc(tslot, 2 * ncols);
         tmem_relinquish();
     }
     __syncthreads();
@@ -212,109 +279,92 @@ __global__ void __launch_bounds__(kThreads, 1) conv_fwd_kernel(const __grid_cons
         tma_prefetch(&maps.src[0]);
         if (a.nsrc > 1) tma_prefetch(&maps.src[1]);
         tma_prefetch(&maps.wts);
-        int issued = 0;
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % a.stages, round = kb / a.stages;
-            if (kb >= a.stages && !bar_wait(&empty[s], (round - 1) & 1, 256)) {
-                atomicOr(a.flags, kFlagTimeout);
-                timed_out = 1;
-                break;
+        long long g = 0;
+        bool stop = false;
+        for (int it = blockIdx.x; it < items && !stop; it += gridDim.x) {
+            const int mt = it / ntn, n0 = (it % ntn) * a.BN;
+            const int img = mt / per_img, rem = mt % per_img;
+            const int x0 = (rem % a.tiles_x) * a.BW, y0 = (rem / a.tiles_x) * a.BH;
+            for (int kb = 0; kb < nkb; ++kb, ++g) {
+                const int s = (int)(g % a.stages);
+                const long long round = g / a.stages;
+                if (g >= a.stages && !bar_wait(&empty[s], (uint32_t)((round - 1) & 1), 256)) {
+                    atomicOr(a.flags, kFlagTimeout);
+                    timed_out = 1;
+                    stop = true;
+                    break;
+                }
+                const int tap = kb / kpt, c = (kb % kpt) * BK;
+                const int src = c >= a.C0 ? 1 : 0, cs = src ? c - a.C0 : c;
+                const int dy = a.taps == 9 ? tap / 3 - 1 : 0, dx = a.taps == 9 ? tap % 3 - 1 : 0;
+                uint8_t* st = smem + s * stage_bytes;
+                bar_expect_tx(&full[s], (uint32_t)stage_bytes);
+                tma_4d(st, &maps.src[src], cs, x0 + dx, y0 + dy, img, &full[s]);
+                tma_2d(st + a_bytes, &maps.wts, tap * a.Ctot + c, n0, &full[s]);
             }
-            const int tap = kb / kpt, c = (kb % kpt) * BK;
-            const int src = c >= a.C0 ? 1 : 0, cs = src ? c - a.C0 : c;
-            const int dy = a.taps == 9 ? tap / 3 - 1 : 0, dx = a.taps == 9 ? tap % 3 - 1 : 0;
-            uint8_t* st = smem + s * stage_bytes;
-            bar_expect_tx(&full[s], (uint32_t)stage_bytes);
-            tma_4d(st, &maps.src[src], cs, x0 + dx, y0 + dy, img, &full[s]);
-            tma_2d(st + a_bytes, &maps.wts, tap * a.Ctot + c, n0, &full[s]);
-            ++issued;
         }
         // Drain: every issued load has landed before the CTA may exit.
-        for (int kb = max(0, issued - a.stages); kb < issued; ++kb)
-            if (!bar_wait(&full[kb % a.stages], (kb / a.stages) & 1, 256)) atomicOr(a.flags, kFlagTimeout);
+        for (long long k = (g > a.stages ? g - a.stages : 0); k < g; ++k)
+            if (!bar_wait(&full[k % a.stages], (uint32_t)((k / a.stages) & 1), 256)) atomicOr(a.flags, kFlagTimeout);
     } else if (warp == 1 && lane == 0) {
         const uint32_t idesc = idesc_bf16(128, a.BN, false, false);
         const uint32_t lay = swizzle_layout(BK * 2), sbo = 8 * BK * 2;
-        for (int kb = 0; kb < nkb; ++kb) {
-            const int s = kb % a.stages, round = kb / a.stages;
-            if (!bar_wait(&full[s], round & 1, 64)) {
+        long long g = 0;
+        int i = 0;
+        bool stop = false;
+        for (int it = blockIdx.x; it < items && !stop; it += gridDim.x, ++i) {
+            const int b = i & 1;
+            if (i >= 2 && !bar_wait(&tempty[b], (uint32_t)(((i >> 1) - 1) & 1), 256)) {
                 atomicOr(a.flags, kFlagTimeout);
                 timed_out = 1;
                 break;
             }
             tc_after();
-            const uint32_t sa = su32(smem + s * stage_bytes), sb = sa + a_bytes;
-#pragma unroll
-            for (int k = 0; k < BK / 16; ++k)
-                mma_bf16(tmem, smem_desc(sa + 32 * k, 16, sbo, lay), smem_desc(sb + 32 * k, 16, sbo, lay), idesc,
-                         (kb | k) != 0);
-            mma_commit(&empty[s]);
-        }
-        mma_commit(done);
-    } else if (warp >= 2) {
-        // tcgen05.ld is warp-collective: decide for the whole warp.
-        const bool ok = __all_sync(0xffffffffu, bar_wait(done, 0, 1024));
-        const bool go = ok && __shfl_sync(0xffffffffu, timed_out, 0) == 0;
-        tc_after();
-        if (!ok) {
-            if (lane == 0) atomicOr(a.flags, kFlagTimeout);
-        } else if (go) {
-            const int q = warp & 3, row = 32 * q + lane;
-            const int px = x0 + row % a.BW, py = y0 + row / a.BW;
-            const size_t pix = ((size_t)img * a.H + py) * a.W + px;
-            for (int c0 = 0; c0 < a.BN; c0 += 32) {
-                float v[32];
-                tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)c0, v);
-                const int n = n0 + c0;
-                if (a.bias) {
-#pragma unroll
-                    for (int i = 0; i < 32; ++i) v[i] += __ldg(a.bias + n + i);
+            const uint32_t tacc = tmem + (uint32_t)(b * ncols);
+            for (int kb = 0; kb < nkb; ++kb, ++g) {
+                const int s = (int)(g % a.stages);
+                if (!bar_wait(&full[s], (uint32_t)((g / a.stages) & 1), 64)) {
+                    atomicOr(a.flags, kFlagTimeout);
+                    timed_out = 1;
+                    stop = true;
+                    break;
                 }
-                if (a.relu) {
+                tc_after();
+                const uint32_t sa = su32(smem + s * stage_bytes), sb = sa + a_bytes;
 #pragma unroll
-                    for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i], 0.f);
-                }
-                if (a.out_f32) {
-                    for (int i = 0; i < 32 && n + i < a.f32_keep; ++i) a.out_f32[pix * a.f32_keep + n + i] = v[i];
-                    continue;
-                }
-                const int d = n >= a.outc[0] ? 1 : 0;
-                const int ch = d ? n - a.outc[0] : n;
-                __nv_bfloat16* dst = a.out[d] + pix * a.outc[d] + ch;
-                if (a.mask[d]) {
-                    const uint4* m4 = reinterpret_cast<const uint4*>(a.mask[d] + pix * a.outc[d] + ch);
-#pragma unroll
-                    for (int j = 0; j < 4; ++j) {
-                        const uint4 mm = m4[j];
-                        const __nv_bfloat16* mb = reinterpret_cast<const __nv_bfloat16*>(&mm);
-#pragma unroll
-                        for (int i = 0; i < 8; ++i)
-                            if (!(__bfloat162float(mb[i]) > 0.f)) v[8 * j + i] = 0.f;
-                    }
-                }
-                uint4* d4 = reinterpret_cast<uint4*>(dst);
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    if (a.accumulate[d]) {
-                        const uint4 old = d4[j];
-                        const __nv_bfloat16* ob = reinterpret_cast<const __nv_bfloat16*>(&old);
-#pragma unroll
-                        for (int i = 0; i < 8; ++i) v[8 * j + i] += __bfloat162float(ob[i]);
-                    }
-                    uint4 pk;
-                    __nv_bfloat162* pb = reinterpret_cast<__nv_bfloat162*>(&pk);
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) pb[i] = __floats2bfloat162_rn(v[8 * j + 2 * i], v[8 * j + 2 * i + 1]);
-                    d4[j] = pk;
-                }
+                for (int k = 0; k < BK / 16; ++k)
+                    mma_bf16(tacc, smem_desc(sa + 32 * k, 16, sbo, lay), smem_desc(sb + 32 * k, 16, sbo, lay), idesc,
+                             (kb | k) != 0);
+                mma_commit(&empty[s]);
             }
+            mma_commit(&tfull[b]);   // also on the timeout path, so the epilogue warps are released
         }
-        tc_before();
+    } else if (warp >= 2) {
+        const int q = warp & 3;
+        int i = 0;
+        for (int it = blockIdx.x; it < items; it += gridDim.x, ++i) {
+            const int b = i & 1;
+            const bool ok = __all_sync(0xffffffffu, bar_wait(&tfull[b], (uint32_t)((i >> 1) & 1), 1024));
+            tc_after();
+            if (!ok) {
+                if (lane == 0) atomicOr(a.flags, kFlagTimeout);
+                break;
+            }
+            if (__shfl_sync(0xffffffffu, timed_out, 0) == 0) {
+                const int mt = it / ntn, n0 = (it % ntn) * a.BN;
+                const int img = mt / per_img, rem = mt % per_img;
+                conv_epilogue<BK>(a, tmem + (uint32_t)(b * ncols), q, lane, img, (rem % a.tiles_x) * a.BW,
+                                  (rem / a.tiles_x) * a.BH, n0);
+            }
+            tc_before();
+            __syncwarp();
+            if (lane == 0) bar_try_arrive(&tempty[b]);
+        }
     }
     __syncthreads();
     if (warp == 1) {
         tc_after();
-        tmem_dealloc(tmem, ncols);
+        tmem_dealloc(tmem, 2 * ncols);
     }
 }
 
