@@ -255,6 +255,21 @@ int sar_resample_phase_history(const void *ph_dev, size_t S, size_t N, const dou
                                size_t new_N, const double *window, const double *kernel, size_t kernel_length,
                                const int *row0, size_t num_rows, void *out_dev, void *stream);
 
+/* ------------------------------------------------ 5. CPHD signal arrays (before the operator)
+ * sar_cphd_decode: widen one CPHD signal array, copied to the device as it lies in the file
+ * (big-endian interleaved I/Q, [num_vectors][num_samples]), to complex64:
+ *   out[v][s] = complex(I, Q) * amp_sf[v]     (amp_sf_dev: device float [num_vectors], or NULL)
+ * format: SAR_CPHD_CI2 (signed 8-bit pairs), SAR_CPHD_CI4 (signed 16-bit pairs), SAR_CPHD_CF8
+ * (binary32 pairs) -- CPHD 1.0.1 Data/SignalArrayFormat, CPHD 0.3 Data/SampleType.  Asynchronous
+ * on `stream`; any alignment (16-byte aligned buffers take the vector path).  Replaces the signal
+ * read of the reference's CPHD datasets through sarpy (src/sarsolver/io/cphd101.py:251-265,
+ * io/cphd03.py:250-263), which decodes on the host. */
+#define SAR_CPHD_CI2 1
+#define SAR_CPHD_CI4 2
+#define SAR_CPHD_CF8 3
+int sar_cphd_decode(const void *raw_dev, int format, size_t num_vectors, size_t num_samples,
+                    const float *amp_sf_dev, void *out_dev, void *stream);
+
 /* Stage timing.  While enabled, every sar_forward / sar_adjoint call records CUDA events on
  * its stream around its stages: [0] range-profile FFT side before the main kernel (adjoint:
  * pack + inverse FFT + unpack; forward: accumulator clear), [1] the main gather / scatter

@@ -30,13 +30,14 @@ EXPORTED = (
     "sar_device_flags", "sar_last_error", "sar_status_string",
     "sar_enable_stage_timing", "sar_stage_times",
     "sar_adjoint_from_profiles_noalloc", "sar_phase_gradient", "sar_sharpness", "sar_cgls", "sar_cgls_ex", "sar_adjoint_pulse_block",
-    "sar_move_srps", "sar_fast_freq_downsample", "sar_resample_phase_history",
+    "sar_move_srps", "sar_fast_freq_downsample", "sar_resample_phase_history", "sar_cphd_decode",
     "sar_unet_create", "sar_unet_destroy", "sar_unet_info", "sar_unet_set_params", "sar_unet_get_params",
     "sar_unet_get_grads", "sar_unet_zero_grad", "sar_unet_forward", "sar_unet_backward", "sar_unet_adam_step",
     "sar_unet_flags", "sar_conv2d_forward_bf16", "sar_conv2d_wgrad_bf16",
 )
 
 SAR_UNET_LAYERS = 15
+SAR_CPHD_CI2, SAR_CPHD_CI4, SAR_CPHD_CF8 = 1, 2, 3
 
 
 class SarGeometry(ctypes.Structure):
@@ -138,6 +139,8 @@ def load() -> ctypes.CDLL:
                                                c_double, c_size_t, c_void_p, c_void_p, c_size_t, c_void_p, c_size_t,
                                                c_void_p, c_void_p]
     lib.sar_resample_phase_history.restype = c_int
+    lib.sar_cphd_decode.argtypes = [c_void_p, c_int, c_size_t, c_size_t, c_void_p, c_void_p, c_void_p]
+    lib.sar_cphd_decode.restype = c_int
     P = c_void_p
     unet_sigs = {
         "sar_unet_create": [c_int, c_int, P],

@@ -300,8 +300,57 @@ class NumpySimpleSarDataset:
     def aperture(self):
         return self._aperture
 
-    def phase_history(self, item: slice = slice(None)) -> np.ndarray:
-        return self._phase_history[item, :]
+    def phase_history(self, item: slice = slice(None)) -> Optional[np.ndarray]:
+        return None if self._phase_history is None else self._phase_history[item, :]
 
     def get_subset(self, item: slice = None) -> "NumpySimpleSarDataset":
-        return NumpySimpleSarDataset(self.aperture.get_subset(item), self._phase_history[item, :])
+        return NumpySimpleSarDataset(self.aperture.get_subset(item), self.phase_history(item))
+
+    @staticmethod
+    def from_scratch(trans_posns: np.ndarray, rec_posns: np.ndarray, srps: np.ndarray, centre_freq: float,
+                     sample_freq: float, phase_history: Optional[np.ndarray] = None,
+                     waveform_fft: Optional[np.ndarray] = None, slow_time_weighting: Optional[np.ndarray] = None,
+                     num_freqs: Optional[int] = None, sign_multiplier: float = 1.0,
+                     c_eff: float = C) -> "NumpySimpleSarDataset":
+        """Aperture and dataset from the aperture's arguments (numpy/measurement.py:258-304)."""
+        ap = NumpySimpleSarAperture(trans_posns, rec_posns, srps, centre_freq, sample_freq, waveform_fft=waveform_fft,
+                                    slow_time_weighting=slow_time_weighting, num_freqs=num_freqs,
+                                    sign_multiplier=sign_multiplier, c_eff=c_eff)
+        return NumpySimpleSarDataset(ap, phase_history)
+
+    @staticmethod
+    def from_resampling(original_dataset, range_amb: Optional[float] = None, cross_range_amb: Optional[float] = None,
+                        fast_downsample_factor: float = 1.0, slow_downsample_factor: int = 1,
+                        new_srp: Optional[np.ndarray] = None, safety_factor: float = 1.2,
+                        num_threads: Optional[int] = None, device=None,
+                        keep_on_device: bool = False) -> "NumpySimpleSarDataset":
+        """Resampled dataset (numpy/measurement.py:342-458), computed on the GPU by
+        ``resample.resample_dataset``; ``num_threads`` is accepted for the reference's signature and
+        unused (there is no host worker pool).  A dataset that can hand over its phase history on
+        the device (``phase_history_device``, e.g. a CPHD file) is read straight to the device."""
+        from .resample import resample_dataset
+        return resample_dataset(original_dataset, fast_downsample_factor, slow_downsample_factor, new_srp=new_srp,
+                                safety_factor=safety_factor, device=device, keep_on_device=keep_on_device,
+                                range_amb=range_amb, cross_range_amb=cross_range_amb)
+
+    @staticmethod
+    def from_datasets(datasets: Sequence) -> "NumpySimpleSarDataset":
+        """Pulse-wise concatenation of datasets sharing the band (numpy/measurement.py:463-504)."""
+        import torch
+
+        aps = [d.aperture for d in datasets]
+        ap0 = aps[0]
+        cat = lambda name: np.concatenate([np.asarray(getattr(a, name)) for a in aps], axis=0)
+        parts = [d.phase_history(slice(None)) for d in datasets]
+        if all(p is None for p in parts):
+            ph = None
+        elif any(isinstance(p, torch.Tensor) for p in parts):
+            dev = next(p.device for p in parts if isinstance(p, torch.Tensor))
+            ph = torch.cat([p.to(dev) if isinstance(p, torch.Tensor) else torch.as_tensor(p, device=dev) for p in parts])
+        else:
+            ph = np.concatenate(parts, axis=0)
+        return NumpySimpleSarDataset.from_scratch(cat("transmitter_positions"), cat("receiver_positions"),
+                                                  cat("stab_ref_posns"), ap0.centre_frequency, ap0.sample_bandwidth,
+                                                  phase_history=ph, waveform_fft=ap0.waveform_fft,
+                                                  slow_time_weighting=cat("slow_time_weighting"),
+                                                  sign_multiplier=ap0.sign_multiplier, c_eff=ap0.c_eff)

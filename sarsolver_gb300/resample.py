@@ -157,7 +157,10 @@ def resample_dataset(dataset, fast_downsample_factor: float = 1.0, slow_downsamp
     dr = range_changes(ap.stab_ref_posns, new_srp, ap.transmitter_positions, ap.receiver_positions)
     win = downsample_window(n, safety_factor)
     ktab = np.ascontiguousarray(np.stack([taps.real, taps.imag], axis=-1).astype(np.float64))
-    x = _device_rows(dataset.phase_history(), dev)
+    if hasattr(dataset, "phase_history_device"):   # e.g. a CPHD file: raw samples decoded on the device
+        x = dataset.phase_history_device(slice(None), device=dev)
+    else:
+        x = _device_rows(dataset.phase_history(), dev)
     out = torch.empty((len(starts), n), dtype=torch.complex64, device=dev)
     lib = _lib.load()
     with torch.cuda.device(dev):
