@@ -188,6 +188,31 @@ int sar_cgls(sar_plan *plan, const void *y_dev, void *x_dev, int zero_start, int
 int sar_cgls_ex(sar_plan *plan, const void *y_dev, void *x_dev, int start, const void *ahy_dev,
                 int max_iterations, double tolerance, double *history, sar_cgls_result *result, void *stream);
 
+/* PDHG (Chambolle-Pock) with the plan's operator pair: min_x ||A x - b||^2 + l1_weight ||x||_1
+ * (l1_weight = 0: no regulariser) -- replaces the CIL PDHG with f = L2NormSquared(b),
+ * g = ZeroFunction that the reference runs on its operator (tests/test_cil.py:25-37).  CIL's
+ * iteration order, from xbar = x0 and y = 0:
+ *   y = (y + sigma (A xbar - b)) / (1 + sigma / 2);  x' = prox_{tau g}(x - tau A^H y);
+ *   xbar = x' + theta (x' - x);  x = x'
+ * (prox of the L1 term: soft threshold of the complex modulus at tau l1_weight).  x_dev holds x0 on
+ * entry (zeroed when zero_start != 0) and the iterate after `iterations` iterations on return.
+ * sigma, tau: step sizes; 0 means "from ||A||", estimated with norm_iterations power iterations
+ * (each one forward and one backprojection; result->operator_norm): both 0 -> sigma = tau =
+ * 1 / ||A||, one 0 -> the other from sigma tau ||A||^2 = 1.  residual_history (host, may be NULL)
+ * receives ||A xbar_k - b|| for k = 0 .. iterations - 1 (xbar_0 = x0).  The loop issues work
+ * without reading back; the host waits once at the end.  Work vectors (2 x S*N + 2 x P complex64)
+ * come from the stream-ordered allocator.  Non-finite values return SAR_ERR_INVALID_ARGUMENT. */
+typedef struct sar_pdhg_result {
+    int iterations;        /* iterations run */
+    double sigma, tau;     /* step sizes used */
+    double theta;          /* relaxation used */
+    double operator_norm;  /* power-method estimate of ||A|| (0 when sigma and tau were both given) */
+} sar_pdhg_result;
+
+int sar_pdhg(sar_plan *plan, const void *b_dev, void *x_dev, int zero_start, int iterations, double sigma,
+             double tau, double theta, double l1_weight, int norm_iterations, double *residual_history,
+             sar_pdhg_result *result, void *stream);
+
 /* ------------------------------------------------ 3. learned warm start (U-Net)
  *
  * New (no counterpart in the reference): the network that maps a backprojected image A^H y to a

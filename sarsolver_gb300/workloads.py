@@ -4,6 +4,7 @@
     python -m sarsolver_gb300.workloads autofocus  # sharpness + phase gradient, 1024^2 x 2048 x 2048
     python -m sarsolver_gb300.workloads resample   # 8192 x 8192 phase history, factors 2 x 2
     python -m sarsolver_gb300.workloads cphd       # 8192 x 8192 CI4 CPHD file -> device
+    python -m sarsolver_gb300.workloads pdhg       # 100 PDHG iterations, 512^2 x 1024 x 1024
 
 Each prints one JSON line with CUDA-event times of the timed call (after one warm-up call).
 """
@@ -74,6 +75,26 @@ def resample_workload() -> dict:
     ds = NumpySimpleSarDataset(ap, ph)
     out, t = _time(lambda: resample_dataset(ds, 2.0, 2, new_srp=np.array([5.0, 5.0, 0.0]), keep_on_device=True))
     return {"workload": "resample", "ms": t, "in": [S, N], "out": list(out.phase_history().shape)}
+
+
+def pdhg_workload() -> dict:
+    """100 PDHG iterations (f = ||A x - b||^2, g = 0; sigma = 1, tau = 1 / ||A||^2) on a held-out
+    scene of the 512^2 x 1024 x 1024 learned-solver workload, against one forward projection plus
+    one backprojection (the operator work of one iteration)."""
+    from .learned import LearnedConfig, SceneSource
+    from .solvers import pdhg
+
+    src = SceneSource(LearnedConfig(), seed=4242, continuous=True)
+    plan, y, _, extent, snr = src.sample()
+    _, norm_info = pdhg(plan, y, iterations=0, norm_iterations=50, tau=1.0)
+    nrm = norm_info.operator_norm
+    iters = 100
+    (x, info), t = _time(lambda: pdhg(plan, y, iterations=iters, sigma=1.0, tau=1.0 / nrm ** 2))
+    xb = plan.adjoint(y)
+    _, t_pair = _time(lambda: plan.adjoint(plan.forward(xb)))
+    return {"workload": "pdhg", "iterations": iters, "ms": t, "ms_per_iteration": t / iters,
+            "operator_pair_ms": t_pair, "overhead_fraction": (t / iters - t_pair) / t_pair,
+            "operator_norm": nrm, "residual_first": info.history[0], "residual_last": info.history[-1]}
 
 
 def cphd_workload() -> dict:
@@ -154,7 +175,7 @@ def main(argv=None) -> None:
     name = argv[0] if argv else "cgls"
     torch.cuda.set_device(0)
     fn = {"cgls": cgls_workload, "autofocus": autofocus_workload, "resample": resample_workload,
-          "cphd": cphd_workload}[name]
+          "cphd": cphd_workload, "pdhg": pdhg_workload}[name]
     print(json.dumps(fn()))
 
 

@@ -1,0 +1,158 @@
+"""GPU PDHG (native driver + fused kernels) against PDHG on the FP64 oracle.
+
+The reference runs CIL's PDHG with f = L2NormSquared(b), g = ZeroFunction on its operator
+(tests/test_cil.py:25-37).  CIL is not available, so CIL's iteration is written here in numpy on
+the oracle's linear-mode operator pair and the GPU iterates and residual history are compared
+with it; the same with an L1 regulariser, and the power-method step sizes against an FP64
+estimate of ||A||.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from cases import crandn, rel_l2, spotlight_case
+from sarsolver_gb300 import SarPlan, _lib
+from sarsolver_gb300.solvers import pdhg
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def cuda_required():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+
+
+def numpy_pdhg(prob, b, iterations, sigma, tau, theta=1.0, l1=0.0, threads=1):
+    """CIL's PDHG order: dual step at xbar, primal step, over-relaxation (f = ||. - b||^2)."""
+    fwd = lambda v: oracle.forward(prob, v, mode="linear", threads=threads)
+    adj = lambda v: oracle.adjoint(prob, v, mode="linear", threads=threads)
+    x = np.zeros(prob.num_scatterers, np.complex128)
+    xbar = x.copy()
+    y = np.zeros_like(b)
+    hist = []
+    for _ in range(iterations):
+        q = fwd(xbar)
+        hist.append(np.linalg.norm(q - b))
+        y = (y + sigma * (q - b)) / (1.0 + 0.5 * sigma)
+        z = x - tau * adj(y)
+        if l1 > 0:
+            m = np.abs(z)
+            z = np.where(m > tau * l1, (1.0 - tau * l1 / np.maximum(m, 1e-300)) * z, 0.0)
+        xbar = z + theta * (z - x)
+        x = z
+    return x, np.array(hist)
+
+
+def numpy_norm(prob, iterations=300, threads=1):
+    rng = np.random.default_rng(0)
+    v = crandn(rng, prob.num_scatterers)
+    v /= np.linalg.norm(v)
+    est = 0.0
+    for _ in range(iterations):
+        q = oracle.forward(prob, v, mode="linear", threads=threads)
+        est = np.linalg.norm(q)
+        w = oracle.adjoint(prob, q, mode="linear", threads=threads)
+        v = w / np.linalg.norm(w)
+    return est
+
+
+def case_and_data(seed=0, snr_db=20.0, scatterers=12):
+    case = spotlight_case(num_pulses=64, num_freqs=128, n=48, spacing=0.5, aperture_deg=4.0)
+    rng = np.random.default_rng(seed)
+    prob = case.problem()
+    x_true = np.zeros(prob.num_scatterers, np.complex128)
+    idx = rng.choice(prob.num_scatterers, scatterers, replace=False)
+    x_true[idx] = crandn(rng, scatterers)
+    y = oracle.forward(prob, x_true, mode="linear", threads=oracle.default_threads())
+    noise = np.sqrt(np.mean(np.abs(y) ** 2) / 10 ** (snr_db / 10))
+    return case, prob, y + noise * crandn(rng, *y.shape), x_true
+
+
+@pytest.fixture(scope="module")
+def problem():
+    case, prob, y, x_true = case_and_data()
+    norm = numpy_norm(prob, threads=oracle.default_threads())
+    return case, prob, y, x_true, norm
+
+
+def test_pdhg_iterates_match_oracle(problem):
+    case, prob, y, _, norm = problem
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp="linear")
+    k = 10
+    s = t = 1.0 / norm
+    x, info = pdhg(plan, torch.from_numpy(y.astype(np.complex64)), iterations=k, sigma=s, tau=t)
+    xo, ho = numpy_pdhg(prob, y, k, s, t, threads=oracle.default_threads())
+    assert info.iterations == k and info.operator_norm == 0.0
+    assert info.sigma == s and info.tau == t and info.theta == 1.0
+    assert rel_l2(x.cpu().numpy(), xo) < 1e-4
+    np.testing.assert_allclose(info.history, ho, rtol=1e-4)
+    assert plan.device_flags() == 0
+
+
+def test_pdhg_l1_and_relaxation_match_oracle(problem):
+    case, prob, y, _, norm = problem
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp="linear")
+    # sigma = 1: the dual variable settles within a few iterations, so pixels with
+    # (2/3) |A^H b| > lam are active from the first one
+    k, s = 12, 1.0
+    t = 1.0 / (s * norm * norm)
+    lam = 0.3 * float(np.abs(oracle.adjoint(prob, y, mode="linear", threads=oracle.default_threads())).max())
+    x, info = pdhg(plan, torch.from_numpy(y.astype(np.complex64)), iterations=k, sigma=s, tau=t, theta=0.7, l1=lam)
+    xo, ho = numpy_pdhg(prob, y, k, s, t, theta=0.7, l1=lam, threads=oracle.default_threads())
+    xg = x.cpu().numpy()
+    assert rel_l2(xg, xo) < 1e-3
+    np.testing.assert_allclose(info.history, ho, rtol=1e-3)
+    # the threshold leaves most pixels exactly zero, as in the oracle
+    zg, zo = xg == 0, xo == 0
+    assert 0.5 < zo.mean() < 1.0 and (zg != zo).mean() < 1e-3
+
+
+def test_pdhg_default_steps_from_operator_norm(problem):
+    case, prob, y, _, norm = problem
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp="linear")
+    b = torch.from_numpy(y.astype(np.complex64)).cuda()
+    _, info = pdhg(plan, b, iterations=3, norm_iterations=100)
+    assert abs(info.operator_norm - norm) <= 2e-3 * norm   # Rayleigh quotient: a lower bound
+    assert info.operator_norm <= norm * (1 + 1e-5)
+    assert info.sigma == pytest.approx(1.0 / info.operator_norm) and info.tau == info.sigma
+    _, info2 = pdhg(plan, b, iterations=2, sigma=0.25 / norm, norm_iterations=100)
+    assert info2.tau * info2.sigma * info2.operator_norm ** 2 == pytest.approx(1.0, rel=1e-12)
+
+
+def test_pdhg_decreases_data_residual_and_warm_start(problem):
+    case, prob, y, _, norm = problem
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp="linear")
+    b = torch.from_numpy(y.astype(np.complex64)).cuda()
+    x, info = pdhg(plan, b, iterations=60, sigma=1.0, tau=1.0 / norm ** 2)
+    assert info.history[-1] < 0.5 * info.history[0]
+    # continuing from x (x0 given) starts at its residual
+    _, info2 = pdhg(plan, b, iterations=1, x0=x, sigma=1.0, tau=1.0 / norm ** 2)
+    direct = float(torch.linalg.vector_norm(plan.forward(x) - b.reshape(plan.forward(x).shape)))
+    assert info2.history[0] == pytest.approx(direct, rel=1e-4)
+
+
+def test_pdhg_argument_errors(problem):
+    case, prob, y, _, norm = problem
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp="linear")
+    b = torch.from_numpy(y.astype(np.complex64)).cuda()
+    with pytest.raises(ValueError):
+        pdhg(plan, b, iterations=2, sigma=-1.0)
+    x = torch.zeros(plan.num_scatterers, dtype=torch.complex64, device="cuda")
+    res = _lib.SarPdhgResult()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    lib = _lib.load()
+    bp, xp = ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(x.data_ptr())
+    assert lib.sar_pdhg(plan._handle, bp, xp, 1, -1, 0.1, 0.1, 1.0, 0.0, 0, None, ctypes.byref(res), st) == 1
+    assert lib.sar_pdhg(plan._handle, bp, xp, 1, 2, 0.0, 0.1, 1.0, 0.0, 0, None, ctypes.byref(res), st) == 1
+    assert lib.sar_pdhg(plan._handle, bp, xp, 1, 2, 0.1, 0.1, 1.0, -1.0, 0, None, ctypes.byref(res), st) == 1
+    plan.set_slow_time_weighting(np.zeros(plan.num_slow_times, np.complex128))   # A = 0
+    with pytest.raises(_lib.SarError):
+        pdhg(plan, b, iterations=2)
+    # zero iterations: x0 returned unchanged
+    x0 = torch.ones(plan.num_scatterers, dtype=torch.complex64, device="cuda")
+    x1, info = pdhg(plan, b, iterations=0, x0=x0, sigma=0.1, tau=0.1)
+    assert info.iterations == 0 and torch.equal(x1, x0)
