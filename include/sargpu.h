@@ -116,6 +116,8 @@ typedef struct sar_plan_info {
     size_t num_fast_times, num_slow_times, num_scatterers;   /* N, S, P */
     int device;                 /* CUDA device of the plan */
     int fft_callbacks;          /* 1: range-profile FFTs run with cuFFT load/store callbacks */
+    int gather_lanes_y;         /* 1: the grid backprojection runs warp lanes along y (bins change
+                                   more slowly along y than along x), 0: along x */
 } sar_plan_info;
 
 /* Create a plan on `device` (-1: the current device).  Copies all host inputs. */

@@ -103,6 +103,7 @@ struct sar_plan {
     long bg0 = 0;
     int Lg = 0;
     int wwin = 0, pb = 32;
+    int lanes_y = 0;
     bool staged = true;
     int seg_tiles = 0, segs_per_column = 0, ws = 0, pbf = 16;
     size_t n_strips = 0;
@@ -437,6 +438,7 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
         const double h = s_r * 2.0 * 16.0 * (nex + ney);
         if (h > 1.0e6) return fail(SAR_ERR_NOT_SUPPORTED, "grid spacing too coarse for the range sampling");
         p->wwin = (2 * ((int)std::ceil(h) + 3) + 3) & ~3;
+        p->lanes_y = choose_lanes_y(tx, rx, S, origin, ex, ey, ez, nx, ny, nz);
         // Nearest-bin decisions must match FP64, and wide tiles need the exact integer part:
         // split the linear bin rates in both cases (sar_geom.cuh, bin_coeffs).
         p->gc_adj.precise_bins = p->gc_fwd.precise_bins = (p->interp == SAR_INTERP_NEAREST_REF || p->wwin > 256) ? 1 : 0;
@@ -712,6 +714,7 @@ int sar_plan_get_info(const sar_plan* p, sar_plan_info* info) {
     info->num_scatterers = p->P;
     info->device = p->device;
     info->fft_callbacks = p->fft_cb ? 1 : 0;
+    info->gather_lanes_y = p->lanes_y;
     return SAR_OK;
 }
 
@@ -797,6 +800,7 @@ int sar_adjoint(sar_plan* p, const void* y_dev, void* x_dev, void* stream) {
         a.pb = p->pb;
         a.staged = p->staged;
         a.accumulate = 0;
+        a.lanes_y = p->lanes_y;
         SAR_CUDA(p->staged ? launch_bp_grid_ws(a, st) : launch_bp_grid(a, st), "backprojection");
     } else {
         SAR_CUDA(launch_bp_points(point_args(p, p->interp == SAR_INTERP_LINEAR ? BIN_LINEAR : BIN_ADJ_NEAREST), p->d_prof, (float2*)x_dev, 0, st),
@@ -896,6 +900,7 @@ int sar_adjoint_pulse_block(sar_plan* p, const void* y_block_dev, size_t first_p
     a.pb = p->pb;
     a.staged = p->staged;
     a.accumulate = accumulate ? 1 : 0;
+    a.lanes_y = p->lanes_y;
     SAR_CUDA(p->staged ? launch_bp_grid_ws(a, st) : launch_bp_grid(a, st), "backprojection");
     return SAR_OK;
 }

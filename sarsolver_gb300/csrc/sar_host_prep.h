@@ -107,4 +107,31 @@ static inline void box_distance_bounds(const double* a, const double* o, const d
     *dmax = best;
 }
 
+// 1 when range bins change more slowly along the grid's y axis than along x, at the grid centre
+// and summed over the pulses (|d bin / d i| vs |d bin / d j| up to the common factor s_r): the
+// backprojection gather then runs its lanes along y (BpGridArgs::lanes_y).
+static inline int choose_lanes_y(const double* tx, const double* rx, size_t S, const double* origin,
+                                 const double* ex, const double* ey, const double* ez, int nx, int ny, int nz) {
+    double c[3];
+    for (int d = 0; d < 3; ++d)
+        c[d] = origin[d] + 0.5 * ((nx - 1) * ex[d] + (ny - 1) * ey[d] + (nz - 1) * ez[d]);
+    double rate_x = 0.0, rate_y = 0.0;
+    for (size_t s = 0; s < S; ++s) {
+        double gx = 0.0, gy = 0.0;
+        for (int ant = 0; ant < 2; ++ant) {
+            const double* a = (ant ? rx : tx) + 3 * s;
+            const double w[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+            const double n = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+            if (!(n > 0.0)) continue;
+            gx += (w[0] * ex[0] + w[1] * ex[1] + w[2] * ex[2]) / n;
+            gy += (w[0] * ey[0] + w[1] * ey[1] + w[2] * ey[2]) / n;
+        }
+        if (isfinite(gx) && isfinite(gy)) {
+            rate_x += fabs(gx);
+            rate_y += fabs(gy);
+        }
+    }
+    return rate_y < rate_x ? 1 : 0;
+}
+
 }  // namespace sar

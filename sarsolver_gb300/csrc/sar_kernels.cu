@@ -476,6 +476,241 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_kernel(const BpGridA
     }
 }
 
+// ------------------------------------- K2, linear bins: two pulses per packed instruction
+// The same pipeline with the consumers' arithmetic on FP32 pairs (fma.rn.f32x2 and friends,
+// one instruction for two values, each rounded as the scalar operation): the two values are
+// the same pixel for two consecutive pulses p (even) and p + 1.  Coefficient sets are stored
+// pair-interleaved, kSetF4 * 2 float4 per (pulse pair, sub-tile):
+//   [c0 c0' c1 c1'] [c2 c2' c3 c3'] [c4 c4' c5 c5'] [c6 c6' c7 c7'] [c8 c8' c9 c9']
+//   [v0 v0' v1 v1'] [v2 v2' v3 v3'] [v4 v4' v5 v5']  (primed: pulse p + 1; 4 float4 unused)
+// so that each half of a 16-byte shared-memory load is one operand pair.  Per pixel the
+// polynomials are evaluated in Horner form in the row offset dj (the only per-row constant a
+// thread keeps), the phase is reduced to [-0.5, 0.5] cycles with the 1.5 * 2^23 shifter
+// instead of rint (keeping the special-function pipe for sin and cos), and the complex
+// multiply-accumulate runs on (pulse p, pulse p + 1) accumulator pairs.  A stage with an odd
+// number of pulses gets a padding pulse with zero coefficients and a zeroed window.
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+
+__device__ __forceinline__ void producer_coeffs_pair(const GridConst& g, const PulseGeom* __restrict__ pulses, int s0,
+                                                     int npb, int pass, const df3* anchors, float4* coef, int* base,
+                                                     int lane) {
+    const int pi = pass + (lane >> 2), q = lane & 3;
+    const bool valid = pi < npb;
+    const bool pad = pi == npb && (npb & 1);   // partner of the last pulse of an odd stage
+    AnchorExpansion ae = {};
+    Coeffs co = {};
+    df vb = df_make(0.0f, 0.0f);
+    if (valid) {
+        const PulseGeom pg = load_pulse(pulses + s0 + pi);
+        ae = expand_anchor(anchors[q], pg, g);
+        phase_coeffs(ae, g, co.c);
+        vb = anchor_bin(ae, g);
+    }
+    const unsigned all = 0xffffffffu;
+    df sum = df_add(vb, df_make(__shfl_xor_sync(all, vb.hi, 1), __shfl_xor_sync(all, vb.lo, 1)));
+    sum = df_add(sum, df_make(__shfl_xor_sync(all, sum.hi, 2), __shfl_xor_sync(all, sum.lo, 2)));
+    int b = base_bin_of(sum, 4.0f);
+    b = __shfl_sync(all, b, lane & ~3);
+    if (valid) bin_coeffs(ae, vb, b, g, co);
+    if (valid || pad) {   // the padding pulse stores zeros (co = {})
+        float* dst = reinterpret_cast<float*>(coef + ((pi >> 1) * 4 + q) * (2 * kSetF4)) + (pi & 1);
+        const float vals[16] = {co.c[0], co.c[1], co.c[2], co.c[3], co.c[4], co.c[5], co.c[6], co.c[7],
+                                co.c[8], co.c[9], co.v[0], co.v[1], co.v[2], co.v[3], co.v[4], co.v[5]};
+#pragma unroll
+        for (int k = 0; k < 16; ++k) dst[2 * k] = vals[k];
+        if (valid && q == 0) base[pi] = b;
+    }
+}
+
+// LANES_Y = false: lane = column i, warp w owns rows 4w .. 4w + 3 (the thread's column terms
+// are polynomials in dj); LANES_Y = true: lane = row j, warp w owns columns 4w .. 4w + 3 (line
+// terms in di).  A quarter-warp's eight 16-byte window loads are conflict-free when they fall
+// in distinct 16-byte bank groups or on the same bin; lanes along the axis where bins change
+// slowly (cross-range) make them land on one or two bins.
+template <bool LANES_Y>
+__global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const BpGridArgs a) {
+    extern __shared__ __align__(16) float4 smem[];
+    const int pb = a.pb, ww = a.wwin;
+    float4* win0 = smem;
+    float4* coef0 = win0 + 2 * pb * ww;
+    int* base0 = reinterpret_cast<int*>(coef0 + 2 * pb * 4 * kSetF4);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(base0 + 2 * pb);   // full[0..1], empty[2..3]
+    df3* anchors = reinterpret_cast<df3*>(bars + 4);
+
+    const GridConst& g = a.g;
+    int tile = blockIdx.x;
+    const int tj = tile % g.tiles_y;
+    tile /= g.tiles_y;
+    const int ti = tile % g.tiles_x;
+    const int k = tile / g.tiles_x;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x < 4) anchors[threadIdx.x] = subtile_anchor(ti, tj, k, threadIdx.x, g);
+    if (threadIdx.x == 0) {
+        mbar_init(&bars[0], kWsProducers);
+        mbar_init(&bars[1], kWsProducers);
+        mbar_init(&bars[2], kWsConsumers / 32);
+        mbar_init(&bars[3], kWsConsumers / 32);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    const int nst = (a.S + pb - 1) / pb;
+
+    if (warp >= kWsConsumers / 32) {
+        // ----------------------------------------------------------- producers
+        const int pw = warp - kWsConsumers / 32;
+        bool ok = true;
+        int issued = 0;
+        for (int st = 0; st < nst; ++st) {
+            const int b = st & 1;
+            if (st >= 2 && !mbar_wait(&bars[2 + b], ((st - 2) >> 1) & 1, 128, 2048)) {
+                ok = false;
+                break;
+            }
+            const int s0 = st * pb, npb = min(pb, a.S - s0);
+            float4* coef = coef0 + b * pb * 4 * kSetF4;
+            int* base = base0 + b * pb;
+            float4* win = win0 + (size_t)b * pb * ww;
+            int mine = 0;   // pulses of this stage staged by this warp
+            for (int pass = 8 * pw; pass < npb; pass += 8 * kWsProducers) {
+                producer_coeffs_pair(g, a.pulses, s0, npb, pass, anchors, coef, base, lane);
+                mine += min(8, npb - pass);
+                if ((npb & 1) && npb - pass < 8) {   // this pass holds the padding pulse: zero its window
+                    float4* pw_ = win + (size_t)npb * ww;
+                    for (int e = lane; e < ww; e += 32) pw_[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive_expect_tx(&bars[b], (uint32_t)(mine * ww * sizeof(float4)));
+            for (int pass = 8 * pw; pass < npb; pass += 8 * kWsProducers) {
+                const int pi = pass + lane;
+                if (lane < 8 && pi < npb) {
+                    long gi = (long)base[pi] - ww / 2 - a.bg0;
+                    if (gi < 0 || gi > (long)a.Lg - ww) {
+                        raise_flag(a.flags, FLAG_TILE_WINDOW);
+                        gi = gi < 0 ? 0 : (long)a.Lg - ww;
+                    }
+                    fence_proxy_async_smem();
+                    bulk_g2s(win + (size_t)pi * ww, a.pairs + (size_t)(s0 + pi) * a.Lg + gi,
+                             (uint32_t)(ww * sizeof(float4)), &bars[b]);
+                }
+            }
+            issued = st + 1;
+        }
+        for (int st = max(0, issued - 2); st < issued; ++st)
+            if (!mbar_wait(&bars[st & 1], (st >> 1) & 1, 128, 2048)) ok = false;
+        if (!ok && lane == 0) raise_flag(a.flags, FLAG_WAIT_TIMEOUT);
+        return;
+    }
+
+    // -------------------------------------------------------------- consumers
+    // u: the thread's fixed offset (from the lane), DU[r]: its four offsets along the other axis
+    const int q = LANES_Y ? (warp >= 4) + 2 * (lane >= 16) : (lane >= 16) + 2 * (warp >= 4);
+    const float u = (float)(lane - 8 - 16 * (lane >= 16));
+    const float2 U1 = f2(u, u), U2 = f2(u * u, u * u), U3 = f2(u * u * u, u * u * u);
+    float2 DU[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const float d = (float)(4 * warp + r - 8 - 16 * (warp >= 4));
+        DU[r] = f2(d, d);
+    }
+    const float2 SH = f2(SAR_SHIFTER, SAR_SHIFTER), NSH = f2(-SAR_SHIFTER, -SAR_SHIFTER);
+    const float2 M1 = f2(-1.f, -1.f), TWO_PI2 = f2(SAR_TWO_PI, SAR_TWO_PI);
+    const int idx_bias = ww / 2 - SAR_SHIFTER_BITS;
+    const unsigned idx_max = (unsigned)(ww - 1);
+    float acc_re[4] = {0.f, 0.f, 0.f, 0.f}, acc_im[4] = {0.f, 0.f, 0.f, 0.f};
+    bool ok = true;
+    for (int st = 0; st < nst; ++st) {
+        const int b = st & 1;
+        if (!mbar_wait(&bars[b], (st >> 1) & 1, 32, 256)) {
+            ok = false;
+            break;
+        }
+        const int npp = (min(pb, a.S - st * pb) + 1) >> 1;
+        const float4* coef = coef0 + b * pb * 4 * kSetF4 + q * (2 * kSetF4);
+        const float4* win = win0 + (size_t)b * pb * ww;
+        float2 st_re[4], st_im[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) st_re[r] = st_im[r] = f2(0.f, 0.f);
+#pragma unroll 1
+        for (int pp = 0; pp < npp; ++pp) {
+            const float4* cs = coef + pp * (8 * kSetF4);
+            const float4 A = cs[0], B = cs[1], C = cs[2], D = cs[3], E = cs[4], F = cs[5], G = cs[6], H = cs[7];
+            // The thread's terms of both pulses: ph = cph + b1 d + b2 d^2 + c9 d^3 and
+            // v = cv + bv1 d + bv2 d^2 in the offset d along the warp's axis (sar_geom.cuh Coeffs:
+            // c0..c9 = A.xy A.zw B.xy B.zw C.xy C.zw D.xy D.zw E.xy E.zw, v0..v5 = F.xy .. H.zw).
+            float2 cph, b1, b2, c9, cv, bv1, bv2;
+            if (LANES_Y) {   // u = dj, d = di
+                cph = fma2(f2(E.z, E.w), U3, fma2(f2(C.z, C.w), U2, fma2(f2(B.x, B.y), U1, f2(A.x, A.y))));
+                b1 = fma2(f2(E.x, E.y), U2, fma2(f2(C.x, C.y), U1, f2(A.z, A.w)));
+                b2 = fma2(f2(D.z, D.w), U1, f2(B.z, B.w));
+                c9 = f2(D.x, D.y);
+                cv = fma2(f2(H.z, H.w), U2, fma2(f2(G.x, G.y), U1, f2(F.x, F.y)));
+                bv1 = fma2(f2(H.x, H.y), U1, f2(F.z, F.w));
+                bv2 = f2(G.z, G.w);
+            } else {         // u = di, d = dj (as column_terms, linear bins)
+                cph = fma2(f2(D.x, D.y), U3, fma2(f2(B.z, B.w), U2, fma2(f2(A.z, A.w), U1, f2(A.x, A.y))));
+                b1 = fma2(f2(D.z, D.w), U2, fma2(f2(C.x, C.y), U1, f2(B.x, B.y)));
+                b2 = fma2(f2(E.x, E.y), U1, f2(C.z, C.w));
+                c9 = f2(E.z, E.w);
+                cv = fma2(f2(G.z, G.w), U2, fma2(f2(F.z, F.w), U1, f2(F.x, F.y)));
+                bv1 = fma2(f2(H.x, H.y), U1, f2(G.x, G.y));
+                bv2 = f2(H.z, H.w);
+            }
+            const float4* wa = win + (size_t)(2 * pp) * ww;
+            const float4* wb = wa + ww;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const float2 d = DU[r];
+                const float2 ph = fma2(fma2(fma2(c9, d, b2), d, b1), d, cph);
+                const float2 f = fma2(f2(rintf(ph.x), rintf(ph.y)), M1, ph);   // ph - rint(ph), exact
+                const float2 v = fma2(fma2(bv2, d, bv1), d, cv);
+                const float2 r1 = add2(v, SH);
+                const float2 s = fma2(add2(r1, NSH), M1, v);               // v - rint(v), exact
+                const unsigned ia = min((unsigned)(__float_as_int(r1.x) + idx_bias), idx_max);
+                const unsigned ib = min((unsigned)(__float_as_int(r1.y) + idx_bias), idx_max);
+                const float4 pa = wa[ia], pq = wb[ib];
+                const float2 re = f2(fmaf(s.x, pa.z, pa.x), fmaf(s.y, pq.z, pq.x));
+                const float2 im = f2(fmaf(s.x, pa.w, pa.y), fmaf(s.y, pq.w, pq.y));
+                const float2 x = mul2(f, TWO_PI2);
+                float2 sn, cn;
+                __sincosf(x.x, &sn.x, &cn.x);
+                __sincosf(x.y, &sn.y, &cn.y);
+                st_re[r] = fma2(re, cn, fma2(im, sn, st_re[r]));
+                st_im[r] = fma2(im, cn, fma2(mul2(re, M1), sn, st_im[r]));
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            acc_re[r] += st_re[r].x + st_re[r].y;
+            acc_im[r] += st_im[r].x + st_im[r].y;
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&bars[2 + b]);
+    }
+    if (!ok) {
+        if (lane == 0) raise_flag(a.flags, FLAG_WAIT_TIMEOUT);
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int i = ti * kTile + (LANES_Y ? 4 * warp + r : lane);
+        const int j = tj * kTile + (LANES_Y ? lane : 4 * warp + r);
+        if (i < g.nx && j < g.ny) {
+            const size_t p = ((size_t)k * g.ny + j) * g.nx + i;
+            float2 o = make_float2(acc_re[r], acc_im[r]);
+            if (a.accumulate) {
+                const float2 old = a.x[p];
+                o.x += old.x;
+                o.y += old.y;
+            }
+            a.x[p] = o;
+        }
+    }
+}
+
 cudaError_t launch_bp_grid_ws(const BpGridArgs& a, cudaStream_t st) {
     if (a.pb < 1 || a.pb > 32 || a.wwin < 4 || (a.wwin & 3)) return cudaErrorInvalidValue;
     const size_t smem = bp_grid_ws_smem_bytes(a.wwin, a.pb);
@@ -485,10 +720,14 @@ cudaError_t launch_bp_grid_ws(const BpGridArgs& a, cudaStream_t st) {
         e = cudaFuncSetAttribute(bp_grid_ws_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         bp_grid_ws_kernel<true><<<blocks, kWsThreads, smem, st>>>(a);
-    } else {
-        e = cudaFuncSetAttribute(bp_grid_ws_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    } else if (a.lanes_y) {
+        e = cudaFuncSetAttribute(bp_grid_ws_pair_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        bp_grid_ws_kernel<false><<<blocks, kWsThreads, smem, st>>>(a);
+        bp_grid_ws_pair_kernel<true><<<blocks, kWsThreads, smem, st>>>(a);
+    } else {
+        e = cudaFuncSetAttribute(bp_grid_ws_pair_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        bp_grid_ws_pair_kernel<false><<<blocks, kWsThreads, smem, st>>>(a);
     }
     return cudaGetLastError();
 }

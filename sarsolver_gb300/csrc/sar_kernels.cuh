@@ -33,6 +33,8 @@ struct BpGridArgs {
     int pb;                    // pulses per stage (multiple of 8, <= 32)
     int staged;                // 1: stage windows in shared memory; 0: read global directly
     int accumulate;            // 1: x += result
+    int lanes_y;               // 1: lanes of a warp run along y (chosen when bins change more slowly
+                               //    along y than along x: fewer shared-memory bank conflicts)
 };
 size_t bp_grid_smem_bytes(int wwin, int pb, int staged);
 cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st);

@@ -182,6 +182,8 @@ extern "C" int sar_adjoint_from_profiles_noalloc(const sar_geometry* g, const vo
         a.bg0 = (int)first_bin;
         a.wwin = wwin;
         a.accumulate = 0;
+        a.lanes_y = choose_lanes_y(g->transmit_posns, g->receive_posns, S, g->grid_origin, g->grid_step_x,
+                                   g->grid_step_y, g->grid_step_z, nx, ny, nz);
         a.pb = 32;
         a.staged = 0;
         for (int pb = 32; pb >= 8; pb -= 8)

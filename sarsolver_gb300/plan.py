@@ -108,6 +108,7 @@ class SarPlan:
         self.device_bytes = int(info.device_bytes)
         self.is_grid = bool(info.grid)
         self.fft_callbacks = bool(info.fft_callbacks)
+        self.gather_lanes_y = bool(info.gather_lanes_y)
         # The aperture's own weighting; phase corrections multiply it (autodiff.phase_weights).
         self.base_weights = torch.as_tensor(
             np.asarray(aperture.slow_time_weighting, dtype=np.complex64).reshape(-1)).to(self.device)
