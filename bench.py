@@ -217,7 +217,7 @@ def run_ours(args):
     k2_ms = stage_ms[1] / max(calls, 1)
     fft_ms = stage_ms[0] / max(calls, 1)
     achieved = P * S / (k2_ms * 1e-3)
-    traffic = read_profile_traffic("bp_grid_ws")
+    traffic = read_profile_traffic("bp_grid_ws_pair")
     result = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -235,7 +235,7 @@ def run_ours(args):
                                   "scatter_kernel": fstage[1] / max(fcalls, 1),
                                   "downsample_fft_side": fstage[2] / max(fcalls, 1)},
                     "note": "y = A x on the same workload (fp_grid_ws_kernel + FFT downsampling), not the headline"},
-        "roofline": {"bound": "sfu", "kernel": "bp_grid_ws_kernel", "achieved": achieved, "peak": r_roof,
+        "roofline": {"bound": "sfu", "kernel": "bp_grid_ws_pair_kernel", "achieved": achieved, "peak": r_roof,
                      "unit": "px*pulse/s", "frac": achieved / r_roof, "traffic": traffic,
                      "peak_basis": f"{props.multi_processor_count} SMs x {sm_max:.0f} MHz x 16 MUFU/clk/SM / "
                                    "3 MUFU per px*pulse (sm_max_mhz of MEASURED_PEAKS.json)"},
