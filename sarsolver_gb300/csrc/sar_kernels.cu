@@ -620,7 +620,10 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
     const float2 M1 = f2(-1.f, -1.f), TWO_PI2 = f2(SAR_TWO_PI, SAR_TWO_PI);
     const int idx_bias = ww / 2 - SAR_SHIFTER_BITS;
     const unsigned idx_max = (unsigned)(ww - 1);
-    float acc_re[4] = {0.f, 0.f, 0.f, 0.f}, acc_im[4] = {0.f, 0.f, 0.f, 0.f};
+    float acc_re[4], acc_im[4];
+    float2 acc2_re[4], acc2_im[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) acc2_re[r] = acc2_im[r] = f2(0.f, 0.f);
     bool ok = true;
     for (int st = 0; st < nst; ++st) {
         const int b = st & 1;
@@ -631,9 +634,8 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
         const int npp = (min(pb, a.S - st * pb) + 1) >> 1;
         const float4* coef = coef0 + b * pb * 4 * kSetF4 + q * (2 * kSetF4);
         const float4* win = win0 + (size_t)b * pb * ww;
-        float2 st_re[4], st_im[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) st_re[r] = st_im[r] = f2(0.f, 0.f);
+        float2* st_re = acc2_re;
+        float2* st_im = acc2_im;
 #pragma unroll 1
         for (int pp = 0; pp < npp; ++pp) {
             const float4* cs = coef + pp * (8 * kSetF4);
@@ -679,13 +681,8 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
                 __sincosf(x.x, &sn.x, &cn.x);
                 __sincosf(x.y, &sn.y, &cn.y);
                 st_re[r] = fma2(re, cn, fma2(im, sn, st_re[r]));
-                st_im[r] = fma2(im, cn, fma2(mul2(re, M1), sn, st_im[r]));
+                st_im[r] = fma2(im, cn, fma2(f2(-re.x, -re.y), sn, st_im[r]));
             }
-        }
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            acc_re[r] += st_re[r].x + st_re[r].y;
-            acc_im[r] += st_im[r].x + st_im[r].y;
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&bars[2 + b]);
@@ -693,6 +690,11 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
     if (!ok) {
         if (lane == 0) raise_flag(a.flags, FLAG_WAIT_TIMEOUT);
         return;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        acc_re[r] = acc2_re[r].x + acc2_re[r].y;
+        acc_im[r] = acc2_im[r].x + acc2_im[r].y;
     }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {

@@ -44,7 +44,9 @@ def test_scale_configuration():
     print(f"scale: forward {t_fwd:.3f} s ({units / t_fwd:.3e} px*pulse/s), backprojection {t_adj:.3f} s "
           f"({units / t_adj:.3e}), streamed from pinned host in 512-pulse blocks {t_stream:.3f} s "
           f"({units / t_stream:.3e})")
-    assert float(torch.linalg.vector_norm(img_s - img) / torch.linalg.vector_norm(img)) < 1e-6
+    # two FP32 summation orders of 16384 pulses (per-pulse-pair accumulators, blocks added into the
+    # image when streamed), each ~2e-6 from the FP64 oracle below
+    assert float(torch.linalg.vector_norm(img_s - img) / torch.linalg.vector_norm(img)) < 5e-6
     assert plan.device_flags() == 0
 
     # 256^2 patch at the scene centre against the FP64 oracle (all pulses).
