@@ -118,6 +118,8 @@ typedef struct sar_plan_info {
     int fft_callbacks;          /* 1: range-profile FFTs run with cuFFT load/store callbacks */
     int gather_lanes_y;         /* 1: the grid backprojection runs warp lanes along y (bins change
                                    more slowly along y than along x), 0: along x */
+    int fused_upsampling;       /* 1: the backprojection's range profiles come from the fused
+                                   upsampling kernel (N = 4096, M a multiple of N), 0: cuFFT */
 } sar_plan_info;
 
 /* Create a plan on `device` (-1: the current device).  Copies all host inputs. */

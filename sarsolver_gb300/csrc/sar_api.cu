@@ -118,6 +118,10 @@ struct sar_plan {
     float2* d_wadj = nullptr;
     float2* d_wfwd = nullptr;
     void* d_spec = nullptr;        // FFT rows: float2, or double2 when fft_double
+    // fused adjoint upsampling (N = 4096, M a multiple of N): twiddle tables e^{2 pi i q / N}, e^{2 pi i q / M}
+    bool fused_up = false;
+    float2* d_tw_n = nullptr;
+    float2* d_tw_m = nullptr;
     bool fft_double = false;
     float4* d_prof = nullptr;   // [S][Lg] pairs (adjoint) / float2 accumulator (forward)
     int* d_strip = nullptr;
@@ -172,6 +176,8 @@ struct sar_plan {
         cudaFree(d_wadj);
         cudaFree(d_wfwd);
         cudaFree(d_spec);
+        cudaFree(d_tw_n);
+        cudaFree(d_tw_m);
         cudaFree(d_prof);
         cudaFree(d_strip);
         cudaFree(d_flags);
@@ -620,6 +626,22 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
         p->have_tail = true;
         p->tail_rows = tail;
     }
+    // Fused adjoint upsampling: for N = 4096 and M a multiple of N the backprojection's range
+    // profiles come from one kernel (eight-way split of the length-M transform into N-point ones,
+    // stored span only) instead of pack + inverse FFT + unpack; twiddles computed in FP64.
+    if (upsample_fused_supported((int)N, (long)M, p->Lg)) {
+        std::vector<float2> tn(N), tm(M);
+        const double two_pi = 6.283185307179586476925286766559;
+        for (size_t q = 0; q < N; ++q)
+            tn[q] = make_float2((float)std::cos(two_pi * (double)q / (double)N), (float)std::sin(two_pi * (double)q / (double)N));
+        for (size_t q = 0; q < M; ++q)
+            tm[q] = make_float2((float)std::cos(two_pi * (double)q / (double)M), (float)std::sin(two_pi * (double)q / (double)M));
+        if ((rc = p->alloc(&p->d_tw_n, N, "twiddles"))) return rc;
+        if ((rc = p->alloc(&p->d_tw_m, M, "twiddles"))) return rc;
+        SAR_CUDA(cudaMemcpy(p->d_tw_n, tn.data(), sizeof(float2) * N, cudaMemcpyHostToDevice), "twiddles");
+        SAR_CUDA(cudaMemcpy(p->d_tw_m, tm.data(), sizeof(float2) * M, cudaMemcpyHostToDevice), "twiddles");
+        p->fused_up = true;
+    }
     // Callback transforms (single precision): opt-in with SAR_FFT_CALLBACKS=1.  On GB300 with the
     // cuFFT of CUDA 13.0, plans with JIT (LTO) callbacks fail to build (CUFFT_INTERNAL_ERROR from
     // cufftMakePlanMany for LTO-IR of compute_90 .. compute_103a alike), so the packing kernels are
@@ -715,6 +737,7 @@ int sar_plan_get_info(const sar_plan* p, sar_plan_info* info) {
     info->device = p->device;
     info->fft_callbacks = p->fft_cb ? 1 : 0;
     info->gather_lanes_y = p->lanes_y;
+    info->fused_upsampling = p->fused_up ? 1 : 0;
     return SAR_OK;
 }
 
@@ -724,6 +747,13 @@ static int upsample_rows(sar_plan* p, const float2* y, size_t begin, size_t end,
     for (size_t first = begin; first < end; first += (size_t)p->chunk) {
         const int rows = (int)std::min<size_t>(p->chunk, end - first);
         const int dbl = p->fft_double;
+        if (pairs_out && p->fused_up) {
+            SAR_CUDA(launch_upsample_pairs_fused(y, p->d_wave, p->d_wadj, p->d_tw_n, p->d_tw_m, p->d_prof, (int)p->N,
+                                                 (long)p->M, p->Lg, p->bg0, rows, (int)first,
+                                                 p->interp == SAR_INTERP_LINEAR, st),
+                     "fused upsampling");
+            continue;
+        }
         if (p->fft_cb) {
             cufftHandle h = 0;
             int rc = cb_plan(p, rows, true, &h);

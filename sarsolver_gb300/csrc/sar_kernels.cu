@@ -1448,6 +1448,192 @@ cudaError_t launch_unpack_pairs(const void* spec, int dbl, const float2* wfac, f
     return cudaGetLastError();
 }
 
+// ------------------------------------------- K1 fused: upsampling FFT straight into pairs
+// For N = 4096 and M = U N (integer U): bin b = U j + r of the inverse length-M transform of the
+// zero-padded spectrum (frequencies k in [-N/2, N/2), X_k = conj(W) y at k mod N) is
+//   p(U j + r) = sum_k X_k e^{2 pi i k r / M} e^{2 pi i k j / N},
+// an N-point inverse DFT of the spectrum twiddled by e^{2 pi i k r / M}.  One CTA per pulse row
+// computes the U such transforms in shared memory (radix-16 Stockham, three passes, one
+// 16-point butterfly per thread and pass), keeps the bins of the stored span
+// [bg0, bg0 + Lg] (taken modulo M) and writes the (value, difference) pairs of
+// unpack_pairs_kernel directly: the row is read once (N values) and only the span is written,
+// where the unfused path writes and reads the M-point rows three times.  Twiddles come from
+// FP64-computed tables e^{2 pi i q / N} and e^{2 pi i q / M}.
+constexpr int kUpN = 4096;
+constexpr int kUpThreads = 256;
+
+__device__ __forceinline__ int up_pad(int x) { return x + (x >> 4); }   // one slot per 16: no bank conflicts
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ void dft4_inv(float2& x0, float2& x1, float2& x2, float2& x3) {
+    const float2 t0 = make_float2(x0.x + x2.x, x0.y + x2.y), t1 = make_float2(x0.x - x2.x, x0.y - x2.y);
+    const float2 t2 = make_float2(x1.x + x3.x, x1.y + x3.y);
+    const float2 t3 = make_float2(-(x1.y - x3.y), x1.x - x3.x);   // i (x1 - x3)
+    x0 = make_float2(t0.x + t2.x, t0.y + t2.y);
+    x1 = make_float2(t1.x + t3.x, t1.y + t3.y);
+    x2 = make_float2(t0.x - t2.x, t0.y - t2.y);
+    x3 = make_float2(t1.x - t3.x, t1.y - t3.y);
+}
+// v[k] <- sum_n v[n] e^{+2 pi i n k / 16}: n = 4 n1 + n2, k = k1 + 4 k2 (two radix-4 stages).
+__device__ __forceinline__ void dft16_inv(float2 (&v)[16]) {
+#pragma unroll
+    for (int n2 = 0; n2 < 4; ++n2) dft4_inv(v[n2], v[4 + n2], v[8 + n2], v[12 + n2]);   // -> Y[n2][k1] at v[4 k1 + n2]
+    const float c1 = 0.92387953251128674f, s1 = 0.38268343236508977f, h = 0.70710678118654752f;
+    // W16^(n2 k1) for (n2, k1) in {1,2,3} x {1,2,3}: exponents 1 2 3 / 2 4 6 / 3 6 9
+    v[4 + 1] = cmulf(v[4 + 1], make_float2(c1, s1));
+    v[8 + 1] = cmulf(v[8 + 1], make_float2(h, h));
+    v[12 + 1] = cmulf(v[12 + 1], make_float2(s1, c1));
+    v[4 + 2] = cmulf(v[4 + 2], make_float2(h, h));
+    v[8 + 2] = make_float2(-v[8 + 2].y, v[8 + 2].x);   // W16^4 = i
+    v[12 + 2] = cmulf(v[12 + 2], make_float2(-h, h));
+    v[4 + 3] = cmulf(v[4 + 3], make_float2(s1, c1));
+    v[8 + 3] = cmulf(v[8 + 3], make_float2(-h, h));
+    v[12 + 3] = cmulf(v[12 + 3], make_float2(-c1, -s1));
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) dft4_inv(v[4 * k1], v[4 * k1 + 1], v[4 * k1 + 2], v[4 * k1 + 3]);
+    // now v[4 k1 + k2] holds X[k1 + 4 k2]: transpose the 4x4 index to natural order
+    float2 t[16];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+        for (int k2 = 0; k2 < 4; ++k2) t[k1 + 4 * k2] = v[4 * k1 + k2];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) v[k] = t[k];
+}
+
+// v[r] *= w^r for r = 1..15, the powers built by squaring (at most four chained products).
+__device__ __forceinline__ void apply_powers(float2 (&v)[16], float2 w) {
+    const float2 w2 = cmulf(w, w), w4 = cmulf(w2, w2), w8 = cmulf(w4, w4);
+    const float2 w3 = cmulf(w2, w), w5 = cmulf(w4, w), w6 = cmulf(w4, w2), w7 = cmulf(w4, w3);
+    v[1] = cmulf(v[1], w);
+    v[2] = cmulf(v[2], w2);
+    v[3] = cmulf(v[3], w3);
+    v[4] = cmulf(v[4], w4);
+    v[5] = cmulf(v[5], w5);
+    v[6] = cmulf(v[6], w6);
+    v[7] = cmulf(v[7], w7);
+    v[8] = cmulf(v[8], w8);
+    v[9] = cmulf(v[9], cmulf(w8, w));
+    v[10] = cmulf(v[10], cmulf(w8, w2));
+    v[11] = cmulf(v[11], cmulf(w8, w3));
+    v[12] = cmulf(v[12], cmulf(w8, w4));
+    v[13] = cmulf(v[13], cmulf(w8, w5));
+    v[14] = cmulf(v[14], cmulf(w8, w6));
+    v[15] = cmulf(v[15], cmulf(w8, w7));
+}
+
+// Radix-16 Stockham pass over 4096 points (sub-transform length ns = 16 or 256 before it).
+__device__ __forceinline__ void up_pass(const float2* in, float2* out, int ns, const float2* __restrict__ tw_n) {
+    const int j = threadIdx.x;
+    float2 v[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) v[r] = in[up_pad(j + r * (kUpN / 16))];
+    const int k = j & (ns - 1);
+    apply_powers(v, __ldg(tw_n + k * (kUpN / (ns * 16))));   // e^{2 pi i r k / (16 ns)}
+    dft16_inv(v);
+    const int base = (j / ns) * ns * 16 + k;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) out[up_pad(base + r * ns)] = v[r];
+}
+
+__global__ void __launch_bounds__(kUpThreads, 2) upsample_pairs_kernel(
+    const float2* __restrict__ y, const float2* __restrict__ wave, const float2* __restrict__ wfac,
+    const float2* __restrict__ tw_n, const float2* __restrict__ tw_m, float4* __restrict__ pairs, int U, long M,
+    int Lg, long bg0, int first, int linear, int C) {
+    extern __shared__ __align__(16) float2 upsm[];
+    float2* A = upsm;
+    float2* B = upsm + up_pad(kUpN);
+    // span bins bg0 .. bg0 + Lg (mod M), residue-major: bin w of residue r = (bg0 + w) mod U at
+    // stage[r C + w / U], C = 2 (mod 16) so that both the scatter and the pair reads avoid bank conflicts
+    float2* stage = upsm + 2 * up_pad(kUpN);
+    const int t = threadIdx.x;
+    const long s = (long)first + blockIdx.x;
+    // this thread's spectrum values, k' = t + 256 e (FFT order index = k mod N)
+    float2 X[16];
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+        const int kp = t + kUpThreads * e;
+        const float2 yv = y[s * kUpN + ((kp + kUpN / 2) & (kUpN - 1))];
+        const float2 w = __ldg(wave + kp);
+        X[e] = make_float2(w.x * yv.x + w.y * yv.y, w.x * yv.y - w.y * yv.x);
+    }
+    const int bmod = (int)(((bg0 % U) + U) % U);
+    for (int r = 0; r < U; ++r) {
+        // pass 1 straight from registers: X holds the spectrum times e^{2 pi i k r / M} (advanced by
+        // one factor e^{2 pi i k / M} per r, read contiguously), 16-point DFT, ns = 1
+        float2 v[16];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+            v[e] = X[e];
+            const int kp = t + kUpThreads * e;
+            X[e] = cmulf(X[e], __ldg(tw_m + (kp < kUpN / 2 ? kp : M - (kUpN - kp))));
+        }
+        dft16_inv(v);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) A[up_pad(t * 16 + e)] = v[e];
+        __syncthreads();
+        up_pass(A, B, 16, tw_n);
+        __syncthreads();
+        up_pass(B, A, 256, tw_n);
+        __syncthreads();
+        // A holds p(U j + r) at j; keep the span's bins with this residue
+        int w0 = r - bmod;
+        if (w0 < 0) w0 += U;
+        for (int i = t; w0 + U * i <= Lg; i += kUpThreads) {
+            long b = (bg0 + w0 + U * i) % M;
+            if (b < 0) b += M;
+            stage[r * C + i] = A[up_pad((int)(b / U))];
+        }
+        __syncthreads();
+    }
+    const float2 f = __ldg(wfac + s);
+    float4* dst = pairs + s * Lg;
+    for (int w = t; w < Lg; w += kUpThreads) {
+        const int r0 = (bmod + w) % U, r1 = (bmod + w + 1) % U;
+        const float2 a = stage[r0 * C + w / U];
+        const float2 p0 = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
+        float4 o;
+        if (linear) {
+            const float2 c = stage[r1 * C + (w + 1) / U];
+            const float2 p1 = make_float2(c.x * f.x - c.y * f.y, c.x * f.y + c.y * f.x);
+            const float dx = p1.x - p0.x, dy = p1.y - p0.y;
+            o = make_float4(fmaf(0.5f, dx, p0.x), fmaf(0.5f, dy, p0.y), dx, dy);
+        } else {
+            o = make_float4(p0.x, p0.y, 0.f, 0.f);
+        }
+        dst[w] = o;
+    }
+}
+
+// Staging row length: ceil((Lg + 1) / U) rounded up to 2 (mod 16).
+static int up_stage_row(int Lg, int U) {
+    const int n = (Lg + 1 + U - 1) / U;
+    return ((n + 13) & ~15) + 2;
+}
+
+size_t upsample_fused_smem_bytes(int Lg, int U) {
+    return sizeof(float2) * ((size_t)2 * (kUpN + kUpN / 16) + (size_t)U * up_stage_row(Lg, U));
+}
+
+bool upsample_fused_supported(int N, long M, int Lg) {
+    return N == kUpN && M % N == 0 && M / N <= 64 && Lg >= 1 &&
+           upsample_fused_smem_bytes(Lg, (int)(M / N)) <= 112 * 1024;
+}
+
+cudaError_t launch_upsample_pairs_fused(const float2* y, const float2* wave, const float2* wfac, const float2* tw_n,
+                                        const float2* tw_m, float4* pairs, int N, long M, int Lg, long bg0, int rows,
+                                        int first, int linear, cudaStream_t st) {
+    if (!upsample_fused_supported(N, M, Lg) || rows < 1) return cudaErrorInvalidValue;
+    const int U = (int)(M / N);
+    const size_t smem = upsample_fused_smem_bytes(Lg, U);
+    cudaError_t e = cudaFuncSetAttribute(upsample_pairs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    upsample_pairs_kernel<<<rows, kUpThreads, smem, st>>>(y, wave, wfac, tw_n, tw_m, pairs, U, M, Lg, bg0, first,
+                                                          linear, up_stage_row(Lg, U));
+    return cudaGetLastError();
+}
+
 cudaError_t launch_unpack_profiles(const void* spec, int dbl, float2* prof, long M, int Lg, long bg0, int rows,
                                    int first, cudaStream_t st) {
     const dim3 grid((unsigned)((Lg + 255) / 256), (unsigned)rows);

@@ -85,6 +85,14 @@ cudaError_t launch_pack_adjoint(const float2* y, const float2* wave, void* spec,
                                 int first, cudaStream_t st);
 cudaError_t launch_unpack_compact(const float2* compact, int Lc, const float2* wfac, float4* pairs, float2* prof,
                                   long M, int Lg, int rows, int first, int linear, cudaStream_t st);
+// Fused adjoint upsampling for N = 4096 and M a multiple of N: pairs over the stored span straight
+// from the fftshifted phase history (replaces pack + inverse FFT + unpack_pairs); twiddle tables
+// tw_n[q] = e^{2 pi i q / N}, tw_m[q] = e^{2 pi i q / M}.
+bool upsample_fused_supported(int N, long M, int Lg);
+size_t upsample_fused_smem_bytes(int Lg, int U);
+cudaError_t launch_upsample_pairs_fused(const float2* y, const float2* wave, const float2* wfac, const float2* tw_n,
+                                        const float2* tw_m, float4* pairs, int N, long M, int Lg, long bg0, int rows,
+                                        int first, int linear, cudaStream_t st);
 cudaError_t launch_unpack_pairs(const void* spec, int dbl, const float2* wfac, float4* pairs, long M, int Lg,
                                 long bg0, int rows, int first, int linear, cudaStream_t st);
 cudaError_t launch_unpack_profiles(const void* spec, int dbl, float2* prof, long M, int Lg, long bg0, int rows,
