@@ -341,148 +341,15 @@ size_t bp_grid_ws_smem_bytes(int wwin, int pb) {
            4 * sizeof(uint64_t) + 4 * sizeof(df3);
 }
 
-template <bool PRECISE>
-__global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_kernel(const BpGridArgs a) {
-    extern __shared__ __align__(16) float4 smem[];
-    const int pb = a.pb, ww = a.wwin;
-    float4* win0 = smem;
-    float4* coef0 = win0 + 2 * pb * ww;
-    int* base0 = reinterpret_cast<int*>(coef0 + 2 * pb * 4 * kSetF4);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(base0 + 2 * pb);   // full[0..1], empty[2..3]
-    df3* anchors = reinterpret_cast<df3*>(bars + 4);
-
-    const GridConst& g = a.g;
-    // Consecutive CTAs walk a tile column (y fastest): tiles stacked along y see nearly the same
-    // range windows when range runs along x, so concurrent CTAs share profile rows in L2.
-    int tile = blockIdx.x;
-    const int tj = tile % g.tiles_y;
-    tile /= g.tiles_y;
-    const int ti = tile % g.tiles_x;
-    const int k = tile / g.tiles_x;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (threadIdx.x < 4) anchors[threadIdx.x] = subtile_anchor(ti, tj, k, threadIdx.x, g);
-    if (threadIdx.x == 0) {
-        mbar_init(&bars[0], kWsProducers);
-        mbar_init(&bars[1], kWsProducers);
-        mbar_init(&bars[2], kWsConsumers / 32);
-        mbar_init(&bars[3], kWsConsumers / 32);
-        mbar_fence_init();
-    }
-    __syncthreads();
-    const int nst = (a.S + pb - 1) / pb;
-
-    if (warp >= kWsConsumers / 32) {
-        // ----------------------------------------------------------- producers
-        const int pw = warp - kWsConsumers / 32;
-        bool ok = true;
-        int issued = 0;
-        for (int st = 0; st < nst; ++st) {
-            const int b = st & 1;
-            if (st >= 2 && !mbar_wait(&bars[2 + b], ((st - 2) >> 1) & 1, 128, 2048)) {
-                ok = false;
-                break;
-            }
-            const int s0 = st * pb, npb = min(pb, a.S - s0);
-            float4* coef = coef0 + b * pb * 4 * kSetF4;
-            int* base = base0 + b * pb;
-            int mine = 0;   // pulses of this stage staged by this warp
-            for (int pass = 8 * pw; pass < npb; pass += 8 * kWsProducers) {
-                producer_coeffs(g, a.pulses, s0, npb, pass, anchors, coef, base, lane);
-                mine += min(8, npb - pass);
-            }
-            __syncwarp();
-            if (lane == 0) mbar_arrive_expect_tx(&bars[b], (uint32_t)(mine * ww * sizeof(float4)));
-            for (int pass = 8 * pw; pass < npb; pass += 8 * kWsProducers) {
-                const int pi = pass + lane;
-                if (lane < 8 && pi < npb) {
-                    long gi = (long)base[pi] - ww / 2 - a.bg0;
-                    if (gi < 0 || gi > (long)a.Lg - ww) {
-                        raise_flag(a.flags, FLAG_TILE_WINDOW);
-                        gi = gi < 0 ? 0 : (long)a.Lg - ww;
-                    }
-                    fence_proxy_async_smem();
-                    bulk_g2s(win0 + (size_t)(b * pb + pi) * ww, a.pairs + (size_t)(s0 + pi) * a.Lg + gi,
-                             (uint32_t)(ww * sizeof(float4)), &bars[b]);
-                }
-            }
-            issued = st + 1;
-        }
-        // Do not leave while this warp's copies may still be landing (bounded).
-        for (int st = max(0, issued - 2); st < issued; ++st)
-            if (!mbar_wait(&bars[st & 1], (st >> 1) & 1, 128, 2048)) ok = false;
-        if (!ok && lane == 0) raise_flag(a.flags, FLAG_WAIT_TIMEOUT);
-        return;
-    }
-
-    // -------------------------------------------------------------- consumers
-    const TileThread tt = tile_thread();
-    float acc_re[4] = {0.f, 0.f, 0.f, 0.f}, acc_im[4] = {0.f, 0.f, 0.f, 0.f};
-    const int half_w = ww / 2;
-    bool ok = true;
-    for (int st = 0; st < nst; ++st) {
-        const int b = st & 1;
-        if (!mbar_wait(&bars[b], (st >> 1) & 1, 32, 256)) {
-            ok = false;
-            break;
-        }
-        const int npb = min(pb, a.S - st * pb);
-        const float4* coef = coef0 + b * pb * 4 * kSetF4;
-        const float4* win = win0 + (size_t)b * pb * ww;
-        float st_re[4] = {0.f, 0.f, 0.f, 0.f}, st_im[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll 2
-        for (int pi = 0; pi < npb; ++pi) {
-            float c9, w9, ib;
-            const ColumnTerms ct = load_column<PRECISE>(coef + (pi * 4 + tt.q) * kSetF4, tt, c9, w9, ib);
-            const float4* wp = win + pi * ww;
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                const PixelEval e = eval_pixel<PRECISE>(ct, c9, w9, ib, tt, r);
-                const unsigned idx = min((unsigned)(e.n + half_w), (unsigned)(ww - 1));
-                const float4 pv = wp[idx];
-                const float re = fmaf(e.sf, pv.z, pv.x);
-                const float im = fmaf(e.sf, pv.w, pv.y);
-                float sn, cn;
-                __sincosf(SAR_TWO_PI * e.f, &sn, &cn);
-                st_re[r] = fmaf(re, cn, fmaf(im, sn, st_re[r]));
-                st_im[r] = fmaf(im, cn, fmaf(-re, sn, st_im[r]));
-            }
-        }
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            acc_re[r] += st_re[r];
-            acc_im[r] += st_im[r];
-        }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&bars[2 + b]);
-    }
-    if (!ok) {
-        if (lane == 0) raise_flag(a.flags, FLAG_WAIT_TIMEOUT);
-        return;
-    }
-    const int i = ti * kTile + lane;
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        const int j = tj * kTile + 4 * warp + r;
-        if (i < g.nx && j < g.ny) {
-            const size_t p = ((size_t)k * g.ny + j) * g.nx + i;
-            float2 o = make_float2(acc_re[r], acc_im[r]);
-            if (a.accumulate) {
-                const float2 old = a.x[p];
-                o.x += old.x;
-                o.y += old.y;
-            }
-            a.x[p] = o;
-        }
-    }
-}
-
-// ------------------------------------- K2, linear bins: two pulses per packed instruction
+// ------------------------------------------- K2: two pulses per packed instruction
 // The same pipeline with the consumers' arithmetic on FP32 pairs (fma.rn.f32x2 and friends,
 // one instruction for two values, each rounded as the scalar operation): the two values are
 // the same pixel for two consecutive pulses p (even) and p + 1.  Coefficient sets are stored
 // pair-interleaved, kSetF4 * 2 float4 per (pulse pair, sub-tile):
 //   [c0 c0' c1 c1'] [c2 c2' c3 c3'] [c4 c4' c5 c5'] [c6 c6' c7 c7'] [c8 c8' c9 c9']
-//   [v0 v0' v1 v1'] [v2 v2' v3 v3'] [v4 v4' v5 v5']  (primed: pulse p + 1; 4 float4 unused)
+//   [v0 v0' v1 v1'] [v2 v2' v3 v3'] [v4 v4' v5 v5']
+//   [ia ia' ib ib'] [w0 w0' w1 w1'] [w2 w2' w3 w3'] [i0 i0' - -]  (primed: pulse p + 1; the last
+//   four only read with split bins: nearest-bin modes and windows wider than 256 bins)
 // so that each half of a 16-byte shared-memory load is one operand pair.  Per pixel the
 // polynomials are evaluated in Horner form in the row offset dj (the only per-row constant a
 // thread keeps), the phase is reduced to [-0.5, 0.5] cycles with the 1.5 * 2^23 shifter
@@ -517,10 +384,11 @@ __device__ __forceinline__ void producer_coeffs_pair(const GridConst& g, const P
     if (valid) bin_coeffs(ae, vb, b, g, co);
     if (valid || pad) {   // the padding pulse stores zeros (co = {})
         float* dst = reinterpret_cast<float*>(coef + ((pi >> 1) * 4 + q) * (2 * kSetF4)) + (pi & 1);
-        const float vals[16] = {co.c[0], co.c[1], co.c[2], co.c[3], co.c[4], co.c[5], co.c[6], co.c[7],
-                                co.c[8], co.c[9], co.v[0], co.v[1], co.v[2], co.v[3], co.v[4], co.v[5]};
+        const float vals[24] = {co.c[0], co.c[1], co.c[2], co.c[3], co.c[4], co.c[5], co.c[6], co.c[7],
+                                co.c[8], co.c[9], co.v[0], co.v[1], co.v[2], co.v[3], co.v[4], co.v[5],
+                                co.ia,   co.ib,   co.w[0], co.w[1], co.w[2], co.w[3], co.i0,   0.f};
 #pragma unroll
-        for (int k = 0; k < 16; ++k) dst[2 * k] = vals[k];
+        for (int k = 0; k < 24; ++k) dst[2 * k] = vals[k];
         if (valid && q == 0) base[pi] = b;
     }
 }
@@ -530,7 +398,7 @@ __device__ __forceinline__ void producer_coeffs_pair(const GridConst& g, const P
 // terms in di).  A quarter-warp's eight 16-byte window loads are conflict-free when they fall
 // in distinct 16-byte bank groups or on the same bin; lanes along the axis where bins change
 // slowly (cross-range) make them land on one or two bins.
-template <bool LANES_Y>
+template <bool LANES_Y, bool PRECISE>
 __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const BpGridArgs a) {
     extern __shared__ __align__(16) float4 smem[];
     const int pb = a.pb, ww = a.wwin;
@@ -644,22 +512,47 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
             // v = cv + bv1 d + bv2 d^2 in the offset d along the warp's axis (sar_geom.cuh Coeffs:
             // c0..c9 = A.xy A.zw B.xy B.zw C.xy C.zw D.xy D.zw E.xy E.zw, v0..v5 = F.xy .. H.zw).
             float2 cph, b1, b2, c9, cv, bv1, bv2;
+            float2 vtop = f2(0.f, 0.f), ci = f2(0.f, 0.f), cid = f2(0.f, 0.f);   // split-bin terms
+            if (PRECISE) {
+                // v also has the cubic monomials w0 di^3 + w1 di^2 dj + w2 di dj^2 + w3 dj^3 and an
+                // exact integer part i0 + ia di + ib dj (I = [ia ib], J = [w0 w1], K = [w2 w3], L = [i0])
+                const float4 I = cs[8], J = cs[9], K = cs[10], L = cs[11];
+                if (LANES_Y) {   // u = dj, d = di
+                    cv = fma2(f2(K.z, K.w), U3, fma2(f2(H.z, H.w), U2, fma2(f2(G.x, G.y), U1, f2(F.x, F.y))));
+                    bv1 = fma2(f2(K.x, K.y), U2, fma2(f2(H.x, H.y), U1, f2(F.z, F.w)));
+                    bv2 = fma2(f2(J.z, J.w), U1, f2(G.z, G.w));
+                    vtop = f2(J.x, J.y);
+                    ci = fma2(f2(I.z, I.w), U1, f2(L.x, L.y));
+                    cid = f2(I.x, I.y);
+                } else {         // u = di, d = dj
+                    cv = fma2(f2(J.x, J.y), U3, fma2(f2(G.z, G.w), U2, fma2(f2(F.z, F.w), U1, f2(F.x, F.y))));
+                    bv1 = fma2(f2(J.z, J.w), U2, fma2(f2(H.x, H.y), U1, f2(G.x, G.y)));
+                    bv2 = fma2(f2(K.x, K.y), U1, f2(H.z, H.w));
+                    vtop = f2(K.z, K.w);
+                    ci = fma2(f2(I.x, I.y), U1, f2(L.x, L.y));
+                    cid = f2(I.z, I.w);
+                }
+            }
             if (LANES_Y) {   // u = dj, d = di
                 cph = fma2(f2(E.z, E.w), U3, fma2(f2(C.z, C.w), U2, fma2(f2(B.x, B.y), U1, f2(A.x, A.y))));
                 b1 = fma2(f2(E.x, E.y), U2, fma2(f2(C.x, C.y), U1, f2(A.z, A.w)));
                 b2 = fma2(f2(D.z, D.w), U1, f2(B.z, B.w));
                 c9 = f2(D.x, D.y);
-                cv = fma2(f2(H.z, H.w), U2, fma2(f2(G.x, G.y), U1, f2(F.x, F.y)));
-                bv1 = fma2(f2(H.x, H.y), U1, f2(F.z, F.w));
-                bv2 = f2(G.z, G.w);
+                if (!PRECISE) {
+                    cv = fma2(f2(H.z, H.w), U2, fma2(f2(G.x, G.y), U1, f2(F.x, F.y)));
+                    bv1 = fma2(f2(H.x, H.y), U1, f2(F.z, F.w));
+                    bv2 = f2(G.z, G.w);
+                }
             } else {         // u = di, d = dj (as column_terms, linear bins)
                 cph = fma2(f2(D.x, D.y), U3, fma2(f2(B.z, B.w), U2, fma2(f2(A.z, A.w), U1, f2(A.x, A.y))));
                 b1 = fma2(f2(D.z, D.w), U2, fma2(f2(C.x, C.y), U1, f2(B.x, B.y)));
                 b2 = fma2(f2(E.x, E.y), U1, f2(C.z, C.w));
                 c9 = f2(E.z, E.w);
-                cv = fma2(f2(G.z, G.w), U2, fma2(f2(F.z, F.w), U1, f2(F.x, F.y)));
-                bv1 = fma2(f2(H.x, H.y), U1, f2(G.x, G.y));
-                bv2 = f2(H.z, H.w);
+                if (!PRECISE) {
+                    cv = fma2(f2(G.z, G.w), U2, fma2(f2(F.z, F.w), U1, f2(F.x, F.y)));
+                    bv1 = fma2(f2(H.x, H.y), U1, f2(G.x, G.y));
+                    bv2 = f2(H.z, H.w);
+                }
             }
             const float4* wa = win + (size_t)(2 * pp) * ww;
             const float4* wb = wa + ww;
@@ -668,9 +561,10 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
                 const float2 d = DU[r];
                 const float2 ph = fma2(fma2(fma2(c9, d, b2), d, b1), d, cph);
                 const float2 f = fma2(f2(rintf(ph.x), rintf(ph.y)), M1, ph);   // ph - rint(ph), exact
-                const float2 v = fma2(fma2(bv2, d, bv1), d, cv);
-                const float2 r1 = add2(v, SH);
+                const float2 v = PRECISE ? fma2(fma2(fma2(vtop, d, bv2), d, bv1), d, cv) : fma2(fma2(bv2, d, bv1), d, cv);
+                float2 r1 = add2(v, SH);
                 const float2 s = fma2(add2(r1, NSH), M1, v);               // v - rint(v), exact
+                if (PRECISE) r1 = add2(r1, fma2(cid, d, ci));              // + the exact integer part
                 const unsigned ia = min((unsigned)(__float_as_int(r1.x) + idx_bias), idx_max);
                 const unsigned ib = min((unsigned)(__float_as_int(r1.y) + idx_bias), idx_max);
                 const float4 pa = wa[ia], pq = wb[ib];
@@ -718,19 +612,17 @@ cudaError_t launch_bp_grid_ws(const BpGridArgs& a, cudaStream_t st) {
     const size_t smem = bp_grid_ws_smem_bytes(a.wwin, a.pb);
     const unsigned blocks = (unsigned)(a.g.tiles_x * a.g.tiles_y * a.g.nz);
     cudaError_t e;
-    if (a.g.precise_bins) {
-        e = cudaFuncSetAttribute(bp_grid_ws_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        bp_grid_ws_kernel<true><<<blocks, kWsThreads, smem, st>>>(a);
-    } else if (a.lanes_y) {
-        e = cudaFuncSetAttribute(bp_grid_ws_pair_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        bp_grid_ws_pair_kernel<true><<<blocks, kWsThreads, smem, st>>>(a);
-    } else {
-        e = cudaFuncSetAttribute(bp_grid_ws_pair_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        bp_grid_ws_pair_kernel<false><<<blocks, kWsThreads, smem, st>>>(a);
-    }
+    auto go = [&](auto kernel) -> cudaError_t {
+        cudaError_t err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return err;
+        kernel<<<blocks, kWsThreads, smem, st>>>(a);
+        return cudaSuccess;
+    };
+    if (a.g.precise_bins)
+        e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, true>) : go(bp_grid_ws_pair_kernel<false, true>);
+    else
+        e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, false>) : go(bp_grid_ws_pair_kernel<false, false>);
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
