@@ -243,7 +243,10 @@ def run_ours(args):
                 "h2d_bytes_per_step": S * N * 8, "d2h_bytes_per_step": P * 8,
                 "api": "NumpySimpleSarOperator.backproject(pinned host complex64 tensor) -> pinned host copy"},
         # our kernels per call: pack + unpack per FFT chunk, then the gather (cuFFT's own excluded)
-        "gpu_launches": args.steps * (2 * ((S + plan_chunk(plan) - 1) // plan_chunk(plan)) + 1),
+        # our kernels per backprojection: per FFT chunk the fused upsampling kernel, or the packing
+        # and unpacking kernels around cuFFT; then the gather
+        "gpu_launches": args.steps * ((1 if plan.fused_upsampling else 2)
+                                      * ((S + plan_chunk(plan) - 1) // plan_chunk(plan)) + 1),
         "clocks": clocks,
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
