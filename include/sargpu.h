@@ -333,6 +333,15 @@ int sar_device_flags(sar_plan *plan, unsigned *flags);
 int sar_adjoint_from_profiles_noalloc(const sar_geometry *geom, const void *prof_dev, long first_bin,
                                       size_t span, void *x_dev, void *stream);
 
+/* Device address of page-locked, mapped host memory (cudaHostGetDevicePointer), for passing a
+ * pinned host buffer to a call that reads it on the device -- e.g. the phase history of
+ * sar_adjoint when the plan uses the fused upsampling (sar_plan_info.fused_upsampling), which
+ * then reads y over the host link inside its transform instead of after a copy.  Such a buffer
+ * must stay unchanged until the stream has passed the call.  SAR_ERR_INVALID_ARGUMENT when the
+ * device cannot address the memory (on systems whose GPU translates host page tables, e.g. over a
+ * chip-to-chip link, pageable memory is addressable too and comes back at its host address). */
+int sar_host_device_pointer(const void *host_ptr, void **dev_ptr);
+
 /* Last error message of the calling thread (empty if none); returns its full length. */
 size_t sar_last_error(char *buf, size_t len);
 const char *sar_status_string(int status);

@@ -30,7 +30,7 @@ EXPORTED = (
     "sar_device_flags", "sar_last_error", "sar_status_string",
     "sar_enable_stage_timing", "sar_stage_times",
     "sar_adjoint_from_profiles_noalloc", "sar_phase_gradient", "sar_sharpness", "sar_cgls", "sar_cgls_ex", "sar_adjoint_pulse_block",
-    "sar_move_srps", "sar_fast_freq_downsample", "sar_resample_phase_history", "sar_cphd_decode", "sar_pdhg",
+    "sar_move_srps", "sar_fast_freq_downsample", "sar_resample_phase_history", "sar_cphd_decode", "sar_pdhg", "sar_host_device_pointer",
     "sar_unet_create", "sar_unet_destroy", "sar_unet_info", "sar_unet_set_params", "sar_unet_get_params",
     "sar_unet_get_grads", "sar_unet_zero_grad", "sar_unet_forward", "sar_unet_backward", "sar_unet_adam_step",
     "sar_unet_flags", "sar_conv2d_forward_bf16", "sar_conv2d_wgrad_bf16",
@@ -138,6 +138,8 @@ def load() -> ctypes.CDLL:
     lib.sar_pdhg.argtypes = [c_void_p, c_void_p, c_void_p, c_int, c_int, c_double, c_double, c_double, c_double,
                              c_int, c_void_p, POINTER(SarPdhgResult), c_void_p]
     lib.sar_pdhg.restype = c_int
+    lib.sar_host_device_pointer.argtypes = [c_void_p, ctypes.POINTER(c_void_p)]
+    lib.sar_host_device_pointer.restype = c_int
     lib.sar_adjoint_pulse_block.argtypes = [c_void_p, c_void_p, c_size_t, c_size_t, c_void_p, c_int, c_void_p]
     lib.sar_adjoint_pulse_block.restype = c_int
     lib.sar_move_srps.argtypes = [c_void_p, c_void_p, c_size_t, c_size_t, c_void_p, c_double, c_double, c_double,

@@ -694,6 +694,19 @@ size_t sar_last_error(char* buf, size_t len) {
     return g_last_error.size();
 }
 
+int sar_host_device_pointer(const void* host_ptr, void** dev_ptr) {
+    if (!host_ptr || !dev_ptr) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    *dev_ptr = nullptr;
+    void* d = nullptr;
+    const cudaError_t e = cudaHostGetDevicePointer(&d, const_cast<void*>(host_ptr), 0);
+    if (e != cudaSuccess || !d) {
+        cudaGetLastError();   // not addressable by the device: not an error for the caller's context
+        return fail(SAR_ERR_INVALID_ARGUMENT, "host memory is not addressable by the device");
+    }
+    *dev_ptr = d;
+    return SAR_OK;
+}
+
 int sar_plan_create(const sar_geometry* geom, int device, sar_plan** plan_out) {
     g_last_error.clear();
     if (!geom || !plan_out) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");

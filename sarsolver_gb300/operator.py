@@ -58,7 +58,10 @@ class NumpySimpleSarOperator(LinearOperator):
         return self.plan.forward(_to_device(x, self.plan.device).reshape(-1))
 
     def backproject(self, y) -> torch.Tensor:
-        """A^H y for a tensor (any device); returns complex64 [P] on the plan's device."""
+        """A^H y for a tensor (any device); returns complex64 [P] on the plan's device.  A pinned
+        host tensor is read by the device in place where the plan allows it (``SarPlan.adjoint_host``)."""
+        if isinstance(y, torch.Tensor) and y.device.type == "cpu" and y.is_pinned():
+            return self.plan.adjoint_host(y)
         return self.plan.adjoint(_to_device(y, self.plan.device).reshape(-1))
 
     # scipy API ------------------------------------------------------------

@@ -159,6 +159,26 @@ class SarPlan:
                                              ctypes.c_void_p(x.data_ptr()), self._stream()), "sar_adjoint")
         return x
 
+    def adjoint_host(self, y_host: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        """x = A^H y with y in host memory.  When the plan uses the fused upsampling and y is a
+        pinned (page-locked, mapped) contiguous complex64 tensor, the upsampling kernel reads y over
+        the host link itself, so the transfer overlaps the transform instead of preceding it; the
+        call returns after the device is done with y (the stream is synchronised).  Otherwise y is
+        copied to the device first."""
+        n = self.num_slow_times * self.num_freqs
+        if (self.fused_upsampling and isinstance(y_host, torch.Tensor) and y_host.device.type == "cpu"
+                and y_host.dtype == torch.complex64 and y_host.numel() == n and y_host.is_contiguous()
+                and not y_host.is_conj() and not y_host.is_neg() and y_host.is_pinned()):
+            dev_ptr = ctypes.c_void_p()
+            if self._lib.sar_host_device_pointer(ctypes.c_void_p(y_host.data_ptr()), ctypes.byref(dev_ptr)) == 0:
+                x = self._check_out(out, (self.num_scatterers,), "out")
+                with torch.cuda.device(self.device):
+                    _lib.check(self._lib.sar_adjoint(self._handle, dev_ptr, ctypes.c_void_p(x.data_ptr()),
+                                                     self._stream()), "sar_adjoint")
+                    torch.cuda.current_stream(self.device).synchronize()
+                return x
+        return self.adjoint(y_host, out)
+
     def adjoint_streamed(self, y_host: torch.Tensor, block: int = 512, out: Optional[torch.Tensor] = None) -> torch.Tensor:
         """x = A^H y with y in host memory (pin it for overlap), streamed through the device in
         blocks of ``block`` pulses: block b + 1 is copied on a side stream while block b is

@@ -160,6 +160,32 @@ def test_fused_upsampling_matches_oracle(mode, srp_shift):
     assert plan.device_flags() == 0
 
 
+def test_backproject_reads_pinned_host_input_in_place():
+    """With the fused upsampling a pinned host phase history is read by the device directly
+    (sar_host_device_pointer + sar_adjoint); the image equals the device-input one bit for bit,
+    as does the copy path for pageable memory, and the call returns only when y may be reused."""
+    rng = np.random.default_rng(8)
+    case = spotlight_case(40, 4096, 40, 0.5, 3.0)
+    op = NumpySimpleSarOperator(case.scene, case.aperture, upsample_ratio=8.0, interp="linear")
+    assert op.plan.fused_upsampling
+    y = crandn(rng, 40, 4096).astype(np.complex64)
+    ref = op.plan.adjoint(torch.from_numpy(y).cuda())
+    yp = torch.from_numpy(y.copy()).pin_memory()
+    lib = _lib.load()
+    dev = ctypes.c_void_p()
+    assert lib.sar_host_device_pointer(ctypes.c_void_p(yp.data_ptr()), ctypes.byref(dev)) == 0 and dev.value
+    x_pinned = op.backproject(yp)
+    yp.zero_()   # y may be reused once the call has returned
+    assert torch.equal(x_pinned, ref)
+    assert torch.equal(op.backproject(torch.from_numpy(y.copy())), ref)   # pageable: copied first
+    # pageable memory: refused where the device cannot address it, the same address where it can
+    # (address translation over the chip-to-chip link); the operator reads only pinned tensors in place
+    page = np.zeros(4, np.complex64)
+    rc = lib.sar_host_device_pointer(ctypes.c_void_p(page.ctypes.data), ctypes.byref(dev))
+    assert rc == _lib.SAR_ERR_INVALID_ARGUMENT or (rc == 0 and dev.value == page.ctypes.data)
+    assert op.plan.device_flags() == 0
+
+
 @pytest.mark.parametrize("kind", ["grid", "points", "bistatic"])
 def test_dot_product_adjoint(kind):
     rng = np.random.default_rng(2)
