@@ -764,12 +764,86 @@ __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, 
     }
 }
 
+// MODE 3 (linear bins): the producer has shown that a sub-tile's bin is monotonic down its 16
+// rows and moves by less than kRunSpan, so a lane's bin takes at most two values n0, n0 + 1 over
+// the half (n0 = the smaller of the bins at rows 0 and 15) and its taps lie in n0 .. n0 + 2.  The
+// lane accumulates those three bins in registers for both pulses and adds them to the windows
+// once per half, in three phases (lanes' bins are distinct at any one row, MODE >= 1), instead of
+// two read-modify-writes per contribution.
+constexpr float kRunSpan = 0.98f;
+
+template <bool TWO>
+__device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float c9p, const ColumnTerms& ctq, float c9q,
+                                                  const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
+                                                  int ws, int lane) {
+    const float2 cph = f2(ctp.cph, ctq.cph), b1 = f2(ctp.b1, ctq.b1), b2 = f2(ctp.b2, ctq.b2), c9 = f2(c9p, c9q);
+    const float2 cv = f2(ctp.cv, ctq.cv), bv1 = f2(ctp.bv1, ctq.bv1), bv2 = f2(ctp.bv2, ctq.bv2);
+    const float2 SH = f2(SAR_SHIFTER, SAR_SHIFTER), NSH = f2(-SAR_SHIFTER, -SAR_SHIFTER);
+    const float2 M1 = f2(-1.f, -1.f), TWO_PI2 = f2(SAR_TWO_PI, SAR_TWO_PI), HALF = f2(0.5f, 0.5f);
+    // window slot n0 of each pulse: the smaller bin of rows 0 and 15
+    int n0p, n0q;
+    {
+        const float2 da = f2(-8.f, -8.f), db = f2(7.f, 7.f);
+        const float2 ra = add2(fma2(fma2(bv2, da, bv1), da, cv), SH);
+        const float2 rb = add2(fma2(fma2(bv2, db, bv1), db, cv), SH);
+        n0p = min(max(min(__float_as_int(ra.x), __float_as_int(rb.x)) - SAR_SHIFTER_BITS + off_p, 0), ws - 3);
+        n0q = min(max(min(__float_as_int(ra.y), __float_as_int(rb.y)) - SAR_SHIFTER_BITS + off_q, 0), ws - 3);
+    }
+    const int hp = n0p - off_p + SAR_SHIFTER_BITS, hq = n0q - off_q + SAR_SHIFTER_BITS;   // bits of bin n0
+    float ap[3][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, aq[3][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll 4
+    for (int rr = 0; rr < 16; ++rr) {
+        const float dj = (float)(rr - 8);
+        const float2 d = f2(dj, dj);
+        const float2 xv = xrow[rr * kTile + lane];
+        const float2 ph = fma2(fma2(fma2(c9, d, b2), d, b1), d, cph);
+        const float2 f = fma2(f2(rintf(ph.x), rintf(ph.y)), M1, ph);   // ph - rint(ph), exact
+        const float2 v = fma2(fma2(bv2, d, bv1), d, cv);
+        const float2 r1 = add2(v, SH);
+        const float2 sv = fma2(add2(r1, NSH), M1, v);                   // v - rint(v), exact
+        const float2 x = mul2(f, TWO_PI2);
+        float2 sn, cn;
+        __sincosf(x.x, &sn.x, &cn.x);
+        __sincosf(x.y, &sn.y, &cn.y);
+        const float2 w0 = fma2(sv, M1, HALF), w1 = add2(HALF, sv);      // taps n and n + 1
+        // c = x exp(+2 pi i f) for both pulses
+        const float crp = fmaf(xv.x, cn.x, -xv.y * sn.x), cip = fmaf(xv.x, sn.x, xv.y * cn.x);
+        {
+            const bool up = __float_as_int(r1.x) != hp;                 // n = n0 + 1
+            const float a0 = up ? 0.f : w0.x, a1 = up ? w0.x : w1.x, a2 = up ? w1.x : 0.f;
+            ap[0][0] = fmaf(a0, crp, ap[0][0]); ap[0][1] = fmaf(a0, cip, ap[0][1]);
+            ap[1][0] = fmaf(a1, crp, ap[1][0]); ap[1][1] = fmaf(a1, cip, ap[1][1]);
+            ap[2][0] = fmaf(a2, crp, ap[2][0]); ap[2][1] = fmaf(a2, cip, ap[2][1]);
+        }
+        if (TWO) {
+            const float crq = fmaf(xv.x, cn.y, -xv.y * sn.y), ciq = fmaf(xv.x, sn.y, xv.y * cn.y);
+            const bool up = __float_as_int(r1.y) != hq;
+            const float a0 = up ? 0.f : w0.y, a1 = up ? w0.y : w1.y, a2 = up ? w1.y : 0.f;
+            aq[0][0] = fmaf(a0, crq, aq[0][0]); aq[0][1] = fmaf(a0, ciq, aq[0][1]);
+            aq[1][0] = fmaf(a1, crq, aq[1][0]); aq[1][1] = fmaf(a1, ciq, aq[1][1]);
+            aq[2][0] = fmaf(a2, crq, aq[2][0]); aq[2][1] = fmaf(a2, ciq, aq[2][1]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        rmw_add(wp, n0p + j, 1.0f, ap[j][0], ap[j][1]);
+        if (TWO) rmw_add(wq, n0q + j, 1.0f, aq[j][0], aq[j][1]);
+        __syncwarp();
+    }
+}
+
 template <bool LINEAR, bool PRECISE, bool TWO>
 __device__ __forceinline__ void scatter_half(int mode, const ColumnTerms& ctp, float c9p, float w9p, float ibp,
                                              const ColumnTerms& ctq, float c9q, float w9q, float ibq,
                                              const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
                                              int ws, int lane) {
-    if (mode == 2)
+    if constexpr (LINEAR && !PRECISE) {
+        if (mode == 3) {
+            scatter_rows_runs<TWO>(ctp, c9p, ctq, c9q, xrow, wp, wq, off_p, off_q, ws, lane);
+            return;
+        }
+    }
+    if (mode >= 2)
         scatter_rows<LINEAR, PRECISE, 2, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane);
     else if (mode == 1)
         scatter_rows<LINEAR, PRECISE, 1, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane);
@@ -847,7 +921,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                 // The rate must also have one sign in all four sub-tiles, so that bins along a
                 // row are monotonic across the sub-tile boundary.
                 const int pi = pass + (lane >> 2), q = lane & 3;
-                bool ok_q = true, wide_q = true, pos_q = true;
+                bool ok_q = true, wide_q = true, pos_q = true, runs_q = true;
                 if (pi < npb) {
                     const float4* cs = coef + (pi * 4 + q) * kSetF4;
                     const float4 C = cs[2], D = cs[3], E = cs[4];
@@ -856,15 +930,23 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                     ok_q = rmin >= kFastBinRate;
                     wide_q = rmin >= kFastBinRate + 1.0f;
                     pos_q = r1 > 0.0f;
+                    // bin down the 16 rows of the sub-tile: monotonic (dv/dj = v2 + v4 di + 2 v5 dj keeps
+                    // its sign) and changing by less than kRunSpan in all
+                    const float curv = 8.0f * fabsf(D.z) + 16.0f * fabsf(D.w);
+                    runs_q = fabsf(D.x) > curv && 15.0f * (fabsf(D.x) + curv) < kRunSpan;
                 }
                 const unsigned all4 = __ballot_sync(0xffffffffu, ok_q);
                 const unsigned wide4 = __ballot_sync(0xffffffffu, wide_q);
                 const unsigned pos4 = __ballot_sync(0xffffffffu, pos_q);
+                const unsigned runs4 = __ballot_sync(0xffffffffu, runs_q);
                 const unsigned grp = lane & ~3;
                 const unsigned sgn = (pos4 >> grp) & 0xFu;
                 const bool mono = sgn == 0xFu || sgn == 0u;
-                if (pi < npb && q == 0)
-                    fast[pi] = !mono ? 0 : (((wide4 >> grp) & 0xFu) == 0xFu ? 2 : (((all4 >> grp) & 0xFu) == 0xFu ? 1 : 0));
+                if (pi < npb && q == 0) {
+                    int m = !mono ? 0 : (((wide4 >> grp) & 0xFu) == 0xFu ? 2 : (((all4 >> grp) & 0xFu) == 0xFu ? 1 : 0));
+                    if (LINEAR && !PRECISE && m >= 1 && ((runs4 >> grp) & 0xFu) == 0xFu) m = 3;
+                    fast[pi] = m;
+                }
             }
             __syncwarp();
             if (lane == 0) mbar_arrive(&bars[b]);
