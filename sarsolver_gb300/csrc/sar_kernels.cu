@@ -764,15 +764,16 @@ __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, 
     }
 }
 
-// MODE 3 (linear bins): the producer has shown that a sub-tile's bin is monotonic down its 16
-// rows and moves by less than kRunSpan, so a lane's bin takes at most two values n0, n0 + 1 over
-// the half (n0 = the smaller of the bins at rows 0 and 15) and its taps lie in n0 .. n0 + 2.  The
-// lane accumulates those three bins in registers for both pulses and adds them to the windows
-// once per half, in three phases (lanes' bins are distinct at any one row, MODE >= 1), instead of
-// two read-modify-writes per contribution.
+// MODES 4 and 3 (linear bins): the producer has shown that a sub-tile's bin is monotonic down its
+// rows and moves by less than kRunSpan over G = 16 (MODE 4) or G = 8 (MODE 3) rows, so in each
+// group of G rows a lane's bin takes at most two values n0, n0 + 1 (n0 = the smaller of the bins
+// at the group's first and last rows) and its taps lie in n0 .. n0 + 2.  The lane accumulates
+// those three bins in registers for both pulses and adds them to the windows once per group, in
+// three phases (lanes' bins are distinct at any one row, MODE >= 1), instead of two
+// read-modify-writes per contribution.
 constexpr float kRunSpan = 0.98f;
 
-template <bool TWO>
+template <bool TWO, int G>
 __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float c9p, const ColumnTerms& ctq, float c9q,
                                                   const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
                                                   int ws, int lane) {
@@ -780,10 +781,12 @@ __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float 
     const float2 cv = f2(ctp.cv, ctq.cv), bv1 = f2(ctp.bv1, ctq.bv1), bv2 = f2(ctp.bv2, ctq.bv2);
     const float2 SH = f2(SAR_SHIFTER, SAR_SHIFTER), NSH = f2(-SAR_SHIFTER, -SAR_SHIFTER);
     const float2 M1 = f2(-1.f, -1.f), TWO_PI2 = f2(SAR_TWO_PI, SAR_TWO_PI), HALF = f2(0.5f, 0.5f);
-    // window slot n0 of each pulse: the smaller bin of rows 0 and 15
+#pragma unroll
+  for (int g0 = 0; g0 < 16; g0 += G) {
+    // window slot n0 of each pulse: the smaller bin of the group's first and last rows
     int n0p, n0q;
     {
-        const float2 da = f2(-8.f, -8.f), db = f2(7.f, 7.f);
+        const float2 da = f2((float)(g0 - 8), (float)(g0 - 8)), db = f2((float)(g0 + G - 9), (float)(g0 + G - 9));
         const float2 ra = add2(fma2(fma2(bv2, da, bv1), da, cv), SH);
         const float2 rb = add2(fma2(fma2(bv2, db, bv1), db, cv), SH);
         n0p = min(max(min(__float_as_int(ra.x), __float_as_int(rb.x)) - SAR_SHIFTER_BITS + off_p, 0), ws - 3);
@@ -792,7 +795,7 @@ __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float 
     const int hp = n0p - off_p + SAR_SHIFTER_BITS, hq = n0q - off_q + SAR_SHIFTER_BITS;   // bits of bin n0
     float ap[3][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, aq[3][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
 #pragma unroll 4
-    for (int rr = 0; rr < 16; ++rr) {
+    for (int rr = g0; rr < g0 + G; ++rr) {
         const float dj = (float)(rr - 8);
         const float2 d = f2(dj, dj);
         const float2 xv = xrow[rr * kTile + lane];
@@ -830,6 +833,7 @@ __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float 
         if (TWO) rmw_add(wq, n0q + j, 1.0f, aq[j][0], aq[j][1]);
         __syncwarp();
     }
+  }
 }
 
 template <bool LINEAR, bool PRECISE, bool TWO>
@@ -838,8 +842,12 @@ __device__ __forceinline__ void scatter_half(int mode, const ColumnTerms& ctp, f
                                              const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
                                              int ws, int lane) {
     if constexpr (LINEAR && !PRECISE) {
+        if (mode == 4) {
+            scatter_rows_runs<TWO, 16>(ctp, c9p, ctq, c9q, xrow, wp, wq, off_p, off_q, ws, lane);
+            return;
+        }
         if (mode == 3) {
-            scatter_rows_runs<TWO>(ctp, c9p, ctq, c9q, xrow, wp, wq, off_p, off_q, ws, lane);
+            scatter_rows_runs<TWO, 8>(ctp, c9p, ctq, c9q, xrow, wp, wq, off_p, off_q, ws, lane);
             return;
         }
     }
@@ -921,7 +929,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                 // The rate must also have one sign in all four sub-tiles, so that bins along a
                 // row are monotonic across the sub-tile boundary.
                 const int pi = pass + (lane >> 2), q = lane & 3;
-                bool ok_q = true, wide_q = true, pos_q = true, runs_q = true;
+                bool ok_q = true, wide_q = true, pos_q = true, runs_q = true, runs8_q = true;
                 if (pi < npb) {
                     const float4* cs = coef + (pi * 4 + q) * kSetF4;
                     const float4 C = cs[2], D = cs[3], E = cs[4];
@@ -933,18 +941,25 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                     // bin down the 16 rows of the sub-tile: monotonic (dv/dj = v2 + v4 di + 2 v5 dj keeps
                     // its sign) and changing by less than kRunSpan in all
                     const float curv = 8.0f * fabsf(D.z) + 16.0f * fabsf(D.w);
-                    runs_q = fabsf(D.x) > curv && 15.0f * (fabsf(D.x) + curv) < kRunSpan;
+                    runs_q = fabsf(D.x) > curv && 15.0f * (fabsf(D.x) + curv) < kRunSpan;    // 16-row runs
+                    runs8_q = fabsf(D.x) > curv && 7.0f * (fabsf(D.x) + curv) < kRunSpan;    // 8-row runs
                 }
                 const unsigned all4 = __ballot_sync(0xffffffffu, ok_q);
                 const unsigned wide4 = __ballot_sync(0xffffffffu, wide_q);
                 const unsigned pos4 = __ballot_sync(0xffffffffu, pos_q);
                 const unsigned runs4 = __ballot_sync(0xffffffffu, runs_q);
+                const unsigned runs8 = __ballot_sync(0xffffffffu, runs8_q);
                 const unsigned grp = lane & ~3;
                 const unsigned sgn = (pos4 >> grp) & 0xFu;
                 const bool mono = sgn == 0xFu || sgn == 0u;
                 if (pi < npb && q == 0) {
                     int m = !mono ? 0 : (((wide4 >> grp) & 0xFu) == 0xFu ? 2 : (((all4 >> grp) & 0xFu) == 0xFu ? 1 : 0));
-                    if (LINEAR && !PRECISE && m >= 1 && ((runs4 >> grp) & 0xFu) == 0xFu) m = 3;
+                    if (LINEAR && !PRECISE && m >= 1) {
+                        if (((runs4 >> grp) & 0xFu) == 0xFu)
+                            m = 4;
+                        else if (((runs8 >> grp) & 0xFu) == 0xFu)
+                            m = 3;
+                    }
                     fast[pi] = m;
                 }
             }
