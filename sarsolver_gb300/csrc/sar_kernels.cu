@@ -764,8 +764,8 @@ __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, 
     }
 }
 
-// MODES 4 and 3 (linear bins): the producer has shown that a sub-tile's bin is monotonic down its
-// rows and moves by less than kRunSpan over G = 16 (MODE 4) or G = 8 (MODE 3) rows, so in each
+// MODES 5, 4 and 3 (linear bins): the producer has shown that a sub-tile's bin is monotonic down
+// its rows and moves by less than kRunSpan over G = 16 (MODE 5), 8 (MODE 4) or 4 (MODE 3) rows, so in each
 // group of G rows a lane's bin takes at most two values n0, n0 + 1 (n0 = the smaller of the bins
 // at the group's first and last rows) and its taps lie in n0 .. n0 + 2.  The lane accumulates
 // those three bins in registers for both pulses and adds them to the windows once per group, in
@@ -842,12 +842,16 @@ __device__ __forceinline__ void scatter_half(int mode, const ColumnTerms& ctp, f
                                              const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
                                              int ws, int lane) {
     if constexpr (LINEAR && !PRECISE) {
-        if (mode == 4) {
+        if (mode == 5) {
             scatter_rows_runs<TWO, 16>(ctp, c9p, ctq, c9q, xrow, wp, wq, off_p, off_q, ws, lane);
             return;
         }
-        if (mode == 3) {
+        if (mode == 4) {
             scatter_rows_runs<TWO, 8>(ctp, c9p, ctq, c9q, xrow, wp, wq, off_p, off_q, ws, lane);
+            return;
+        }
+        if (mode == 3) {
+            scatter_rows_runs<TWO, 4>(ctp, c9p, ctq, c9q, xrow, wp, wq, off_p, off_q, ws, lane);
             return;
         }
     }
@@ -929,7 +933,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                 // The rate must also have one sign in all four sub-tiles, so that bins along a
                 // row are monotonic across the sub-tile boundary.
                 const int pi = pass + (lane >> 2), q = lane & 3;
-                bool ok_q = true, wide_q = true, pos_q = true, runs_q = true, runs8_q = true;
+                bool ok_q = true, wide_q = true, pos_q = true, runs_q = true, runs8_q = true, runs4_q = true;
                 if (pi < npb) {
                     const float4* cs = coef + (pi * 4 + q) * kSetF4;
                     const float4 C = cs[2], D = cs[3], E = cs[4];
@@ -943,12 +947,14 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                     const float curv = 8.0f * fabsf(D.z) + 16.0f * fabsf(D.w);
                     runs_q = fabsf(D.x) > curv && 15.0f * (fabsf(D.x) + curv) < kRunSpan;    // 16-row runs
                     runs8_q = fabsf(D.x) > curv && 7.0f * (fabsf(D.x) + curv) < kRunSpan;    // 8-row runs
+                    runs4_q = fabsf(D.x) > curv && 3.0f * (fabsf(D.x) + curv) < kRunSpan;    // 4-row runs
                 }
                 const unsigned all4 = __ballot_sync(0xffffffffu, ok_q);
                 const unsigned wide4 = __ballot_sync(0xffffffffu, wide_q);
                 const unsigned pos4 = __ballot_sync(0xffffffffu, pos_q);
                 const unsigned runs4 = __ballot_sync(0xffffffffu, runs_q);
                 const unsigned runs8 = __ballot_sync(0xffffffffu, runs8_q);
+                const unsigned runs4g = __ballot_sync(0xffffffffu, runs4_q);
                 const unsigned grp = lane & ~3;
                 const unsigned sgn = (pos4 >> grp) & 0xFu;
                 const bool mono = sgn == 0xFu || sgn == 0u;
@@ -956,8 +962,10 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                     int m = !mono ? 0 : (((wide4 >> grp) & 0xFu) == 0xFu ? 2 : (((all4 >> grp) & 0xFu) == 0xFu ? 1 : 0));
                     if (LINEAR && !PRECISE && m >= 1) {
                         if (((runs4 >> grp) & 0xFu) == 0xFu)
-                            m = 4;
+                            m = 5;
                         else if (((runs8 >> grp) & 0xFu) == 0xFu)
+                            m = 4;
+                        else if (((runs4g >> grp) & 0xFu) == 0xFu)
                             m = 3;
                     }
                     fast[pi] = m;
