@@ -1,9 +1,10 @@
 // sar_kernels.cu -- sm_103a kernels of the SAR operator pair.
 //
-//   K1  pack_adjoint / unpack_pairs    range-profile upsampling around a batched C2C FFT
-//                                      (replaces sarsolver_cxx.cpp:331-344)
-//   K2  bp_grid / bp_points            backprojection gather (replaces :345-350)
-//   K3  fp_grid / fp_points            forward scatter, the exact transpose of K2 (:284-291)
+//   K1  upsample_pairs (fused, N = 4096) or pack_adjoint / cuFFT / unpack_pairs
+//                                      range-profile upsampling (replaces sarsolver_cxx.cpp:331-344)
+//   K2  bp_grid_ws_pair / bp_grid / bp_points
+//                                      backprojection gather (replaces :345-350)
+//   K3  fp_grid_ws / fp_points         forward scatter, the exact transpose of K2 (:284-291)
 //   K4  pack_forward / extract_forward range-profile downsampling around the FFT (:292-307)
 //
 // Layout in HBM: images are complex64 [nz][ny][nx]; phase histories complex64 [S][N] with
@@ -240,14 +241,14 @@ cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st) {
     return a.g.precise_bins ? launch_bp_grid_t<true>(a, st) : launch_bp_grid_t<false>(a, st);
 }
 
-// ------------------------------------------- K2 (grid, warp-specialised pipeline)
-// Producer warp (warp 8): for stage k+1 it computes the (pulse, sub-tile) coefficient sets
-// and the tile base bins, then one lane per pulse issues a 1-D bulk copy (cp.async.bulk) of
-// that pulse's profile window into the stage's shared-memory buffer, completing on the
-// buffer's "full" mbarrier.  Consumer warps (0..7) wait on "full", gather, and arrive on the
-// buffer's "empty" mbarrier, which the producer waits on before reusing the buffer.  Every
-// wait is bounded by a clock budget; on expiry the kernel raises FLAG_WAIT_TIMEOUT and
-// leaves the loop instead of hanging.
+// ------------------------------------------- warp-specialised pipelines (K2 gather, K3 scatter)
+// Producer warps (8 and 9): for the next stage they compute the (pulse, sub-tile) coefficient
+// sets and the tile base bins (the gather also issues, one lane per pulse, a 1-D bulk copy
+// (cp.async.bulk) of that pulse's profile window into the stage's shared-memory buffer,
+// completing on the buffer's "full" mbarrier).  Consumer warps (0..7) wait on "full", work, and
+// arrive on the buffer's "empty" mbarrier, which the producers wait on before reusing the
+// buffer.  Every wait is bounded by a clock budget; on expiry the kernel raises
+// FLAG_WAIT_TIMEOUT and leaves the loop instead of hanging.
 constexpr int kWsConsumers = 256;
 constexpr int kWsProducers = 2;   // producer warps; producer w handles pulse passes 8w, 8w + 16, ...
 constexpr int kWsThreads = kWsConsumers + 32 * kWsProducers;
