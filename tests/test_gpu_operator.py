@@ -113,12 +113,16 @@ def test_linear_matches_fp64_oracle(kind):
     assert plan.device_flags() == 0
 
 
+@pytest.mark.parametrize("mode", ["linear", "nearest_ref"])
 @pytest.mark.parametrize("turn", [0, 1])
-def test_gather_lane_layouts_match_oracle(turn):
+def test_gather_lane_layouts_match_oracle(turn, mode):
     """The grid backprojection runs its lanes along the axis where range bins change slowly:
     along y for a collection looking along x, along x once the collection is turned by 90
     degrees.  Both layouts against the FP64 oracle, with an odd pulse count (a padding pulse
-    in the last stage of pulse pairs) and partial tiles."""
+    in the last stage of pulse pairs) and partial tiles; linear and split (nearest-bin) bins on
+    the grid path.  The forward projection of the same plans covers the scatter's register run
+    windows (bins barely move down the rows) and its atomic fallback (turned: bins change fast
+    down the rows, slowly along them)."""
     rng = np.random.default_rng(21 + turn)
     case = spotlight_case(37, 96, 70, 0.3, 4.0, weights=np.exp(1j * rng.uniform(-3, 3, 37)))
     if turn:
@@ -127,11 +131,15 @@ def test_gather_lane_layouts_match_oracle(turn):
         case.aperture = NumpySimpleSarAperture(ap.transmitter_positions @ rot.T, ap.receiver_positions @ rot.T,
                                                ap.stab_ref_posns, ap.centre_frequency, ap.sample_bandwidth,
                                                num_freqs=ap.num_freqs, slow_time_weighting=ap.slow_time_weighting)
-    plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp="linear")
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp=mode, path="grid")
     assert plan.gather_lanes_y == (turn == 0)
     y = crandn(rng, 37, 96)
-    e_a = rel_l2(gpu_adjoint(plan, y), oracle.adjoint(case.problem(), y, "linear", threads=8))
-    assert e_a < LINEAR_TOL, e_a
+    tol = LINEAR_TOL if mode == "linear" else NEAREST_TOL
+    e_a = rel_l2(gpu_adjoint(plan, y), oracle.adjoint(case.problem(), y, mode, threads=8))
+    assert e_a < tol, e_a
+    x = crandn(rng, case.scene.num_scatterers)
+    e_f = rel_l2(gpu_forward(plan, x), oracle.forward(case.problem(), x, mode, threads=8))
+    assert e_f < tol, e_f
     assert plan.device_flags() == 0
 
 
