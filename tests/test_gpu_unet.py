@@ -150,6 +150,6 @@ def test_unet_adam_reduces_a_regression_loss():
         net.backward(2.0 * r / r.numel())
         net.adam_step(lr=2e-3)
     # weight gradients are summed with float atomics, so the trajectory varies a little from run
-    # to run (last-step ratio 0.34-0.48 over repeated runs); judge the mean of the last steps
+    # to run (last-step ratio 0.34-0.48 over repeated runs); test the mean of the last steps
     assert sum(losses[-5:]) / 5 < 0.6 * losses[0] and losses[-1] < losses[0], losses
     assert net.flags() == 0
