@@ -120,6 +120,8 @@ typedef struct sar_plan_info {
                                    more slowly along y than along x), 0: along x */
     int fused_upsampling;       /* 1: the backprojection's range profiles come from the fused
                                    upsampling kernel (N = 4096, M a multiple of N), 0: cuFFT */
+    int fused_downsampling;     /* 1: the forward projection's FFT side is the fused downsampling
+                                   kernel (N = 4096, M a multiple of N), 0: cuFFT */
 } sar_plan_info;
 
 /* Create a plan on `device` (-1: the current device).  Copies all host inputs. */

@@ -84,7 +84,7 @@ class SarPlanInfo(ctypes.Structure):
         ("working_length", c_size_t), ("profile_first_bin", c_long), ("profile_length", c_size_t),
         ("tile_window", c_size_t), ("strip_window", c_size_t), ("device_bytes", c_size_t), ("grid", c_int),
         ("interp", c_int), ("num_fast_times", c_size_t), ("num_slow_times", c_size_t), ("num_scatterers", c_size_t),
-        ("device", c_int), ("fft_callbacks", c_int), ("gather_lanes_y", c_int), ("fused_upsampling", c_int),
+        ("device", c_int), ("fft_callbacks", c_int), ("gather_lanes_y", c_int), ("fused_upsampling", c_int), ("fused_downsampling", c_int),
     ]
 
 

@@ -120,6 +120,7 @@ struct sar_plan {
     void* d_spec = nullptr;        // FFT rows: float2, or double2 when fft_double
     // fused adjoint upsampling (N = 4096, M a multiple of N): twiddle tables e^{2 pi i q / N}, e^{2 pi i q / M}
     bool fused_up = false;
+    bool fused_down = false;   // fused forward downsampling (N = 4096, M a multiple of N, Lg <= M)
     float2* d_tw_n = nullptr;
     float2* d_tw_m = nullptr;
     bool fft_double = false;
@@ -629,7 +630,9 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
     // Fused adjoint upsampling: for N = 4096 and M a multiple of N the backprojection's range
     // profiles come from one kernel (eight-way split of the length-M transform into N-point ones,
     // stored span only) instead of pack + inverse FFT + unpack; twiddles computed in FP64.
-    if (upsample_fused_supported((int)N, (long)M, p->Lg)) {
+    const bool up_ok = upsample_fused_supported((int)N, (long)M, p->Lg);
+    const bool down_ok = downsample_fused_supported((int)N, (long)M, p->Lg);
+    if (up_ok || down_ok) {
         std::vector<float2> tn(N), tm(M);
         const double two_pi = 6.283185307179586476925286766559;
         for (size_t q = 0; q < N; ++q)
@@ -640,7 +643,8 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
         if ((rc = p->alloc(&p->d_tw_m, M, "twiddles"))) return rc;
         SAR_CUDA(cudaMemcpy(p->d_tw_n, tn.data(), sizeof(float2) * N, cudaMemcpyHostToDevice), "twiddles");
         SAR_CUDA(cudaMemcpy(p->d_tw_m, tm.data(), sizeof(float2) * M, cudaMemcpyHostToDevice), "twiddles");
-        p->fused_up = true;
+        p->fused_up = up_ok;
+        p->fused_down = down_ok;
     }
     // Callback transforms (single precision): opt-in with SAR_FFT_CALLBACKS=1.  On GB300 with the
     // cuFFT of CUDA 13.0, plans with JIT (LTO) callbacks fail to build (CUFFT_INTERNAL_ERROR from
@@ -751,6 +755,7 @@ int sar_plan_get_info(const sar_plan* p, sar_plan_info* info) {
     info->fft_callbacks = p->fft_cb ? 1 : 0;
     info->gather_lanes_y = p->lanes_y;
     info->fused_upsampling = p->fused_up ? 1 : 0;
+    info->fused_downsampling = p->fused_down ? 1 : 0;
     return SAR_OK;
 }
 
@@ -890,6 +895,12 @@ int sar_forward(sar_plan* p, const void* x_dev, void* y_dev, void* stream) {
     mark(ev, 2, st);
     for (size_t first = 0; first < p->S; first += (size_t)p->chunk) {
         const int rows = (int)std::min<size_t>(p->chunk, p->S - first);
+        if (p->fused_down) {
+            SAR_CUDA(launch_downsample_forward_fused(acc, p->d_wave, p->d_wfwd, p->d_tw_n, p->d_tw_m, (float2*)y_dev,
+                                                     (int)p->N, (long)p->M, p->Lg, p->bg0, rows, (int)first, st),
+                     "fused downsampling");
+            continue;
+        }
         if (p->fft_cb) {
             cufftHandle h = 0;
             int rc = cb_plan(p, rows, false, &h);

@@ -1610,6 +1610,90 @@ static int up_stage_row(int Lg, int U) {
     return ((n + 13) & ~15) + 2;
 }
 
+// Fused forward downsampling for N = 4096, M = U N: the transpose of the fused upsampling.  With
+// the accumulated bins a[b] (b = U j + r, taken modulo M) the forward transform at frequency k in
+// [-N/2, N/2) is  K(k) = sum_r e^{-2 pi i k r / M} DFT_N(a_r)[k mod N],  a_r[j] = a[U j + r]; each
+// forward DFT is computed as conj(inverse DFT(conj a_r)) with the Stockham passes above, and
+// y[(i + N/2) mod N] = W[i] f K(k_i) is written directly (replaces pack_forward + FFT + extract).
+// The twiddle e^{2 pi i k r / M} advances by one factor per r in registers; the accumulation
+// runs on the conjugate and is conjugated once at the end.
+__global__ void __launch_bounds__(kUpThreads, 2) downsample_forward_kernel(
+    const float2* __restrict__ acc, const float2* __restrict__ wave, const float2* __restrict__ wfac,
+    const float2* __restrict__ tw_n, const float2* __restrict__ tw_m, float2* __restrict__ y, int U, long M, int Lg,
+    long bg0, int first) {
+    extern __shared__ __align__(16) float2 dnsm[];
+    float2* A = dnsm;
+    float2* B = dnsm + up_pad(kUpN);
+    const int t = threadIdx.x;
+    const long s = (long)first + blockIdx.x;
+    const float2* arow = acc + s * Lg;
+    const int bmod = (int)(((bg0 % U) + U) % U);
+    float2 Y[16], T[16];   // conj of the output at k = t + 256 e, and e^{2 pi i k r / M}
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+        Y[e] = make_float2(0.f, 0.f);
+        T[e] = make_float2(1.f, 0.f);
+    }
+    for (int r = 0; r < U; ++r) {
+        // conj(a_r) into A
+        for (int e = t; e < up_pad(kUpN); e += kUpThreads) A[e] = make_float2(0.f, 0.f);
+        __syncthreads();
+        int w0 = r - bmod;
+        if (w0 < 0) w0 += U;
+        for (int w = w0 + U * t; w < Lg; w += U * kUpThreads) {
+            long b = (bg0 + w) % M;
+            if (b < 0) b += M;
+            const float2 v = __ldg(arow + w);
+            A[up_pad((int)(b / U))] = make_float2(v.x, -v.y);
+        }
+        __syncthreads();
+        float2 v[16];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) v[e] = A[up_pad(t + kUpThreads * e)];
+        dft16_inv(v);
+#pragma unroll
+        for (int e = 0; e < 16; ++e) B[up_pad(t * 16 + e)] = v[e];
+        __syncthreads();
+        up_pass(B, A, 16, tw_n);
+        __syncthreads();
+        up_pass(A, B, 256, tw_n);
+        __syncthreads();
+        // Y += e^{2 pi i k r / M} B[k]  (conjugate domain), then advance the twiddles
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+            const int kp = t + kUpThreads * e;
+            const float2 c = cmulf(T[e], B[up_pad(kp)]);
+            Y[e].x += c.x;
+            Y[e].y += c.y;
+            T[e] = cmulf(T[e], __ldg(tw_m + (kp < kUpN / 2 ? kp : M - (kUpN - kp))));
+        }
+        __syncthreads();
+    }
+    const float2 f = __ldg(wfac + s);
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+        const int i = t + kUpThreads * e;
+        const float2 k = make_float2(Y[e].x, -Y[e].y);
+        const float2 w = __ldg(wave + i);
+        const float2 a = make_float2(w.x * k.x - w.y * k.y, w.x * k.y + w.y * k.x);
+        y[s * kUpN + ((i + kUpN / 2) & (kUpN - 1))] = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
+    }
+}
+
+bool downsample_fused_supported(int N, long M, int Lg) { return N == kUpN && M % N == 0 && M / N <= 64 && Lg >= 1 && Lg <= M; }
+
+cudaError_t launch_downsample_forward_fused(const float2* acc, const float2* wave, const float2* wfac,
+                                            const float2* tw_n, const float2* tw_m, float2* y, int N, long M, int Lg,
+                                            long bg0, int rows, int first, cudaStream_t st) {
+    if (!downsample_fused_supported(N, M, Lg) || rows < 1) return cudaErrorInvalidValue;
+    const size_t smem = sizeof(float2) * 2 * (kUpN + kUpN / 16);
+    cudaError_t e = cudaFuncSetAttribute(downsample_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    downsample_forward_kernel<<<rows, kUpThreads, smem, st>>>(acc, wave, wfac, tw_n, tw_m, y, (int)(M / N), M, Lg,
+                                                              bg0, first);
+    return cudaGetLastError();
+}
+
 size_t upsample_fused_smem_bytes(int Lg, int U) {
     return sizeof(float2) * ((size_t)2 * (kUpN + kUpN / 16) + (size_t)U * up_stage_row(Lg, U));
 }

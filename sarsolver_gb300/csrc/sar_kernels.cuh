@@ -93,6 +93,12 @@ size_t upsample_fused_smem_bytes(int Lg, int U);
 cudaError_t launch_upsample_pairs_fused(const float2* y, const float2* wave, const float2* wfac, const float2* tw_n,
                                         const float2* tw_m, float4* pairs, int N, long M, int Lg, long bg0, int rows,
                                         int first, int linear, cudaStream_t st);
+// Fused forward downsampling for N = 4096, M a multiple of N and Lg <= M: y straight from the
+// bin accumulator acc [S][Lg] (replaces pack_forward + forward FFT + extract_forward).
+bool downsample_fused_supported(int N, long M, int Lg);
+cudaError_t launch_downsample_forward_fused(const float2* acc, const float2* wave, const float2* wfac,
+                                            const float2* tw_n, const float2* tw_m, float2* y, int N, long M, int Lg,
+                                            long bg0, int rows, int first, cudaStream_t st);
 cudaError_t launch_unpack_pairs(const void* spec, int dbl, const float2* wfac, float4* pairs, long M, int Lg,
                                 long bg0, int rows, int first, int linear, cudaStream_t st);
 cudaError_t launch_unpack_profiles(const void* spec, int dbl, float2* prof, long M, int Lg, long bg0, int rows,

@@ -146,9 +146,10 @@ def test_gather_lane_layouts_match_oracle(turn, mode):
 @pytest.mark.parametrize("mode,srp_shift", [("linear", 0.0), ("nearest_ref", 0.0), ("linear", 1.0)])
 def test_fused_upsampling_matches_oracle(mode, srp_shift):
     """N = 4096 samples with U = 8 (M = 32768): the range profiles come from the fused upsampling
-    kernel (eight 4096-point transforms per pulse, stored span only).  Against the FP64 oracle in
-    both modes; the stored span starts below bin 0 (taken modulo M), also with the SRP moved off
-    the scene centre."""
+    kernel (eight 4096-point transforms per pulse, stored span only), and the forward projection
+    ends in the fused downsampling kernel (its transpose).  Against the FP64 oracle in both modes;
+    the stored span starts below bin 0 (taken modulo M), also with the SRP moved off the scene
+    centre."""
     rng = np.random.default_rng(31)
     case = spotlight_case(48, 4096, 48, 0.5, 3.0, weights=np.exp(1j * rng.uniform(-3, 3, 48)))
     if srp_shift:
@@ -158,13 +159,16 @@ def test_fused_upsampling_matches_oracle(mode, srp_shift):
                                                ap.centre_frequency, ap.sample_bandwidth, num_freqs=4096,
                                                slow_time_weighting=ap.slow_time_weighting)
     plan = SarPlan(case.scene, case.aperture, upsample_ratio=8.0, interp=mode)
-    assert plan.fused_upsampling
+    assert plan.fused_upsampling and plan.fused_downsampling
     assert plan.profile_first_bin < 0
     y = crandn(rng, 48, 4096)
     got = gpu_adjoint(plan, y)
     ref = oracle.adjoint(case.problem(), y, mode, threads=8)
     tol = LINEAR_TOL if mode == "linear" else NEAREST_TOL
     assert rel_l2(got, ref) < tol
+    # the forward projection's fused downsampling against the oracle's forward
+    x = crandn(rng, case.scene.num_scatterers)
+    assert rel_l2(gpu_forward(plan, x), oracle.forward(case.problem(), x, mode, threads=8)) < tol
     assert plan.device_flags() == 0
 
 
