@@ -119,7 +119,7 @@ typedef struct sar_plan_info {
     int gather_lanes_y;         /* 1: the grid backprojection runs warp lanes along y (bins change
                                    more slowly along y than along x), 0: along x */
     int fused_upsampling;       /* 1: the backprojection's range profiles come from the fused
-                                   upsampling kernel (N = 4096, M a multiple of N), 0: cuFFT */
+                                   upsampling kernel (N = 1024, 2048 or 4096, M a multiple of N), 0: cuFFT */
     int fused_downsampling;     /* 1: the forward projection's FFT side is the fused downsampling
                                    kernel (N = 4096, M a multiple of N), 0: cuFFT */
 } sar_plan_info;

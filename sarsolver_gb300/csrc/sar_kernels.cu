@@ -1447,18 +1447,23 @@ cudaError_t launch_unpack_pairs(const void* spec, int dbl, const float2* wfac, f
 }
 
 // ------------------------------------------- K1 fused: upsampling FFT straight into pairs
-// For N = 4096 and M = U N (integer U): bin b = U j + r of the inverse length-M transform of the
+// For N = 1024, 2048 or 4096 and M = U N (integer U): bin b = U j + r of the inverse length-M transform of the
 // zero-padded spectrum (frequencies k in [-N/2, N/2), X_k = conj(W) y at k mod N) is
 //   p(U j + r) = sum_k X_k e^{2 pi i k r / M} e^{2 pi i k j / N},
-// an N-point inverse DFT of the spectrum twiddled by e^{2 pi i k r / M}.  One CTA per pulse row
-// computes the U such transforms in shared memory (radix-16 Stockham, three passes, one
-// 16-point butterfly per thread and pass), keeps the bins of the stored span
+// an N-point inverse DFT of the spectrum twiddled by e^{2 pi i k r / M}.  One CTA of N / 16
+// threads per pulse row computes the U such transforms in shared memory (Stockham: a radix-N/256
+// first pass on the 16 values each thread holds, then two radix-16 passes with one 16-point
+// butterfly per thread), keeps the bins of the stored span
 // [bg0, bg0 + Lg] (taken modulo M) and writes the (value, difference) pairs of
 // unpack_pairs_kernel directly: the row is read once (N values) and only the span is written,
 // where the unfused path writes and reads the M-point rows three times.  Twiddles come from
 // FP64-computed tables e^{2 pi i q / N} and e^{2 pi i q / M}.
-constexpr int kUpN = 4096;
-constexpr int kUpThreads = 256;
+template <int N>
+struct UpShape {
+    static constexpr int T = N / 16;     // threads per row: one radix-16 butterfly each
+    static constexpr int R0 = N / 256;   // radix of the first pass: 4, 8 or 16
+    static constexpr int NB = 16 / R0;   // first-pass butterflies per thread
+};
 
 __device__ __forceinline__ int up_pad(int x) { return x + (x >> 4); }   // one slot per 16: no bank conflicts
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
@@ -1500,6 +1505,59 @@ __device__ __forceinline__ void dft16_inv(float2 (&v)[16]) {
     for (int k = 0; k < 16; ++k) v[k] = t[k];
 }
 
+// v[k] <- sum_n v[n] e^{+2 pi i n k / 8}: n = 2 n1 + n2, k = k1 + 4 k2 (radix 4, then radix 2).
+__device__ __forceinline__ void dft8_inv(float2 (&v)[8]) {
+    dft4_inv(v[0], v[2], v[4], v[6]);   // n2 = 0: Y0[k1] at v[2 k1]
+    dft4_inv(v[1], v[3], v[5], v[7]);   // n2 = 1: Y1[k1] at v[2 k1 + 1]
+    const float h = 0.70710678118654752f;
+    v[3] = cmulf(v[3], make_float2(h, h));            // W8^1
+    v[5] = make_float2(-v[5].y, v[5].x);              // W8^2 = i
+    v[7] = cmulf(v[7], make_float2(-h, h));           // W8^3
+    float2 t[8];
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+        const float2 a = v[2 * k1], b = v[2 * k1 + 1];
+        t[k1] = make_float2(a.x + b.x, a.y + b.y);
+        t[k1 + 4] = make_float2(a.x - b.x, a.y - b.y);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = t[k];
+}
+
+// First Stockham pass (sub-transform length 1) on the 16 values x[e] = element t + T e a thread
+// holds: butterfly j = t + T e1 (e1 < NB) combines elements j + 256 m (m < R0), which are
+// x[e1 + NB m], and writes out[j R0 + m].
+template <int N>
+__device__ __forceinline__ void up_first_pass(const float2 (&x)[16], float2* out, int t) {
+    constexpr int T = UpShape<N>::T, R0 = UpShape<N>::R0, NB = UpShape<N>::NB;
+#pragma unroll
+    for (int e1 = 0; e1 < NB; ++e1) {
+        const int j = t + T * e1;
+        if constexpr (R0 == 16) {
+            float2 v[16];
+#pragma unroll
+            for (int m = 0; m < 16; ++m) v[m] = x[m];
+            dft16_inv(v);
+#pragma unroll
+            for (int m = 0; m < 16; ++m) out[up_pad(j * 16 + m)] = v[m];
+        } else if constexpr (R0 == 8) {
+            float2 v[8];
+#pragma unroll
+            for (int m = 0; m < 8; ++m) v[m] = x[e1 + NB * m];
+            dft8_inv(v);
+#pragma unroll
+            for (int m = 0; m < 8; ++m) out[up_pad(j * 8 + m)] = v[m];
+        } else {
+            float2 a = x[e1], b = x[e1 + NB], c = x[e1 + 2 * NB], d = x[e1 + 3 * NB];
+            dft4_inv(a, b, c, d);
+            out[up_pad(j * 4)] = a;
+            out[up_pad(j * 4 + 1)] = b;
+            out[up_pad(j * 4 + 2)] = c;
+            out[up_pad(j * 4 + 3)] = d;
+        }
+    }
+}
+
 // v[r] *= w^r for r = 1..15, the powers built by squaring (at most four chained products).
 __device__ __forceinline__ void apply_powers(float2 (&v)[16], float2 w) {
     const float2 w2 = cmulf(w, w), w4 = cmulf(w2, w2), w8 = cmulf(w4, w4);
@@ -1521,64 +1579,65 @@ __device__ __forceinline__ void apply_powers(float2 (&v)[16], float2 w) {
     v[15] = cmulf(v[15], cmulf(w8, w7));
 }
 
-// Radix-16 Stockham pass over 4096 points (sub-transform length ns = 16 or 256 before it).
+// Radix-16 Stockham pass over N points (sub-transform length ns = N / 256 or N / 16 before it).
+template <int N>
 __device__ __forceinline__ void up_pass(const float2* in, float2* out, int ns, const float2* __restrict__ tw_n) {
     const int j = threadIdx.x;
     float2 v[16];
 #pragma unroll
-    for (int r = 0; r < 16; ++r) v[r] = in[up_pad(j + r * (kUpN / 16))];
+    for (int r = 0; r < 16; ++r) v[r] = in[up_pad(j + r * (N / 16))];
     const int k = j & (ns - 1);
-    apply_powers(v, __ldg(tw_n + k * (kUpN / (ns * 16))));   // e^{2 pi i r k / (16 ns)}
+    apply_powers(v, __ldg(tw_n + k * (N / (ns * 16))));   // e^{2 pi i r k / (16 ns)}
     dft16_inv(v);
     const int base = (j / ns) * ns * 16 + k;
 #pragma unroll
     for (int r = 0; r < 16; ++r) out[up_pad(base + r * ns)] = v[r];
 }
 
-__global__ void __launch_bounds__(kUpThreads, 2) upsample_pairs_kernel(
+template <int N>
+__global__ void __launch_bounds__(N / 16, 8192 / N) upsample_pairs_kernel(
     const float2* __restrict__ y, const float2* __restrict__ wave, const float2* __restrict__ wfac,
     const float2* __restrict__ tw_n, const float2* __restrict__ tw_m, float4* __restrict__ pairs, int U, long M,
     int Lg, long bg0, int first, int linear, int C) {
+    constexpr int T = UpShape<N>::T, R0 = UpShape<N>::R0;
     extern __shared__ __align__(16) float2 upsm[];
     float2* A = upsm;
-    float2* B = upsm + up_pad(kUpN);
+    float2* B = upsm + up_pad(N);
     // span bins bg0 .. bg0 + Lg (mod M), residue-major: bin w of residue r = (bg0 + w) mod U at
     // stage[r C + w / U], C = 2 (mod 16) so that both the scatter and the pair reads avoid bank conflicts
-    float2* stage = upsm + 2 * up_pad(kUpN);
+    float2* stage = upsm + 2 * up_pad(N);
     const int t = threadIdx.x;
     const long s = (long)first + blockIdx.x;
-    // this thread's spectrum values, k' = t + 256 e (FFT order index = k mod N)
+    // this thread's spectrum values, k' = t + T e (FFT order index = k mod N)
     float2 X[16];
 #pragma unroll
     for (int e = 0; e < 16; ++e) {
-        const int kp = t + kUpThreads * e;
-        const float2 yv = y[s * kUpN + ((kp + kUpN / 2) & (kUpN - 1))];
+        const int kp = t + T * e;
+        const float2 yv = y[s * N + ((kp + N / 2) & (N - 1))];
         const float2 w = __ldg(wave + kp);
         X[e] = make_float2(w.x * yv.x + w.y * yv.y, w.x * yv.y - w.y * yv.x);
     }
     const int bmod = (int)(((bg0 % U) + U) % U);
     for (int r = 0; r < U; ++r) {
         // pass 1 straight from registers: X holds the spectrum times e^{2 pi i k r / M} (advanced by
-        // one factor e^{2 pi i k / M} per r, read contiguously), 16-point DFT, ns = 1
+        // one factor e^{2 pi i k / M} per r, read contiguously)
         float2 v[16];
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
             v[e] = X[e];
-            const int kp = t + kUpThreads * e;
-            X[e] = cmulf(X[e], __ldg(tw_m + (kp < kUpN / 2 ? kp : M - (kUpN - kp))));
+            const int kp = t + T * e;
+            X[e] = cmulf(X[e], __ldg(tw_m + (kp < N / 2 ? kp : M - (N - kp))));
         }
-        dft16_inv(v);
-#pragma unroll
-        for (int e = 0; e < 16; ++e) A[up_pad(t * 16 + e)] = v[e];
+        up_first_pass<N>(v, A, t);
         __syncthreads();
-        up_pass(A, B, 16, tw_n);
+        up_pass<N>(A, B, R0, tw_n);
         __syncthreads();
-        up_pass(B, A, 256, tw_n);
+        up_pass<N>(B, A, 16 * R0, tw_n);
         __syncthreads();
         // A holds p(U j + r) at j; keep the span's bins with this residue
         int w0 = r - bmod;
         if (w0 < 0) w0 += U;
-        for (int i = t; w0 + U * i <= Lg; i += kUpThreads) {
+        for (int i = t; w0 + U * i <= Lg; i += T) {
             long b = (bg0 + w0 + U * i) % M;
             if (b < 0) b += M;
             stage[r * C + i] = A[up_pad((int)(b / U))];
@@ -1587,7 +1646,7 @@ __global__ void __launch_bounds__(kUpThreads, 2) upsample_pairs_kernel(
     }
     const float2 f = __ldg(wfac + s);
     float4* dst = pairs + s * Lg;
-    for (int w = t; w < Lg; w += kUpThreads) {
+    for (int w = t; w < Lg; w += T) {
         const int r0 = (bmod + w) % U, r1 = (bmod + w + 1) % U;
         const float2 a = stage[r0 * C + w / U];
         const float2 p0 = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
@@ -1610,37 +1669,39 @@ static int up_stage_row(int Lg, int U) {
     return ((n + 13) & ~15) + 2;
 }
 
-// Fused forward downsampling for N = 4096, M = U N: the transpose of the fused upsampling.  With
+// Fused forward downsampling for N = 1024, 2048 or 4096, M = U N: the transpose of the fused upsampling.  With
 // the accumulated bins a[b] (b = U j + r, taken modulo M) the forward transform at frequency k in
 // [-N/2, N/2) is  K(k) = sum_r e^{-2 pi i k r / M} DFT_N(a_r)[k mod N],  a_r[j] = a[U j + r]; each
 // forward DFT is computed as conj(inverse DFT(conj a_r)) with the Stockham passes above, and
 // y[(i + N/2) mod N] = W[i] f K(k_i) is written directly (replaces pack_forward + FFT + extract).
 // The twiddle e^{2 pi i k r / M} advances by one factor per r in registers; the accumulation
 // runs on the conjugate and is conjugated once at the end.
-__global__ void __launch_bounds__(kUpThreads, 2) downsample_forward_kernel(
+template <int N>
+__global__ void __launch_bounds__(N / 16, 8192 / N) downsample_forward_kernel(
     const float2* __restrict__ acc, const float2* __restrict__ wave, const float2* __restrict__ wfac,
     const float2* __restrict__ tw_n, const float2* __restrict__ tw_m, float2* __restrict__ y, int U, long M, int Lg,
     long bg0, int first) {
+    constexpr int T = UpShape<N>::T, R0 = UpShape<N>::R0;
     extern __shared__ __align__(16) float2 dnsm[];
     float2* A = dnsm;
-    float2* B = dnsm + up_pad(kUpN);
+    float2* B = dnsm + up_pad(N);
     const int t = threadIdx.x;
     const long s = (long)first + blockIdx.x;
     const float2* arow = acc + s * Lg;
     const int bmod = (int)(((bg0 % U) + U) % U);
-    float2 Y[16], T[16];   // conj of the output at k = t + 256 e, and e^{2 pi i k r / M}
+    float2 Y[16], Z[16];   // conj of the output at k = t + T e, and e^{2 pi i k r / M}
 #pragma unroll
     for (int e = 0; e < 16; ++e) {
         Y[e] = make_float2(0.f, 0.f);
-        T[e] = make_float2(1.f, 0.f);
+        Z[e] = make_float2(1.f, 0.f);
     }
     for (int r = 0; r < U; ++r) {
         // conj(a_r) into A
-        for (int e = t; e < up_pad(kUpN); e += kUpThreads) A[e] = make_float2(0.f, 0.f);
+        for (int e = t; e < up_pad(N); e += T) A[e] = make_float2(0.f, 0.f);
         __syncthreads();
         int w0 = r - bmod;
         if (w0 < 0) w0 += U;
-        for (int w = w0 + U * t; w < Lg; w += U * kUpThreads) {
+        for (int w = w0 + U * t; w < Lg; w += U * T) {
             long b = (bg0 + w) % M;
             if (b < 0) b += M;
             const float2 v = __ldg(arow + w);
@@ -1649,71 +1710,91 @@ __global__ void __launch_bounds__(kUpThreads, 2) downsample_forward_kernel(
         __syncthreads();
         float2 v[16];
 #pragma unroll
-        for (int e = 0; e < 16; ++e) v[e] = A[up_pad(t + kUpThreads * e)];
-        dft16_inv(v);
-#pragma unroll
-        for (int e = 0; e < 16; ++e) B[up_pad(t * 16 + e)] = v[e];
+        for (int e = 0; e < 16; ++e) v[e] = A[up_pad(t + T * e)];
+        up_first_pass<N>(v, B, t);
         __syncthreads();
-        up_pass(B, A, 16, tw_n);
+        up_pass<N>(B, A, R0, tw_n);
         __syncthreads();
-        up_pass(A, B, 256, tw_n);
+        up_pass<N>(A, B, 16 * R0, tw_n);
         __syncthreads();
         // Y += e^{2 pi i k r / M} B[k]  (conjugate domain), then advance the twiddles
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
-            const int kp = t + kUpThreads * e;
-            const float2 c = cmulf(T[e], B[up_pad(kp)]);
+            const int kp = t + T * e;
+            const float2 c = cmulf(Z[e], B[up_pad(kp)]);
             Y[e].x += c.x;
             Y[e].y += c.y;
-            T[e] = cmulf(T[e], __ldg(tw_m + (kp < kUpN / 2 ? kp : M - (kUpN - kp))));
+            Z[e] = cmulf(Z[e], __ldg(tw_m + (kp < N / 2 ? kp : M - (N - kp))));
         }
         __syncthreads();
     }
     const float2 f = __ldg(wfac + s);
 #pragma unroll
     for (int e = 0; e < 16; ++e) {
-        const int i = t + kUpThreads * e;
+        const int i = t + T * e;
         const float2 k = make_float2(Y[e].x, -Y[e].y);
         const float2 w = __ldg(wave + i);
         const float2 a = make_float2(w.x * k.x - w.y * k.y, w.x * k.y + w.y * k.x);
-        y[s * kUpN + ((i + kUpN / 2) & (kUpN - 1))] = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
+        y[s * N + ((i + N / 2) & (N - 1))] = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
     }
 }
 
-bool downsample_fused_supported(int N, long M, int Lg) { return N == kUpN && M % N == 0 && M / N <= 64 && Lg >= 1 && Lg <= M; }
+static bool fused_fft_length(int N) { return N == 1024 || N == 2048 || N == 4096; }
+
+bool downsample_fused_supported(int N, long M, int Lg) {
+    return fused_fft_length(N) && M % N == 0 && M / N <= 64 && Lg >= 1 && Lg <= M;
+}
+
+template <int N>
+static cudaError_t launch_down_t(const float2* acc, const float2* wave, const float2* wfac, const float2* tw_n,
+                                 const float2* tw_m, float2* y, long M, int Lg, long bg0, int rows, int first,
+                                 cudaStream_t st) {
+    const size_t smem = sizeof(float2) * 2 * (N + N / 16);
+    cudaError_t e = cudaFuncSetAttribute(downsample_forward_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    downsample_forward_kernel<N><<<rows, N / 16, smem, st>>>(acc, wave, wfac, tw_n, tw_m, y, (int)(M / N), M, Lg, bg0,
+                                                             first);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_downsample_forward_fused(const float2* acc, const float2* wave, const float2* wfac,
                                             const float2* tw_n, const float2* tw_m, float2* y, int N, long M, int Lg,
                                             long bg0, int rows, int first, cudaStream_t st) {
     if (!downsample_fused_supported(N, M, Lg) || rows < 1) return cudaErrorInvalidValue;
-    const size_t smem = sizeof(float2) * 2 * (kUpN + kUpN / 16);
-    cudaError_t e = cudaFuncSetAttribute(downsample_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    downsample_forward_kernel<<<rows, kUpThreads, smem, st>>>(acc, wave, wfac, tw_n, tw_m, y, (int)(M / N), M, Lg,
-                                                              bg0, first);
-    return cudaGetLastError();
+    if (N == 1024) return launch_down_t<1024>(acc, wave, wfac, tw_n, tw_m, y, M, Lg, bg0, rows, first, st);
+    if (N == 2048) return launch_down_t<2048>(acc, wave, wfac, tw_n, tw_m, y, M, Lg, bg0, rows, first, st);
+    return launch_down_t<4096>(acc, wave, wfac, tw_n, tw_m, y, M, Lg, bg0, rows, first, st);
 }
 
-size_t upsample_fused_smem_bytes(int Lg, int U) {
-    return sizeof(float2) * ((size_t)2 * (kUpN + kUpN / 16) + (size_t)U * up_stage_row(Lg, U));
+size_t upsample_fused_smem_bytes(int N, int Lg, int U) {
+    return sizeof(float2) * ((size_t)2 * (N + N / 16) + (size_t)U * up_stage_row(Lg, U));
 }
 
 bool upsample_fused_supported(int N, long M, int Lg) {
-    return N == kUpN && M % N == 0 && M / N <= 64 && Lg >= 1 &&
-           upsample_fused_smem_bytes(Lg, (int)(M / N)) <= 112 * 1024;
+    return fused_fft_length(N) && M % N == 0 && M / N <= 64 && Lg >= 1 &&
+           upsample_fused_smem_bytes(N, Lg, (int)(M / N)) <= 112 * 1024;
+}
+
+template <int N>
+static cudaError_t launch_up_t(const float2* y, const float2* wave, const float2* wfac, const float2* tw_n,
+                               const float2* tw_m, float4* pairs, long M, int Lg, long bg0, int rows, int first,
+                               int linear, cudaStream_t st) {
+    const int U = (int)(M / N);
+    const size_t smem = upsample_fused_smem_bytes(N, Lg, U);
+    cudaError_t e = cudaFuncSetAttribute(upsample_pairs_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    upsample_pairs_kernel<N><<<rows, N / 16, smem, st>>>(y, wave, wfac, tw_n, tw_m, pairs, U, M, Lg, bg0, first,
+                                                         linear, up_stage_row(Lg, U));
+    return cudaGetLastError();
 }
 
 cudaError_t launch_upsample_pairs_fused(const float2* y, const float2* wave, const float2* wfac, const float2* tw_n,
                                         const float2* tw_m, float4* pairs, int N, long M, int Lg, long bg0, int rows,
                                         int first, int linear, cudaStream_t st) {
     if (!upsample_fused_supported(N, M, Lg) || rows < 1) return cudaErrorInvalidValue;
-    const int U = (int)(M / N);
-    const size_t smem = upsample_fused_smem_bytes(Lg, U);
-    cudaError_t e = cudaFuncSetAttribute(upsample_pairs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    upsample_pairs_kernel<<<rows, kUpThreads, smem, st>>>(y, wave, wfac, tw_n, tw_m, pairs, U, M, Lg, bg0, first,
-                                                          linear, up_stage_row(Lg, U));
-    return cudaGetLastError();
+    if (N == 1024) return launch_up_t<1024>(y, wave, wfac, tw_n, tw_m, pairs, M, Lg, bg0, rows, first, linear, st);
+    if (N == 2048) return launch_up_t<2048>(y, wave, wfac, tw_n, tw_m, pairs, M, Lg, bg0, rows, first, linear, st);
+    return launch_up_t<4096>(y, wave, wfac, tw_n, tw_m, pairs, M, Lg, bg0, rows, first, linear, st);
 }
 
 cudaError_t launch_unpack_profiles(const void* spec, int dbl, float2* prof, long M, int Lg, long bg0, int rows,

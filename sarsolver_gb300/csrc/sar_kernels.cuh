@@ -85,15 +85,15 @@ cudaError_t launch_pack_adjoint(const float2* y, const float2* wave, void* spec,
                                 int first, cudaStream_t st);
 cudaError_t launch_unpack_compact(const float2* compact, int Lc, const float2* wfac, float4* pairs, float2* prof,
                                   long M, int Lg, int rows, int first, int linear, cudaStream_t st);
-// Fused adjoint upsampling for N = 4096 and M a multiple of N: pairs over the stored span straight
+// Fused adjoint upsampling for N = 1024, 2048 or 4096 and M a multiple of N: pairs over the stored span straight
 // from the fftshifted phase history (replaces pack + inverse FFT + unpack_pairs); twiddle tables
 // tw_n[q] = e^{2 pi i q / N}, tw_m[q] = e^{2 pi i q / M}.
 bool upsample_fused_supported(int N, long M, int Lg);
-size_t upsample_fused_smem_bytes(int Lg, int U);
+size_t upsample_fused_smem_bytes(int N, int Lg, int U);
 cudaError_t launch_upsample_pairs_fused(const float2* y, const float2* wave, const float2* wfac, const float2* tw_n,
                                         const float2* tw_m, float4* pairs, int N, long M, int Lg, long bg0, int rows,
                                         int first, int linear, cudaStream_t st);
-// Fused forward downsampling for N = 4096, M a multiple of N and Lg <= M: y straight from the
+// Fused forward downsampling for N = 1024, 2048 or 4096, M a multiple of N and Lg <= M: y straight from the
 // bin accumulator acc [S][Lg] (replaces pack_forward + forward FFT + extract_forward).
 bool downsample_fused_supported(int N, long M, int Lg);
 cudaError_t launch_downsample_forward_fused(const float2* acc, const float2* wave, const float2* wfac,

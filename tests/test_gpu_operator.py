@@ -143,25 +143,26 @@ def test_gather_lane_layouts_match_oracle(turn, mode):
     assert plan.device_flags() == 0
 
 
-@pytest.mark.parametrize("mode,srp_shift", [("linear", 0.0), ("nearest_ref", 0.0), ("linear", 1.0)])
-def test_fused_upsampling_matches_oracle(mode, srp_shift):
-    """N = 4096 samples with U = 8 (M = 32768): the range profiles come from the fused upsampling
-    kernel (eight 4096-point transforms per pulse, stored span only), and the forward projection
+@pytest.mark.parametrize("mode,srp_shift,nf", [("linear", 0.0, 4096), ("nearest_ref", 0.0, 4096), ("linear", 1.0, 4096),
+                                               ("linear", 0.0, 2048), ("linear", 0.0, 1024), ("nearest_ref", 1.0, 1024)])
+def test_fused_upsampling_matches_oracle(mode, srp_shift, nf):
+    """N = 1024, 2048 or 4096 samples with U = 8: the range profiles come from the fused upsampling
+    kernel (eight N-point transforms per pulse, stored span only), and the forward projection
     ends in the fused downsampling kernel (its transpose).  Against the FP64 oracle in both modes;
     the stored span starts below bin 0 (taken modulo M), also with the SRP moved off the scene
     centre."""
     rng = np.random.default_rng(31)
-    case = spotlight_case(48, 4096, 48, 0.5, 3.0, weights=np.exp(1j * rng.uniform(-3, 3, 48)))
+    case = spotlight_case(48, nf, 48, 0.5, 3.0, weights=np.exp(1j * rng.uniform(-3, 3, 48)))
     if srp_shift:
         ap = case.aperture
         srp = np.tile(np.array([12.0, -3.0, 0.0]), (48, 1))
         case.aperture = NumpySimpleSarAperture(ap.transmitter_positions, ap.receiver_positions, srp,
-                                               ap.centre_frequency, ap.sample_bandwidth, num_freqs=4096,
+                                               ap.centre_frequency, ap.sample_bandwidth, num_freqs=nf,
                                                slow_time_weighting=ap.slow_time_weighting)
     plan = SarPlan(case.scene, case.aperture, upsample_ratio=8.0, interp=mode)
     assert plan.fused_upsampling and plan.fused_downsampling
     assert plan.profile_first_bin < 0
-    y = crandn(rng, 48, 4096)
+    y = crandn(rng, 48, nf)
     got = gpu_adjoint(plan, y)
     ref = oracle.adjoint(case.problem(), y, mode, threads=8)
     tol = LINEAR_TOL if mode == "linear" else NEAREST_TOL
