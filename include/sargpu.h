@@ -121,7 +121,7 @@ typedef struct sar_plan_info {
     int fused_upsampling;       /* 1: the backprojection's range profiles come from the fused
                                    upsampling kernel (N = 1024, 2048 or 4096, M a multiple of N), 0: cuFFT */
     int fused_downsampling;     /* 1: the forward projection's FFT side is the fused downsampling
-                                   kernel (N = 4096, M a multiple of N), 0: cuFFT */
+                                   kernel (N = 1024, 2048 or 4096, M a multiple of N), 0: cuFFT */
 } sar_plan_info;
 
 /* Create a plan on `device` (-1: the current device).  Copies all host inputs. */

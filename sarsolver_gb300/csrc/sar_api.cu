@@ -118,9 +118,9 @@ struct sar_plan {
     float2* d_wadj = nullptr;
     float2* d_wfwd = nullptr;
     void* d_spec = nullptr;        // FFT rows: float2, or double2 when fft_double
-    // fused adjoint upsampling (N = 4096, M a multiple of N): twiddle tables e^{2 pi i q / N}, e^{2 pi i q / M}
+    // fused up/downsampling (N = 1024, 2048, 4096; M a multiple of N): twiddle tables e^{2 pi i q / N}, e^{2 pi i q / M}
     bool fused_up = false;
-    bool fused_down = false;   // fused forward downsampling (N = 4096, M a multiple of N, Lg <= M)
+    bool fused_down = false;   // fused forward downsampling (those N, M a multiple of N, Lg <= M)
     float2* d_tw_n = nullptr;
     float2* d_tw_m = nullptr;
     bool fft_double = false;
@@ -627,7 +627,7 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
         p->have_tail = true;
         p->tail_rows = tail;
     }
-    // Fused adjoint upsampling: for N = 4096 and M a multiple of N the backprojection's range
+    // Fused adjoint upsampling: for N = 1024, 2048 or 4096 and M a multiple of N the backprojection's range
     // profiles come from one kernel (eight-way split of the length-M transform into N-point ones,
     // stored span only) instead of pack + inverse FFT + unpack; twiddles computed in FP64.
     const bool up_ok = upsample_fused_supported((int)N, (long)M, p->Lg);
