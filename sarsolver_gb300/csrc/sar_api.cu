@@ -628,7 +628,7 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
         p->tail_rows = tail;
     }
     // Fused adjoint upsampling: for N = 1024, 2048 or 4096 and M a multiple of N the backprojection's range
-    // profiles come from one kernel (eight-way split of the length-M transform into N-point ones,
+    // profiles come from one kernel (U-way split of the length-M transform into N-point ones,
     // stored span only) instead of pack + inverse FFT + unpack; twiddles computed in FP64.
     const bool up_ok = upsample_fused_supported((int)N, (long)M, p->Lg);
     const bool down_ok = downsample_fused_supported((int)N, (long)M, p->Lg);
