@@ -772,6 +772,11 @@ __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, 
 // those three bins in registers for both pulses and adds them to the windows once per group, in
 // three phases (lanes' bins are distinct at any one row, MODE >= 1), instead of two
 // read-modify-writes per contribution.
+//
+// With u = v + 1/2 the tap position (taps floor(u), floor(u) + 1) and a = u - (n0 + 1) in [-1, 1),
+// the three slot weights are the hat functions max(0, -a), 1 - |a| and max(0, a).  The lane keeps
+// per pulse the sums C = sum c, D = sum a c and E = sum |a| c, packed over the pulse pair, and
+// the slots are (E - D) / 2, C - E and (E + D) / 2: no per-row bin test or weight selection.
 constexpr float kRunSpan = 0.98f;
 
 template <bool TWO, int G>
@@ -780,8 +785,8 @@ __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float 
                                                   int ws, int lane) {
     const float2 cph = f2(ctp.cph, ctq.cph), b1 = f2(ctp.b1, ctq.b1), b2 = f2(ctp.b2, ctq.b2), c9 = f2(c9p, c9q);
     const float2 cv = f2(ctp.cv, ctq.cv), bv1 = f2(ctp.bv1, ctq.bv1), bv2 = f2(ctp.bv2, ctq.bv2);
-    const float2 SH = f2(SAR_SHIFTER, SAR_SHIFTER), NSH = f2(-SAR_SHIFTER, -SAR_SHIFTER);
-    const float2 M1 = f2(-1.f, -1.f), TWO_PI2 = f2(SAR_TWO_PI, SAR_TWO_PI), HALF = f2(0.5f, 0.5f);
+    const float2 SH = f2(SAR_SHIFTER, SAR_SHIFTER);
+    const float2 M1 = f2(-1.f, -1.f), TWO_PI2 = f2(SAR_TWO_PI, SAR_TWO_PI);
 #pragma unroll
   for (int g0 = 0; g0 < 16; g0 += G) {
     // window slot n0 of each pulse: the smaller bin of the group's first and last rows
@@ -793,8 +798,10 @@ __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float 
         n0p = min(max(min(__float_as_int(ra.x), __float_as_int(rb.x)) - SAR_SHIFTER_BITS + off_p, 0), ws - 3);
         n0q = min(max(min(__float_as_int(ra.y), __float_as_int(rb.y)) - SAR_SHIFTER_BITS + off_q, 0), ws - 3);
     }
-    const int hp = n0p - off_p + SAR_SHIFTER_BITS, hq = n0q - off_q + SAR_SHIFTER_BITS;   // bits of bin n0
-    float ap[3][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}}, aq[3][2] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    // -(n0 + 1/2) in the frame of v (exact for |n0| < 2^22), so that a = v - (n0 + 1/2)
+    const float2 nc = f2(-((float)(n0p - off_p) + 0.5f), -((float)(n0q - off_q) + 0.5f));
+    float2 Cr = f2(0.f, 0.f), Ci = f2(0.f, 0.f), Dr = f2(0.f, 0.f), Di = f2(0.f, 0.f);
+    float2 Er = f2(0.f, 0.f), Ei = f2(0.f, 0.f);
 #pragma unroll 4
     for (int rr = g0; rr < g0 + G; ++rr) {
         const float dj = (float)(rr - 8);
@@ -803,35 +810,34 @@ __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float 
         const float2 ph = fma2(fma2(fma2(c9, d, b2), d, b1), d, cph);
         const float2 f = fma2(f2(rintf(ph.x), rintf(ph.y)), M1, ph);   // ph - rint(ph), exact
         const float2 v = fma2(fma2(bv2, d, bv1), d, cv);
-        const float2 r1 = add2(v, SH);
-        const float2 sv = fma2(add2(r1, NSH), M1, v);                   // v - rint(v), exact
+        const float2 av = add2(v, nc);
+        const float2 aa = f2(fabsf(av.x), fabsf(av.y));
         const float2 x = mul2(f, TWO_PI2);
         float2 sn, cn;
         __sincosf(x.x, &sn.x, &cn.x);
         __sincosf(x.y, &sn.y, &cn.y);
-        const float2 w0 = fma2(sv, M1, HALF), w1 = add2(HALF, sv);      // taps n and n + 1
         // c = x exp(+2 pi i f) for both pulses
-        const float crp = fmaf(xv.x, cn.x, -xv.y * sn.x), cip = fmaf(xv.x, sn.x, xv.y * cn.x);
-        {
-            const bool up = __float_as_int(r1.x) != hp;                 // n = n0 + 1
-            const float a0 = up ? 0.f : w0.x, a1 = up ? w0.x : w1.x, a2 = up ? w1.x : 0.f;
-            ap[0][0] = fmaf(a0, crp, ap[0][0]); ap[0][1] = fmaf(a0, cip, ap[0][1]);
-            ap[1][0] = fmaf(a1, crp, ap[1][0]); ap[1][1] = fmaf(a1, cip, ap[1][1]);
-            ap[2][0] = fmaf(a2, crp, ap[2][0]); ap[2][1] = fmaf(a2, cip, ap[2][1]);
-        }
-        if (TWO) {
-            const float crq = fmaf(xv.x, cn.y, -xv.y * sn.y), ciq = fmaf(xv.x, sn.y, xv.y * cn.y);
-            const bool up = __float_as_int(r1.y) != hq;
-            const float a0 = up ? 0.f : w0.y, a1 = up ? w0.y : w1.y, a2 = up ? w1.y : 0.f;
-            aq[0][0] = fmaf(a0, crq, aq[0][0]); aq[0][1] = fmaf(a0, ciq, aq[0][1]);
-            aq[1][0] = fmaf(a1, crq, aq[1][0]); aq[1][1] = fmaf(a1, ciq, aq[1][1]);
-            aq[2][0] = fmaf(a2, crq, aq[2][0]); aq[2][1] = fmaf(a2, ciq, aq[2][1]);
-        }
+        const float2 cr = f2(fmaf(xv.x, cn.x, -xv.y * sn.x), fmaf(xv.x, cn.y, -xv.y * sn.y));
+        const float2 ci = f2(fmaf(xv.x, sn.x, xv.y * cn.x), fmaf(xv.x, sn.y, xv.y * cn.y));
+        Cr = add2(Cr, cr);
+        Ci = add2(Ci, ci);
+        Dr = fma2(av, cr, Dr);
+        Di = fma2(av, ci, Di);
+        Er = fma2(aa, cr, Er);
+        Ei = fma2(aa, ci, Ei);
     }
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        rmw_add(wp, n0p + j, 1.0f, ap[j][0], ap[j][1]);
-        if (TWO) rmw_add(wq, n0q + j, 1.0f, aq[j][0], aq[j][1]);
+    {
+        const float2 s0r = mul2(add2(Er, mul2(Dr, M1)), f2(0.5f, 0.5f)), s0i = mul2(add2(Ei, mul2(Di, M1)), f2(0.5f, 0.5f));
+        const float2 s1r = add2(Cr, mul2(Er, M1)), s1i = add2(Ci, mul2(Ei, M1));
+        const float2 s2r = mul2(add2(Er, Dr), f2(0.5f, 0.5f)), s2i = mul2(add2(Ei, Di), f2(0.5f, 0.5f));
+        rmw_add(wp, n0p, 1.0f, s0r.x, s0i.x);
+        if (TWO) rmw_add(wq, n0q, 1.0f, s0r.y, s0i.y);
+        __syncwarp();
+        rmw_add(wp, n0p + 1, 1.0f, s1r.x, s1i.x);
+        if (TWO) rmw_add(wq, n0q + 1, 1.0f, s1r.y, s1i.y);
+        __syncwarp();
+        rmw_add(wp, n0p + 2, 1.0f, s2r.x, s2i.x);
+        if (TWO) rmw_add(wq, n0q + 2, 1.0f, s2r.y, s2i.y);
         __syncwarp();
     }
   }
