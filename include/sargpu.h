@@ -122,6 +122,8 @@ typedef struct sar_plan_info {
                                    upsampling kernel (N = 1024, 2048 or 4096, M a multiple of N), 0: cuFFT */
     int fused_downsampling;     /* 1: the forward projection's FFT side is the fused downsampling
                                    kernel (N = 1024, 2048 or 4096, M a multiple of N), 0: cuFFT */
+    int scatter_lanes_y;        /* 1: the grid forward scatter runs warp lanes along y and walks the
+                                   tile along x (bins change more slowly along x), 0: lanes along x */
 } sar_plan_info;
 
 /* Create a plan on `device` (-1: the current device).  Copies all host inputs. */

@@ -85,6 +85,7 @@ class SarPlanInfo(ctypes.Structure):
         ("tile_window", c_size_t), ("strip_window", c_size_t), ("device_bytes", c_size_t), ("grid", c_int),
         ("interp", c_int), ("num_fast_times", c_size_t), ("num_slow_times", c_size_t), ("num_scatterers", c_size_t),
         ("device", c_int), ("fft_callbacks", c_int), ("gather_lanes_y", c_int), ("fused_upsampling", c_int), ("fused_downsampling", c_int),
+        ("scatter_lanes_y", c_int),
     ]
 
 
@@ -221,6 +222,7 @@ def load_host() -> ctypes.CDLL:
         P = c_void_p
         lib.sar_geom_host_eval.argtypes = [P, P, P, P, c_int, c_int, c_int, c_size_t, P, P, P, c_double, c_double,
                                            ctypes.c_float, c_int, P, P]
+        lib.sar_geom_host_eval_transposed.argtypes = lib.sar_geom_host_eval.argtypes
         lib.sar_geom_host_eval_points.argtypes = [P, c_size_t, P, c_size_t, P, P, P, c_double, c_double,
                                                   ctypes.c_float, P, P]
         _HOST = lib

@@ -14,11 +14,13 @@
 
 using namespace sar;
 
-extern "C" int sar_geom_host_eval(const double* origin, const double* ex, const double* ey,
-                                  const double* ez, int nx, int ny, int nz, size_t num_pulses,
-                                  const double* tx, const double* rx, const double* srp,
-                                  double kappa, double s_r, float bin_offset, int precise_bins,
-                                  float* phase_out, double* bin_out) {
+// transposed: the forward scatter's other layout, where a thread holds dj and walks di
+// (row_terms); otherwise a thread holds di and walks dj (column_terms), as the backprojection
+// and the default scatter layout do.
+static int geom_host_eval(const double* origin, const double* ex, const double* ey, const double* ez, int nx,
+                          int ny, int nz, size_t num_pulses, const double* tx, const double* rx,
+                          const double* srp, double kappa, double s_r, float bin_offset, int precise_bins,
+                          bool transposed, float* phase_out, double* bin_out) {
     if (nx <= 0 || ny <= 0 || nz <= 0) return 1;
     GridConst g = make_grid_const(ex, ey, ez, kappa, s_r, bin_offset, nx, ny, nz);
     g.precise_bins = precise_bins;
@@ -51,21 +53,49 @@ extern "C" int sar_geom_host_eval(const double* origin, const double* ex, const 
                             float di = (float)(li - 8 - 16 * (q & 1));
                             float dj = (float)(lj - 8 - 16 * (q >> 1));
                             const bool pr = g.precise_bins != 0;
-                            ColumnTerms ct = pr ? column_terms<true>(co[q], di, di * di, di * di * di)
-                                                : column_terms<false>(co[q], di, di * di, di * di * di);
-                            float ph = pixel_phase(ct, co[q].c[9], dj, dj * dj, dj * dj * dj);
-                            float v = pr ? pixel_bin<true>(ct, co[q].w[3], dj, dj * dj, dj * dj * dj)
-                                         : pixel_bin<false>(ct, 0.0f, dj, dj * dj, dj * dj * dj);
+                            // u: the offset a thread holds, d: the one it walks
+                            const float u = transposed ? dj : di, d = transposed ? di : dj;
+                            ColumnTerms ct;
+                            if (transposed)
+                                ct = pr ? row_terms<true>(co[q], u, u * u, u * u * u)
+                                        : row_terms<false>(co[q], u, u * u, u * u * u);
+                            else
+                                ct = pr ? column_terms<true>(co[q], u, u * u, u * u * u)
+                                        : column_terms<false>(co[q], u, u * u, u * u * u);
+                            const float c9 = transposed ? co[q].c[6] : co[q].c[9];
+                            const float w9 = transposed ? co[q].w[0] : co[q].w[3];
+                            const float ib = transposed ? co[q].ia : co[q].ib;
+                            float ph = pixel_phase(ct, c9, d, d * d, d * d * d);
+                            float v = pr ? pixel_bin<true>(ct, w9, d, d * d, d * d * d)
+                                         : pixel_bin<false>(ct, 0.0f, d, d * d, d * d * d);
                             size_t p = ((size_t)k * ny + j) * nx + i;
                             phase_out[s * P + p] = ph - round_shift(ph);
                             // the kernels' bin index and in-bin coordinate, recombined
-                            BinPos bp = pr ? bin_position<true>(v, fmaf(co[q].ib, dj, ct.ci))
+                            BinPos bp = pr ? bin_position<true>(v, fmaf(ib, d, ct.ci))
                                            : bin_position<false>(v, 0.0f);
                             bin_out[s * P + p] = (double)base + (double)bp.n + (double)bp.s;
                         }
                 }
     }
     return 0;
+}
+
+extern "C" int sar_geom_host_eval(const double* origin, const double* ex, const double* ey,
+                                  const double* ez, int nx, int ny, int nz, size_t num_pulses,
+                                  const double* tx, const double* rx, const double* srp,
+                                  double kappa, double s_r, float bin_offset, int precise_bins,
+                                  float* phase_out, double* bin_out) {
+    return geom_host_eval(origin, ex, ey, ez, nx, ny, nz, num_pulses, tx, rx, srp, kappa, s_r, bin_offset,
+                          precise_bins, false, phase_out, bin_out);
+}
+
+extern "C" int sar_geom_host_eval_transposed(const double* origin, const double* ex, const double* ey,
+                                             const double* ez, int nx, int ny, int nz, size_t num_pulses,
+                                             const double* tx, const double* rx, const double* srp,
+                                             double kappa, double s_r, float bin_offset, int precise_bins,
+                                             float* phase_out, double* bin_out) {
+    return geom_host_eval(origin, ex, ey, ez, nx, ny, nz, num_pulses, tx, rx, srp, kappa, s_r, bin_offset,
+                          precise_bins, true, phase_out, bin_out);
 }
 
 // Unstructured-position scheme: phase (cycles, [-0.5, 0.5]) and bin position per point.

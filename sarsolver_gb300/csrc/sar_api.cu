@@ -756,6 +756,7 @@ int sar_plan_get_info(const sar_plan* p, sar_plan_info* info) {
     info->gather_lanes_y = p->lanes_y;
     info->fused_upsampling = p->fused_up ? 1 : 0;
     info->fused_downsampling = p->fused_down ? 1 : 0;
+    info->scatter_lanes_y = (p->grid && !p->forward_points && !p->lanes_y) ? 1 : 0;
     return SAR_OK;
 }
 
@@ -887,6 +888,9 @@ int sar_forward(sar_plan* p, const void* x_dev, void* y_dev, void* stream) {
         a.ws = p->ws;
         a.pbf = p->pbf;
         a.linear = p->interp == SAR_INTERP_LINEAR;
+        // the scatter walks the axis along which bins change slowly: the transpose of the gather's
+        // lane choice
+        a.transposed = p->lanes_y ? 0 : 1;
         SAR_CUDA(launch_fp_grid_ws(a, st), "forward scatter");
     } else {
         SAR_CUDA(launch_fp_points(point_args(p, p->interp == SAR_INTERP_LINEAR ? BIN_LINEAR : BIN_FWD_NEAREST), (const float2*)x_dev, acc, st),

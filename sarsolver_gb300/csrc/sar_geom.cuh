@@ -383,6 +383,29 @@ SAR_HD ColumnTerms column_terms(const Coeffs& q, float di, float di2, float di3)
     return t;
 }
 
+// The same terms with the roles of the offsets exchanged: a thread at fixed dj walks di (rows of
+// a transposed tile).  The returned polynomials are in di; the di^3 coefficients are c6 (phase)
+// and w0 (split bins), and the exact integer part is i0 + ib dj + ia di.
+template <bool PRECISE>
+SAR_HD ColumnTerms row_terms(const Coeffs& q, float dj, float dj2, float dj3) {
+    ColumnTerms t;
+    t.cph = fmaf(q.c[9], dj3, fmaf(q.c[5], dj2, fmaf(q.c[2], dj, q.c[0])));
+    t.b1 = fmaf(q.c[8], dj2, fmaf(q.c[4], dj, q.c[1]));
+    t.b2 = fmaf(q.c[7], dj, q.c[3]);
+    if (PRECISE) {
+        t.cv = fmaf(q.w[3], dj3, fmaf(q.v[5], dj2, fmaf(q.v[2], dj, q.v[0])));
+        t.bv1 = fmaf(q.w[2], dj2, fmaf(q.v[4], dj, q.v[1]));
+        t.bv2 = fmaf(q.w[1], dj, q.v[3]);
+        t.ci = fmaf(q.ib, dj, q.i0);
+    } else {
+        t.cv = fmaf(q.v[5], dj2, fmaf(q.v[2], dj, q.v[0]));
+        t.bv1 = fmaf(q.v[4], dj, q.v[1]);
+        t.bv2 = q.v[3];
+        t.ci = 0.0f;
+    }
+    return t;
+}
+
 SAR_HD float pixel_phase(const ColumnTerms& t, float c9, float dj, float dj2, float dj3) {
     return fmaf(c9, dj3, fmaf(t.b2, dj2, fmaf(t.b1, dj, t.cph)));
 }

@@ -111,7 +111,9 @@ struct PixelEval {
     int n;      // bin relative to the tile's base bin
 };
 
-template <bool PRECISE>
+// The thread's polynomials in the offset it walks, from a coefficient set: in dj for a fixed di
+// (TRANSPOSED false), or in di for a fixed dj (TRANSPOSED true; tt.di then holds the dj offset).
+template <bool PRECISE, bool TRANSPOSED = false>
 __device__ __forceinline__ ColumnTerms load_column(const float4* cs, const TileThread& tt, float& c9,
                                                    float& w9, float& ib) {
     const float4 A = cs[0], B = cs[1], C = cs[2], D = cs[3];
@@ -129,12 +131,18 @@ __device__ __forceinline__ ColumnTerms load_column(const float4* cs, const TileT
         co.i0 = co.ia = co.ib = 0.f;
         co.w[0] = co.w[1] = co.w[2] = co.w[3] = 0.f;
     }
-    ib = co.ib;
-    w9 = co.w[3];
     co.c[0] = A.x; co.c[1] = A.y; co.c[2] = A.z; co.c[3] = A.w;
     co.c[4] = B.x; co.c[5] = B.y; co.c[6] = B.z; co.c[7] = B.w;
     co.c[8] = C.x; co.c[9] = C.y; co.v[0] = C.z; co.v[1] = C.w;
     co.v[2] = D.x; co.v[3] = D.y; co.v[4] = D.z; co.v[5] = D.w;
+    if (TRANSPOSED) {
+        ib = co.ia;
+        w9 = co.w[0];
+        c9 = co.c[6];
+        return row_terms<PRECISE>(co, tt.di, tt.di2, tt.di3);
+    }
+    ib = co.ib;
+    w9 = co.w[3];
     c9 = co.c[9];
     return column_terms<PRECISE>(co, tt.di, tt.di2, tt.di3);
 }
@@ -639,7 +647,12 @@ cudaError_t launch_bp_grid_ws(const BpGridArgs& a, cudaStream_t st) {
 // so plain read-modify-writes are safe: first to bin n, then to bin n + 1, with __syncwarp in
 // between.  Otherwise shared-memory atomics are used.  After the strip the windows are merged
 // into the global accumulator with one atomic add per bin.
+// Template argument TRANSPOSED: lanes run along y and the warp walks the tile's 32 columns (the
+// image tile is staged transposed, rows padded to 33 values), for collections whose range bins
+// change fast along y and slowly along x; the producer's tests then take the bin rates along y
+// for the lanes and along x for the rows.
 constexpr float kFastBinRate = 1.05f;
+constexpr int kXtStride = kTile + 1;   // staged image tile: 32 lines of 33 values
 
 __device__ __forceinline__ size_t align_up(size_t n, size_t a) { return (n + a - 1) & ~(a - 1); }
 
@@ -655,7 +668,7 @@ __host__ __device__ inline FpWsLayout fp_ws_layout(int ws, int pbf) {
     L.coef = L.win + (size_t)pbf * window_slots(ws) * sizeof(float2);
     L.coef = (L.coef + 15) & ~(size_t)15;
     L.xt = L.coef + (size_t)2 * pbf * 4 * kSetF4 * sizeof(float4);
-    L.base = L.xt + (size_t)2 * kTile * kTile * sizeof(float2);
+    L.base = L.xt + (size_t)2 * kTile * kXtStride * sizeof(float2);
     L.fast = L.base + (size_t)2 * pbf * sizeof(int);
     L.wst = L.fast + (size_t)2 * pbf * sizeof(int);
     L.bars = (L.wst + (size_t)pbf * sizeof(int) + 7) & ~(size_t)7;
@@ -709,7 +722,7 @@ __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, 
 #pragma unroll 2
     for (int rr = 0; rr < 16; ++rr) {
         const float dj = (float)(rr - 8);
-        const float2 xv = xrow[rr * kTile + lane];
+        const float2 xv = xrow[rr * kXtStride + lane];
         const RowEval<PRECISE> ep = scatter_eval<PRECISE>(ctp, c9p, w9p, ibp, dj, xv);
         const int ip = (int)min((unsigned)(ep.bp.n + off_p), (unsigned)(ws - 2));
         RowEval<PRECISE> eq;
@@ -806,7 +819,7 @@ __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float 
     for (int rr = g0; rr < g0 + G; ++rr) {
         const float dj = (float)(rr - 8);
         const float2 d = f2(dj, dj);
-        const float2 xv = xrow[rr * kTile + lane];
+        const float2 xv = xrow[rr * kXtStride + lane];
         const float2 ph = fma2(fma2(fma2(c9, d, b2), d, b1), d, cph);
         const float2 f = fma2(f2(rintf(ph.x), rintf(ph.y)), M1, ph);   // ph - rint(ph), exact
         const float2 v = fma2(fma2(bv2, d, bv1), d, cv);
@@ -870,7 +883,7 @@ __device__ __forceinline__ void scatter_half(int mode, const ColumnTerms& ctp, f
         scatter_rows<LINEAR, PRECISE, 0, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane);
 }
 
-template <bool LINEAR, bool PRECISE>
+template <bool LINEAR, bool PRECISE, bool TRANSPOSED>
 __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridArgs a) {
     extern __shared__ __align__(16) unsigned char fsm[];
     const int pbf = a.pbf, ws = a.ws, wslots = window_slots(ws);
@@ -921,12 +934,13 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
             const int tj = tj0 + t;
             if (lane < 4) anchors[lane] = subtile_anchor(ti, tj, k, lane, g);
             // this warp's half of the tile's image values (rows 16 pw .. 16 pw + 15)
-            float2* xt = xt0 + b * kTile * kTile;
+            float2* xt = xt0 + b * kTile * kXtStride;
             const int i = ti * kTile + lane;
             for (int r = 16 * pw; r < 16 * pw + 16; ++r) {
                 const int j = tj * kTile + r;
-                xt[r * kTile + lane] =
+                const float2 xv =
                     (i < g.nx && j < g.ny) ? a.x[((size_t)k * g.ny + j) * g.nx + i] : make_float2(0.f, 0.f);
+                xt[TRANSPOSED ? lane * kXtStride + r : r * kXtStride + lane] = xv;   // line = walked offset
             }
             __syncwarp();
             float4* coef = coef0 + b * pbf * 4 * kSetF4;
@@ -944,17 +958,21 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                 if (pi < npb) {
                     const float4* cs = coef + (pi * 4 + q) * kSetF4;
                     const float4 C = cs[2], D = cs[3], E = cs[4];
-                    const float r1 = C.w + E.x;                     // v1 (+ ia in precise mode)
-                    const float rmin = fabsf(r1) - 16.0f * fabsf(D.y) - 8.0f * fabsf(D.z);
+                    // bin rates along x: dv/di = v1 (+ ia) + 2 v3 di + v4 dj; along y: dv/dj = v2 (+ ib) +
+                    // v4 di + 2 v5 dj, with di, dj in [-8, 7]
+                    const float rx = C.w + E.x, ry = D.x + E.y;
+                    const float cx = 16.0f * fabsf(D.y) + 8.0f * fabsf(D.z), cy = 8.0f * fabsf(D.z) + 16.0f * fabsf(D.w);
+                    const float r1 = TRANSPOSED ? ry : rx;            // along the lanes
+                    const float rmin = fabsf(r1) - (TRANSPOSED ? cy : cx);
                     ok_q = rmin >= kFastBinRate;
                     wide_q = rmin >= kFastBinRate + 1.0f;
                     pos_q = r1 > 0.0f;
-                    // bin down the 16 rows of the sub-tile: monotonic (dv/dj = v2 + v4 di + 2 v5 dj keeps
-                    // its sign) and changing by less than kRunSpan in all
-                    const float curv = 8.0f * fabsf(D.z) + 16.0f * fabsf(D.w);
-                    runs_q = fabsf(D.x) > curv && 15.0f * (fabsf(D.x) + curv) < kRunSpan;    // 16-row runs
-                    runs8_q = fabsf(D.x) > curv && 7.0f * (fabsf(D.x) + curv) < kRunSpan;    // 8-row runs
-                    runs4_q = fabsf(D.x) > curv && 3.0f * (fabsf(D.x) + curv) < kRunSpan;    // 4-row runs
+                    // bin down the 16 walked lines of the sub-tile: monotonic (the rate keeps its
+                    // sign) and changing by less than kRunSpan in all
+                    const float rw = fabsf(TRANSPOSED ? C.w : D.x), curv = TRANSPOSED ? cx : cy;
+                    runs_q = rw > curv && 15.0f * (rw + curv) < kRunSpan;    // 16-line runs
+                    runs8_q = rw > curv && 7.0f * (rw + curv) < kRunSpan;    // 8-line runs
+                    runs4_q = rw > curv && 3.0f * (rw + curv) < kRunSpan;    // 4-line runs
                 }
                 const unsigned all4 = __ballot_sync(0xffffffffu, ok_q);
                 const unsigned wide4 = __ballot_sync(0xffffffffu, wide_q);
@@ -998,7 +1016,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
         if (ok && !mbar_wait(&bars[b], (t >> 1) & 1, 32, 256)) ok = false;
         if (ok) {
             const float4* coef = coef0 + b * pbf * 4 * kSetF4;
-            const float2* xt = xt0 + b * kTile * kTile;
+            const float2* xt = xt0 + b * kTile * kXtStride;
             // Pulses are processed in pairs (p, p + 8): both share each image value and give the
             // warp two independent accumulation chains.
             for (int p = warp; p < npb; p += 2 * (kWsConsumers / 32)) {
@@ -1013,11 +1031,13 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
 #pragma unroll
                 for (int half = 0; half < 2; ++half) {
                     float c9p, w9p, ibp, c9q, w9q, ibq;
+                    // sub-tile: lanes >= 16 are its upper half along the lane axis, half along the other
+                    const int qs = TRANSPOSED ? half + 2 * qx : qx + 2 * half;
                     const ColumnTerms ctp =
-                        load_column<PRECISE>(coef + (p * 4 + qx + 2 * half) * kSetF4, tt, c9p, w9p, ibp);
+                        load_column<PRECISE, TRANSPOSED>(coef + (p * 4 + qs) * kSetF4, tt, c9p, w9p, ibp);
                     const ColumnTerms ctq =
-                        load_column<PRECISE>(coef + (pq * 4 + qx + 2 * half) * kSetF4, tt, c9q, w9q, ibq);
-                    const float2* xrow = xt + 16 * half * kTile;
+                        load_column<PRECISE, TRANSPOSED>(coef + (pq * 4 + qs) * kSetF4, tt, c9q, w9q, ibq);
+                    const float2* xrow = xt + 16 * half * kXtStride;
                     if (two)
                         scatter_half<LINEAR, PRECISE, true>(mode, ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq,
                                                             off_p, off_q, ws, lane);
@@ -1053,22 +1073,29 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
     }
 }
 
-template <bool LINEAR, bool PRECISE>
+template <bool LINEAR, bool PRECISE, bool TRANSPOSED>
 static cudaError_t launch_fp_grid_ws_t(const FpGridArgs& a, cudaStream_t st) {
     const size_t smem = fp_grid_ws_smem_bytes(a.ws, a.pbf);
     const dim3 grid((unsigned)(a.segs_per_column * a.g.tiles_x * a.g.nz), (unsigned)((a.S + a.pbf - 1) / a.pbf));
-    cudaError_t e = cudaFuncSetAttribute(fp_grid_ws_kernel<LINEAR, PRECISE>,
+    cudaError_t e = cudaFuncSetAttribute(fp_grid_ws_kernel<LINEAR, PRECISE, TRANSPOSED>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    fp_grid_ws_kernel<LINEAR, PRECISE><<<grid, kWsThreads, smem, st>>>(a);
+    fp_grid_ws_kernel<LINEAR, PRECISE, TRANSPOSED><<<grid, kWsThreads, smem, st>>>(a);
     return cudaGetLastError();
+}
+
+template <bool TRANSPOSED>
+static cudaError_t launch_fp_grid_ws_o(const FpGridArgs& a, cudaStream_t st) {
+    if (a.linear)
+        return a.g.precise_bins ? launch_fp_grid_ws_t<true, true, TRANSPOSED>(a, st)
+                                : launch_fp_grid_ws_t<true, false, TRANSPOSED>(a, st);
+    return a.g.precise_bins ? launch_fp_grid_ws_t<false, true, TRANSPOSED>(a, st)
+                            : launch_fp_grid_ws_t<false, false, TRANSPOSED>(a, st);
 }
 
 cudaError_t launch_fp_grid_ws(const FpGridArgs& a, cudaStream_t st) {
     if (a.pbf < 8 || a.pbf > 32 || (a.pbf & 7) || a.ws < 32 || (a.ws & 31)) return cudaErrorInvalidValue;
-    if (a.linear)
-        return a.g.precise_bins ? launch_fp_grid_ws_t<true, true>(a, st) : launch_fp_grid_ws_t<true, false>(a, st);
-    return a.g.precise_bins ? launch_fp_grid_ws_t<false, true>(a, st) : launch_fp_grid_ws_t<false, false>(a, st);
+    return a.transposed ? launch_fp_grid_ws_o<true>(a, st) : launch_fp_grid_ws_o<false>(a, st);
 }
 
 // ------------------------------------------------------- K2 / K3 (points)

@@ -57,6 +57,7 @@ struct FpGridArgs {
     int ws;                    // strip window length (bins), multiple of 32
     int pbf;                   // pulses per CTA (multiple of 8, <= 32)
     int linear;                // 1: linear interpolation weights; 0: nearest bin
+    int transposed;            // 1: lanes along y, rows walked along x (bins change slowly along x)
 };
 // Warp-specialised variant: producer warps stage image tiles and coefficient sets; each
 // gathering warp owns whole pulses, so its windows need no atomics when bins along a row of

@@ -111,6 +111,7 @@ class SarPlan:
         self.gather_lanes_y = bool(info.gather_lanes_y)
         self.fused_upsampling = bool(info.fused_upsampling)
         self.fused_downsampling = bool(info.fused_downsampling)
+        self.scatter_lanes_y = bool(info.scatter_lanes_y)
         # The aperture's own weighting; phase corrections multiply it (autodiff.phase_weights).
         self.base_weights = torch.as_tensor(
             np.asarray(aperture.slow_time_weighting, dtype=np.complex64).reshape(-1)).to(self.device)

@@ -20,15 +20,18 @@ def fp64_truth(tx, rx, srp, pos, kappa, s_r):
     return cyc - np.round(cyc), s_r * dr
 
 
-def host_eval_grid(scene, tx, rx, srp, kappa, s_r, bin_offset=0.0, precise=0):
+def host_eval_grid(scene, tx, rx, srp, kappa, s_r, bin_offset=0.0, precise=0, transposed=False):
+    """transposed: the forward scatter's layout for collections looking along y (a thread holds
+    the y offset and walks x), otherwise the layout holding x and walking y."""
     lib = _lib.load_host()
+    fn = lib.sar_geom_host_eval_transposed if transposed else lib.sar_geom_host_eval
     shape, origin, ex, ey, ez = grid_axes(scene)
     nz, ny, nx = shape
     S = tx.shape[0]
     ph = np.zeros((S, nz * ny * nx), np.float32)
     bn = np.zeros((S, nz * ny * nx))
     arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (origin, ex, ey, ez, tx, rx, srp)]
-    assert lib.sar_geom_host_eval(*[a.ctypes.data for a in arrs[:4]], nx, ny, nz, S,
+    assert fn(*[a.ctypes.data for a in arrs[:4]], nx, ny, nz, S,
                                   *[a.ctypes.data for a in arrs[4:]], kappa, s_r, bin_offset, precise,
                                   ph.ctypes.data, bn.ctypes.data) == 0
     return ph, bn
@@ -72,6 +75,23 @@ def test_grid_phase_and_bin_precision(n, spacing, aperture, pulses):
     assert pmax < 1.0e-5, pmax      # radians
     assert prms < 1.5e-6, prms
     assert bmax < 5.0e-5, bmax      # range bins
+
+
+@pytest.mark.parametrize("transposed", [False, True])
+def test_turned_collection_precision_in_both_layouts(transposed):
+    """The benchmark image seen from 90 degrees (range along y): the scatter holds y and walks x
+    there (transposed), the backprojection holds x and walks y; both meet the same bounds."""
+    tx = spotlight(4096, 5.0, centre_az_deg=90.0)[[0, 2047, 4095]]
+    srp = np.zeros_like(tx)
+    n, spacing = 2048, 0.25
+    scene = GridSarScene([1, n, n], [0.0, spacing * (n - 1), spacing * (n - 1)])
+    kappa, s_r = 10.0e9 / C, 200.0e6 * 8 / C
+    ph, bn = host_eval_grid(scene, tx, tx, srp, kappa, s_r, transposed=transposed)
+    pos = scene.positions
+    for s in range(tx.shape[0]):
+        tp, tb = fp64_truth(tx[s], tx[s], srp[s], pos, kappa, s_r)
+        pmax, prms, bmax = errors(ph[s], bn[s], tp, tb)
+        assert pmax < 1.0e-5 and prms < 1.5e-6 and bmax < 5.0e-5, (pmax, prms, bmax)
 
 
 def test_bistatic_rotated_grid_precision():
@@ -122,9 +142,10 @@ def test_precise_bins_match_fp64_rounding_at_short_range_and_fine_bins():
     s_r = ap.sample_bandwidth * M / (ap.num_freqs * ap.c_eff)
     kappa = ap.centre_frequency / ap.c_eff
     pos = case.scene.positions
-    for precise, max_flips, max_err in ((0, None, 5e-4), (1, 10, 5e-6)):
+    for precise, max_flips, max_err, transposed in ((0, None, 5e-4, False), (1, 10, 5e-6, False),
+                                                    (1, 10, 5e-6, True)):
         ph, bn = host_eval_grid(case.scene, ap.transmitter_positions, ap.receiver_positions, ap.stab_ref_posns,
-                                kappa, s_r, 0.5, precise)
+                                kappa, s_r, 0.5, precise, transposed)
         flips, err = 0, 0.0
         for s in range(ap.num_slow_times):
             _, tb = fp64_truth(ap.transmitter_positions[s], ap.receiver_positions[s], ap.stab_ref_posns[s], pos,

@@ -120,9 +120,10 @@ def test_gather_lane_layouts_match_oracle(turn, mode):
     along y for a collection looking along x, along x once the collection is turned by 90
     degrees.  Both layouts against the FP64 oracle, with an odd pulse count (a padding pulse
     in the last stage of pulse pairs) and partial tiles; linear and split (nearest-bin) bins on
-    the grid path.  The forward projection of the same plans covers the scatter's register run
-    windows (bins barely move down the rows) and its atomic fallback (turned: bins change fast
-    down the rows, slowly along them)."""
+    the grid path.  The forward projection of the same plans runs its lanes the other way (along
+    the axis where bins change fast, walking the slow one): lanes along x, then lanes along y on
+    a transposed tile once turned, with register run windows (linear) and single-bin
+    read-modify-writes (nearest) in both layouts."""
     rng = np.random.default_rng(21 + turn)
     case = spotlight_case(37, 96, 70, 0.3, 4.0, weights=np.exp(1j * rng.uniform(-3, 3, 37)))
     if turn:
@@ -132,7 +133,7 @@ def test_gather_lane_layouts_match_oracle(turn, mode):
                                                ap.stab_ref_posns, ap.centre_frequency, ap.sample_bandwidth,
                                                num_freqs=ap.num_freqs, slow_time_weighting=ap.slow_time_weighting)
     plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp=mode, path="grid")
-    assert plan.gather_lanes_y == (turn == 0)
+    assert plan.gather_lanes_y == (turn == 0) and plan.scatter_lanes_y == (turn == 1)
     y = crandn(rng, 37, 96)
     tol = LINEAR_TOL if mode == "linear" else NEAREST_TOL
     e_a = rel_l2(gpu_adjoint(plan, y), oracle.adjoint(case.problem(), y, mode, threads=8))
@@ -199,7 +200,7 @@ def test_backproject_reads_pinned_host_input_in_place():
     assert op.plan.device_flags() == 0
 
 
-@pytest.mark.parametrize("kind", ["grid", "points", "bistatic"])
+@pytest.mark.parametrize("kind", ["grid", "points", "bistatic", "turned"])
 def test_dot_product_adjoint(kind):
     rng = np.random.default_rng(2)
     if kind == "points":
@@ -207,6 +208,12 @@ def test_dot_product_adjoint(kind):
     else:
         case = spotlight_case(96, 256, 100, 0.5, 5.0, bistatic=(kind == "bistatic"),
                               weights=np.exp(1j * rng.uniform(-2, 2, 96)))
+    if kind == "turned":   # looking along y: the scatter walks x on a transposed tile
+        ap = case.aperture
+        rot = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+        case.aperture = NumpySimpleSarAperture(ap.transmitter_positions @ rot.T, ap.receiver_positions @ rot.T,
+                                               ap.stab_ref_posns, ap.centre_frequency, ap.sample_bandwidth,
+                                               num_freqs=ap.num_freqs, slow_time_weighting=ap.slow_time_weighting)
     plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp="linear")
     x = torch.from_numpy(crandn(rng, case.scene.num_scatterers)).to(torch.complex64).cuda()
     y = torch.from_numpy(crandn(rng, case.aperture.num_slow_times, case.aperture.num_freqs)).to(torch.complex64).cuda()
