@@ -112,6 +112,7 @@ struct sar_plan {
 
     PulseGeom* d_pulses = nullptr;
     float4* d_alpha2 = nullptr;
+    double* d_steps = nullptr;      // grid steps ex, ey, ez (FP64) for exact nearest-bin decisions
     PointGeom* d_points = nullptr;
     float2* d_wave = nullptr;
     float2* d_w = nullptr;
@@ -171,6 +172,7 @@ struct sar_plan {
         DeviceGuard g(device);
         cudaFree(d_pulses);
         cudaFree(d_alpha2);
+        cudaFree(d_steps);
         cudaFree(d_points);
         cudaFree(d_wave);
         cudaFree(d_w);
@@ -368,6 +370,19 @@ int validate_geometry(const sar_geometry* g) {
     return SAR_OK;
 }
 
+// Tile window (bins) of the grid gather and whether it stages in shared memory: the grid paths
+// take nearest_ref by default only then (the wide-window fallback reads global memory and is
+// slower than the per-pixel kernel at the reference's default upsampling).
+static int grid_tile_window(const sar_geometry* g, double s_r) {
+    const double* ex = g->grid_step_x;
+    const double* ey = g->grid_step_y;
+    const double nex = std::sqrt(ex[0] * ex[0] + ex[1] * ex[1] + ex[2] * ex[2]);
+    const double ney = std::sqrt(ey[0] * ey[0] + ey[1] * ey[1] + ey[2] * ey[2]);
+    const double h = s_r * 2.0 * 16.0 * (nex + ney);
+    if (!(h <= 1.0e6)) return -1;
+    return (2 * ((int)std::ceil(h) + 3) + 3) & ~3;
+}
+
 int build_plan(const sar_geometry* g_in, sar_plan* p) {
     const sar_geometry* g = g_in;
     const size_t N = g->num_fast_times, S = g->num_slow_times, P = g->num_scatterers;
@@ -376,8 +391,14 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
     // A grid routed to the per-pixel path is expanded into explicit positions.
     sar_geometry expanded;
     std::vector<double> grid_positions;
+    bool nearest_staged = false;
+    if (grid && g->path == SAR_PATH_AUTO && g->interp == SAR_INTERP_NEAREST_REF && g->c_eff > 0.0 && N > 0) {
+        const int ww = grid_tile_window(g, g->sample_frequency * (double)M / ((double)N * g->c_eff));
+        nearest_staged = ww > 0 && bp_grid_ws_smem_bytes(ww, 8) <= kBpSmemBudget;
+    }
     const bool to_points =
-        grid && (g->path == SAR_PATH_POINTS || (g->path == SAR_PATH_AUTO && g->interp == SAR_INTERP_NEAREST_REF));
+        grid && (g->path == SAR_PATH_POINTS ||
+                 (g->path == SAR_PATH_AUTO && g->interp == SAR_INTERP_NEAREST_REF && !nearest_staged));
     if (to_points) {
         const size_t nz = g->grid_shape[0], ny = g->grid_shape[1], nx = g->grid_shape[2];
         grid_positions.resize(3 * P);
@@ -440,11 +461,8 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
         }
         // Tile window: every pixel of a tile lies within 16|ex| + 16|ey| of the tile centre,
         // and each of the two ranges changes by at most that distance.
-        const double nex = std::sqrt(ex[0] * ex[0] + ex[1] * ex[1] + ex[2] * ex[2]);
-        const double ney = std::sqrt(ey[0] * ey[0] + ey[1] * ey[1] + ey[2] * ey[2]);
-        const double h = s_r * 2.0 * 16.0 * (nex + ney);
-        if (h > 1.0e6) return fail(SAR_ERR_NOT_SUPPORTED, "grid spacing too coarse for the range sampling");
-        p->wwin = (2 * ((int)std::ceil(h) + 3) + 3) & ~3;
+        p->wwin = grid_tile_window(g, s_r);
+        if (p->wwin < 0) return fail(SAR_ERR_NOT_SUPPORTED, "grid spacing too coarse for the range sampling");
         p->lanes_y = choose_lanes_y(tx, rx, S, origin, ex, ey, ez, nx, ny, nz);
         // Nearest-bin decisions must match FP64, and wide tiles need the exact integer part:
         // split the linear bin rates in both cases (sar_geom.cuh, bin_coeffs).
@@ -567,6 +585,8 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
         p->Lg = (int)span;
         p->wwin = 0;
     }
+    // nearest bins on the grid paths: antenna norms for the exact decisions near a boundary
+    if (grid && p->interp == SAR_INTERP_NEAREST_REF) alpha2.resize(S);
     if (!alpha2.empty()) {
         for (size_t s = 0; s < S; ++s) {
             double at[3], ar[3];
@@ -587,8 +607,20 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
     if (!points.empty()) {
         if ((rc = p->alloc(&p->d_points, P, "point table"))) return rc;
         SAR_CUDA(cudaMemcpy(p->d_points, points.data(), sizeof(PointGeom) * P, cudaMemcpyHostToDevice), "point table");
+    }
+    if (!alpha2.empty()) {
         if ((rc = p->alloc(&p->d_alpha2, S, "antenna norms"))) return rc;
         SAR_CUDA(cudaMemcpy(p->d_alpha2, alpha2.data(), sizeof(float4) * S, cudaMemcpyHostToDevice), "antenna norms");
+    }
+    if (grid) {
+        double steps[9];
+        for (int c = 0; c < 3; ++c) {
+            steps[c] = g->grid_step_x[c];
+            steps[3 + c] = g->grid_step_y[c];
+            steps[6 + c] = g->grid_step_z[c];
+        }
+        if ((rc = p->alloc(&p->d_steps, 9, "grid steps"))) return rc;
+        SAR_CUDA(cudaMemcpy(p->d_steps, steps, sizeof steps, cudaMemcpyHostToDevice), "grid steps");
     }
     if (!strip_start.empty()) {
         if ((rc = p->alloc(&p->d_strip, strip_start.size(), "strip table"))) return rc;
@@ -850,6 +882,12 @@ int sar_adjoint(sar_plan* p, const void* y_dev, void* x_dev, void* stream) {
         a.staged = p->staged;
         a.accumulate = 0;
         a.lanes_y = p->lanes_y;
+    a.nearest = p->interp == SAR_INTERP_NEAREST_REF;
+    a.steps = p->d_steps;
+    a.alpha2 = p->d_alpha2;
+        a.nearest = p->interp == SAR_INTERP_NEAREST_REF;
+        a.steps = p->d_steps;
+        a.alpha2 = p->d_alpha2;
         SAR_CUDA(p->staged ? launch_bp_grid_ws(a, st) : launch_bp_grid(a, st), "backprojection");
     } else {
         SAR_CUDA(launch_bp_points(point_args(p, p->interp == SAR_INTERP_LINEAR ? BIN_LINEAR : BIN_ADJ_NEAREST), p->d_prof, (float2*)x_dev, 0, st),
@@ -891,6 +929,8 @@ int sar_forward(sar_plan* p, const void* x_dev, void* y_dev, void* stream) {
         // the scatter walks the axis along which bins change slowly: the transpose of the gather's
         // lane choice
         a.transposed = p->lanes_y ? 0 : 1;
+        a.steps = p->d_steps;
+        a.alpha2 = p->d_alpha2;
         SAR_CUDA(launch_fp_grid_ws(a, st), "forward scatter");
     } else {
         SAR_CUDA(launch_fp_points(point_args(p, p->interp == SAR_INTERP_LINEAR ? BIN_LINEAR : BIN_FWD_NEAREST), (const float2*)x_dev, acc, st),
@@ -959,6 +999,9 @@ int sar_adjoint_pulse_block(sar_plan* p, const void* y_block_dev, size_t first_p
     a.staged = p->staged;
     a.accumulate = accumulate ? 1 : 0;
     a.lanes_y = p->lanes_y;
+    a.nearest = p->interp == SAR_INTERP_NEAREST_REF;
+    a.steps = p->d_steps;
+    a.alpha2 = p->d_alpha2;
     SAR_CUDA(p->staged ? launch_bp_grid_ws(a, st) : launch_bp_grid(a, st), "backprojection");
     return SAR_OK;
 }

@@ -160,6 +160,49 @@ __device__ __forceinline__ PixelEval eval_pixel(const ColumnTerms& ct, float c9,
     return e;
 }
 
+// Nearest-bin sampling on the grid paths.  The FP32 bin coordinate s (about the chosen bin, in
+// [-0.5, 0.5]) is within ~5e-6 bins of the FP64 position (split bins, sar_geom.cuh); where |s|
+// exceeds kNearEdge the bin is decided again from the per-pixel double-float range with the
+// unstructured path's exact rule (exact_bin: FP64 rounding of the same value, ties away from
+// zero), so the grid kernels pick the bins the per-pixel path picks.  About 1e-4 of the
+// pixel·pulses take this branch.
+constexpr float kNearEdge = 0.49995f;
+
+// Stored-span index (bins from bg0) of grid pixel (i, j, k) for pulse s under nearest rule `rule`:
+// pixel offset from the grid origin in FP64 as the host forms it, then the double-float range and
+// rounding of the per-pixel kernels (eval_point).
+__device__ __noinline__ int exact_grid_bin(const double* __restrict__ steps, const PulseGeom* __restrict__ pulses,
+                                           const float4* __restrict__ alpha2, float sr_hi, float sr_lo, int bg0,
+                                           int rule, int i, int j, int k, int s) {
+    double q[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+        q[c] = __dadd_rn(__dadd_rn(__dmul_rn((double)i, steps[c]), __dmul_rn((double)j, steps[3 + c])),
+                         __dmul_rn((double)k, steps[6 + c]));
+    const double qq = __dadd_rn(__dadd_rn(__dmul_rn(q[0], q[0]), __dmul_rn(q[1], q[1])), __dmul_rn(q[2], q[2]));
+    PointGeom pt;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        pt.qh[c] = __double2float_rn(q[c]);
+        pt.ql[c] = __double2float_rn(__dsub_rn(q[c], (double)pt.qh[c]));
+    }
+    pt.qh[3] = __double2float_rn(qq);
+    pt.ql[3] = __double2float_rn(__dsub_rn(qq, (double)pt.qh[3]));
+    const PulseGeom pg = load_pulse(pulses + s);
+    const float4 a2 = __ldg(alpha2 + s);
+    df r = point_range(pulse_tx(pg), df_make(a2.x, a2.y), pt);
+    if (pg.monostatic != 0.0f)
+        r = df_mulf(r, 2.0f);
+    else
+        r = df_add(r, point_range(pulse_rx(pg), df_make(a2.z, a2.w), pt));
+    r = df_sub(r, df_make(pg.rref_hi, pg.rref_lo));
+    const df V = df_sub(df_mul(df_make(sr_hi, sr_lo), r), df_make((float)bg0, 0.0f));
+    int gi;
+    float sf;
+    exact_bin(V, bg0, rule, &gi, &sf);
+    return gi;
+}
+
 // ------------------------------------------------------------------- K2 (grid, wide windows)
 // Fallback for tiles whose range window is too wide to stage in shared memory: coefficient sets
 // per block of pulses in shared memory, profile pairs read straight from global memory (L2).
@@ -169,7 +212,7 @@ size_t bp_grid_smem_bytes(int wwin, int pb, int staged) {
     return ((size_t)pb * 4 * kSetF4 + (size_t)((pb + 3) / 4) + 6) * sizeof(float4);
 }
 
-template <bool PRECISE>
+template <bool PRECISE, bool NEAREST>
 __global__ void __launch_bounds__(kThreads, 2) bp_grid_kernel(const BpGridArgs a) {
     extern __shared__ float4 smem[];
     const int pb = a.pb;
@@ -201,7 +244,12 @@ __global__ void __launch_bounds__(kThreads, 2) bp_grid_kernel(const BpGridArgs a
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
                 const PixelEval e = eval_pixel<PRECISE>(ct, c9, w9, ib, tt, r);
-                const int gi = min(max(bb + e.n, 0), a.Lg - 1);
+                int gi = min(max(bb + e.n, 0), a.Lg - 1);
+                if (NEAREST && fabsf(e.sf) > kNearEdge)
+                    gi = min(max(exact_grid_bin(a.steps, a.pulses, a.alpha2, g.s_r.hi, g.s_r.lo, a.bg0,
+                                                BIN_ADJ_NEAREST, ti * kTile + (threadIdx.x & 31),
+                                                tj * kTile + 4 * (threadIdx.x >> 5) + r, k, s0 + pi),
+                                 0), a.Lg - 1);
                 const float4 pv = __ldg(gp + gi);
                 const float re = fmaf(e.sf, pv.z, pv.x);
                 const float im = fmaf(e.sf, pv.w, pv.y);
@@ -235,18 +283,23 @@ __global__ void __launch_bounds__(kThreads, 2) bp_grid_kernel(const BpGridArgs a
     }
 }
 
-template <bool PRECISE>
+template <bool PRECISE, bool NEAREST>
 static cudaError_t launch_bp_grid_t(const BpGridArgs& a, cudaStream_t st) {
     const size_t smem = bp_grid_smem_bytes(a.wwin, a.pb, 0);
     const unsigned blocks = (unsigned)(a.g.tiles_x * a.g.tiles_y * a.g.nz);
-    cudaError_t e = cudaFuncSetAttribute(bp_grid_kernel<PRECISE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = cudaFuncSetAttribute(bp_grid_kernel<PRECISE, NEAREST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
     if (e != cudaSuccess) return e;
-    bp_grid_kernel<PRECISE><<<blocks, kThreads, smem, st>>>(a);
+    bp_grid_kernel<PRECISE, NEAREST><<<blocks, kThreads, smem, st>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st) {
-    return a.g.precise_bins ? launch_bp_grid_t<true>(a, st) : launch_bp_grid_t<false>(a, st);
+    if (a.nearest) {
+        if (!a.g.precise_bins || !a.steps || !a.alpha2) return cudaErrorInvalidValue;
+        return launch_bp_grid_t<true, true>(a, st);
+    }
+    return a.g.precise_bins ? launch_bp_grid_t<true, false>(a, st) : launch_bp_grid_t<false, false>(a, st);
 }
 
 // ------------------------------------------- warp-specialised pipelines (K2 gather, K3 scatter)
@@ -407,7 +460,7 @@ __device__ __forceinline__ void producer_coeffs_pair(const GridConst& g, const P
 // terms in di).  A quarter-warp's eight 16-byte window loads are conflict-free when they fall
 // in distinct 16-byte bank groups or on the same bin; lanes along the axis where bins change
 // slowly (cross-range) make them land on one or two bins.
-template <bool LANES_Y, bool PRECISE>
+template <bool LANES_Y, bool PRECISE, bool NEAREST>
 __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const BpGridArgs a) {
     extern __shared__ __align__(16) float4 smem[];
     const int pb = a.pb, ww = a.wwin;
@@ -574,8 +627,23 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
                 float2 r1 = add2(v, SH);
                 const float2 s = fma2(add2(r1, NSH), M1, v);               // v - rint(v), exact
                 if (PRECISE) r1 = add2(r1, fma2(cid, d, ci));              // + the exact integer part
-                const unsigned ia = min((unsigned)(__float_as_int(r1.x) + idx_bias), idx_max);
-                const unsigned ib = min((unsigned)(__float_as_int(r1.y) + idx_bias), idx_max);
+                unsigned ia = min((unsigned)(__float_as_int(r1.x) + idx_bias), idx_max);
+                unsigned ib = min((unsigned)(__float_as_int(r1.y) + idx_bias), idx_max);
+                if (NEAREST && (fabsf(s.x) > kNearEdge || fabsf(s.y) > kNearEdge)) {
+                    // near a rounding boundary: the exact bin, as a window index of the pulse
+                    const int px = ti * kTile + (LANES_Y ? 4 * warp + r : lane);
+                    const int py = tj * kTile + (LANES_Y ? lane : 4 * warp + r);
+                    const int sp = st * pb + 2 * pp;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        if (fabsf(h ? s.y : s.x) <= kNearEdge || sp + h >= a.S) continue;
+                        const int g0 = min(max(base0[b * pb + 2 * pp + h] - ww / 2 - a.bg0, 0), a.Lg - ww);
+                        const int gi = exact_grid_bin(a.steps, a.pulses, a.alpha2, g.s_r.hi, g.s_r.lo, a.bg0,
+                                                      BIN_ADJ_NEAREST, px, py, k, sp + h);
+                        const unsigned w = min((unsigned)(gi - g0), idx_max);
+                        if (h) ib = w; else ia = w;
+                    }
+                }
                 const float4 pa = wa[ia], pq = wb[ib];
                 const float2 re = f2(fmaf(s.x, pa.z, pa.x), fmaf(s.y, pq.z, pq.x));
                 const float2 im = f2(fmaf(s.x, pa.w, pa.y), fmaf(s.y, pq.w, pq.y));
@@ -627,10 +695,15 @@ cudaError_t launch_bp_grid_ws(const BpGridArgs& a, cudaStream_t st) {
         kernel<<<blocks, kWsThreads, smem, st>>>(a);
         return cudaSuccess;
     };
-    if (a.g.precise_bins)
-        e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, true>) : go(bp_grid_ws_pair_kernel<false, true>);
-    else
-        e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, false>) : go(bp_grid_ws_pair_kernel<false, false>);
+    if (a.nearest) {
+        if (!a.g.precise_bins || !a.steps || !a.alpha2) return cudaErrorInvalidValue;
+        e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, true, true>) : go(bp_grid_ws_pair_kernel<false, true, true>);
+    } else if (a.g.precise_bins) {
+        e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, true, false>) : go(bp_grid_ws_pair_kernel<false, true, false>);
+    } else {
+        e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, false, false>)
+                      : go(bp_grid_ws_pair_kernel<false, false, false>);
+    }
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
@@ -712,13 +785,27 @@ __device__ __forceinline__ void rmw_add(float2* wp, int idx, float w, float cr, 
     *q = u;
 }
 
+// What the nearest-bin scatter needs to decide a bin again exactly (exact_grid_bin): the pixel of
+// row 0 / lane 0 of the half tile, the walk direction, both pulses and their window starts.
+struct NearCtx {
+    const double* steps;
+    const PulseGeom* pulses;
+    const float4* alpha2;
+    float sr_hi, sr_lo;
+    int bg0, i0, j0, k, transposed;
+    int sp, sq;     // pulse indices
+    int wsp, wsq;   // first bin (absolute) of each pulse's window
+};
+
 // 16 rows of one half tile for the pulse pair (p, q).  MODE 2: bins n, n+1 of different lanes
-// disjoint (one phase per row); MODE 1: bins n distinct (two phases); MODE 0: atomics.
+// disjoint (one phase per row); MODE 1: bins n distinct (two phases); MODE 0: atomics.  Nearest
+// bins within 5e-5 of a rounding boundary are decided again exactly; such a bin may equal a
+// neighbouring lane's, so those contributions go in with atomics in a phase of their own.
 template <bool LINEAR, bool PRECISE, int MODE, bool TWO>
 __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, float w9p, float ibp,
                                              const ColumnTerms& ctq, float c9q, float w9q, float ibq,
                                              const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
-                                             int ws, int lane) {
+                                             int ws, int lane, const NearCtx& nc) {
 #pragma unroll 2
     for (int rr = 0; rr < 16; ++rr) {
         const float dj = (float)(rr - 8);
@@ -762,15 +849,41 @@ __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, 
                 }
             }
         } else {
+            bool fp = false, fq = false;
+            int xp = ip, xq = iq;
+            if (PRECISE) {   // nearest bins are always split: re-decide those near a boundary
+                fp = fabsf(ep.bp.s) > kNearEdge;
+                fq = TWO && fabsf(eq.bp.s) > kNearEdge;
+                if (fp || fq) {
+                    const int pi = nc.i0 + (nc.transposed ? rr : lane), pj = nc.j0 + (nc.transposed ? lane : rr);
+                    if (fp)
+                        xp = min(max(exact_grid_bin(nc.steps, nc.pulses, nc.alpha2, nc.sr_hi, nc.sr_lo, nc.bg0,
+                                                    BIN_FWD_NEAREST, pi, pj, nc.k, nc.sp) + nc.bg0 - nc.wsp, 0), ws - 1);
+                    if (fq)
+                        xq = min(max(exact_grid_bin(nc.steps, nc.pulses, nc.alpha2, nc.sr_hi, nc.sr_lo, nc.bg0,
+                                                    BIN_FWD_NEAREST, pi, pj, nc.k, nc.sq) + nc.bg0 - nc.wsq, 0), ws - 1);
+                }
+            }
             if (MODE >= 1) {
-                rmw_add(wp, ip, 1.0f, ep.cr, ep.ci);
-                if (TWO) rmw_add(wq, iq, 1.0f, eq.cr, eq.ci);
+                if (!fp) rmw_add(wp, ip, 1.0f, ep.cr, ep.ci);
+                if (TWO && !fq) rmw_add(wq, iq, 1.0f, eq.cr, eq.ci);
                 __syncwarp();
+                if (PRECISE && __any_sync(0xffffffffu, fp || fq)) {
+                    if (fp) {
+                        float2* a0 = wp + wslot(xp);
+                        atomicAdd(&a0->x, ep.cr); atomicAdd(&a0->y, ep.ci);
+                    }
+                    if (fq) {
+                        float2* b0 = wq + wslot(xq);
+                        atomicAdd(&b0->x, eq.cr); atomicAdd(&b0->y, eq.ci);
+                    }
+                    __syncwarp();
+                }
             } else {
-                float2* a0 = wp + wslot(ip);
+                float2* a0 = wp + wslot(xp);
                 atomicAdd(&a0->x, ep.cr); atomicAdd(&a0->y, ep.ci);
                 if (TWO) {
-                    float2* b0 = wq + wslot(iq);
+                    float2* b0 = wq + wslot(xq);
                     atomicAdd(&b0->x, eq.cr); atomicAdd(&b0->y, eq.ci);
                 }
             }
@@ -860,7 +973,7 @@ template <bool LINEAR, bool PRECISE, bool TWO>
 __device__ __forceinline__ void scatter_half(int mode, const ColumnTerms& ctp, float c9p, float w9p, float ibp,
                                              const ColumnTerms& ctq, float c9q, float w9q, float ibq,
                                              const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
-                                             int ws, int lane) {
+                                             int ws, int lane, const NearCtx& nc) {
     if constexpr (LINEAR && !PRECISE) {
         if (mode == 5) {
             scatter_rows_runs<TWO, 16>(ctp, c9p, ctq, c9q, xrow, wp, wq, off_p, off_q, ws, lane);
@@ -876,11 +989,14 @@ __device__ __forceinline__ void scatter_half(int mode, const ColumnTerms& ctp, f
         }
     }
     if (mode >= 2)
-        scatter_rows<LINEAR, PRECISE, 2, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane);
+        scatter_rows<LINEAR, PRECISE, 2, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
+                                              nc);
     else if (mode == 1)
-        scatter_rows<LINEAR, PRECISE, 1, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane);
+        scatter_rows<LINEAR, PRECISE, 1, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
+                                              nc);
     else
-        scatter_rows<LINEAR, PRECISE, 0, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane);
+        scatter_rows<LINEAR, PRECISE, 0, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
+                                              nc);
 }
 
 template <bool LINEAR, bool PRECISE, bool TRANSPOSED>
@@ -1038,12 +1154,29 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                     const ColumnTerms ctq =
                         load_column<PRECISE, TRANSPOSED>(coef + (pq * 4 + qs) * kSetF4, tt, c9q, w9q, ibq);
                     const float2* xrow = xt + 16 * half * kXtStride;
+                    NearCtx nc;
+                    if (!LINEAR) {
+                        nc.steps = a.steps;
+                        nc.pulses = a.pulses;
+                        nc.alpha2 = a.alpha2;
+                        nc.sr_hi = g.s_r.hi;
+                        nc.sr_lo = g.s_r.lo;
+                        nc.bg0 = a.bg0;
+                        nc.transposed = TRANSPOSED;
+                        nc.i0 = ti * kTile + (TRANSPOSED ? 16 * half : 0);
+                        nc.j0 = (tj0 + t) * kTile + (TRANSPOSED ? 0 : 16 * half);
+                        nc.k = k;
+                        nc.sp = s0 + p;
+                        nc.sq = s0 + pq;
+                        nc.wsp = wst[p];
+                        nc.wsq = wst[pq];
+                    }
                     if (two)
                         scatter_half<LINEAR, PRECISE, true>(mode, ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq,
-                                                            off_p, off_q, ws, lane);
+                                                            off_p, off_q, ws, lane, nc);
                     else
                         scatter_half<LINEAR, PRECISE, false>(mode, ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp,
-                                                             wq, off_p, off_q, ws, lane);
+                                                             wq, off_p, off_q, ws, lane, nc);
                 }
             }
         }
@@ -1095,6 +1228,7 @@ static cudaError_t launch_fp_grid_ws_o(const FpGridArgs& a, cudaStream_t st) {
 
 cudaError_t launch_fp_grid_ws(const FpGridArgs& a, cudaStream_t st) {
     if (a.pbf < 8 || a.pbf > 32 || (a.pbf & 7) || a.ws < 32 || (a.ws & 31)) return cudaErrorInvalidValue;
+    if (!a.linear && a.g.precise_bins && (!a.steps || !a.alpha2)) return cudaErrorInvalidValue;
     return a.transposed ? launch_fp_grid_ws_o<true>(a, st) : launch_fp_grid_ws_o<false>(a, st);
 }
 

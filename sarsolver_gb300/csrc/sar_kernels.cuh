@@ -35,6 +35,10 @@ struct BpGridArgs {
     int accumulate;            // 1: x += result
     int lanes_y;               // 1: lanes of a warp run along y (chosen when bins change more slowly
                                //    along y than along x: fewer shared-memory bank conflicts)
+    int nearest;               // 1: nearest-bin pairs; bins near a rounding boundary are decided again
+                               //    with the per-pixel double-float range (needs steps, alpha2)
+    const double* steps;       // [9] grid steps ex, ey, ez (FP64), for those exact decisions
+    const float4* alpha2;      // [S] |tx-o|^2, |rx-o|^2 as (hi, lo) pairs, the same
 };
 size_t bp_grid_smem_bytes(int wwin, int pb, int staged);
 cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st);
@@ -58,6 +62,8 @@ struct FpGridArgs {
     int pbf;                   // pulses per CTA (multiple of 8, <= 32)
     int linear;                // 1: linear interpolation weights; 0: nearest bin
     int transposed;            // 1: lanes along y, rows walked along x (bins change slowly along x)
+    const double* steps;       // nearest bins: FP64 grid steps and antenna norms for the exact
+    const float4* alpha2;      //   decisions near rounding boundaries (as BpGridArgs)
 };
 // Warp-specialised variant: producer warps stage image tiles and coefficient sets; each
 // gathering warp owns whole pulses, so its windows need no atomics when bins along a row of

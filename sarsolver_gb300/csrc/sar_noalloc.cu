@@ -12,6 +12,8 @@
 //   [0, 256)            device check flags (cleared by every call)
 //   pulse table         S x 64 bytes (PulseGeom, double-float antenna positions)
 //   pulse factors       S x 8 bytes (slow-time weight, conjugated for linear interpolation)
+//   grid steps          9 doubles, and antenna norms S x 16 bytes (nearest-bin decisions near a
+//                       rounding boundary are taken again exactly from these)
 //   profile pairs       S x span x 16 bytes (value at mid-bin, difference), fully rewritten
 // Sizes beyond the array are rejected with SAR_ERR_INVALID_ARGUMENT and a message.
 //
@@ -96,7 +98,9 @@ extern "C" int sar_adjoint_from_profiles_noalloc(const sar_geometry* g, const vo
     // Scratch sizes: reject what does not fit the fixed array.
     const size_t off_table = 256;
     const size_t off_w = off_table + round256(S * sizeof(PulseGeom));
-    const size_t off_pairs = off_w + round256(S * sizeof(float2));
+    const size_t off_steps = off_w + round256(S * sizeof(float2));
+    const size_t off_a2 = off_steps + 256;
+    const size_t off_pairs = off_a2 + round256(S * sizeof(float4));
     const size_t need = off_pairs + S * span * sizeof(float4);
     if (need > kScratchBytes) {
         char m[200];
@@ -126,6 +130,13 @@ extern "C" int sar_adjoint_from_profiles_noalloc(const sar_geometry* g, const vo
 
     std::vector<PulseGeom> table(S);
     std::vector<float2> wfac(S);
+    std::vector<float4> a2(S);
+    double steps[9];
+    for (int c = 0; c < 3; ++c) {
+        steps[c] = g->grid_step_x[c];
+        steps[3 + c] = g->grid_step_y[c];
+        steps[6 + c] = g->grid_step_z[c];
+    }
     double vmin = INFINITY, vmax = -INFINITY;
     const int tx_tiles = gc.tiles_x, ty_tiles = gc.tiles_y;
     for (size_t s = 0; s < S; ++s) {
@@ -134,6 +145,16 @@ extern "C" int sar_adjoint_from_profiles_noalloc(const sar_geometry* g, const vo
             if (!std::isfinite(tx[c]) || !std::isfinite(rx[c]) || !std::isfinite(srp[c]))
                 return noalloc_fail(SAR_ERR_INVALID_ARGUMENT, "non-finite antenna or SRP position");
         table[s] = make_pulse_geom(tx, rx, srp, g->grid_origin);
+        {
+            double at[3], ar[3];
+            for (int c = 0; c < 3; ++c) {
+                at[c] = tx[c] - g->grid_origin[c];
+                ar[c] = rx[c] - g->grid_origin[c];
+            }
+            const df n1 = to_df(at[0] * at[0] + at[1] * at[1] + at[2] * at[2]);
+            const df n2 = to_df(ar[0] * ar[0] + ar[1] * ar[1] + ar[2] * ar[2]);
+            a2[s] = make_float4(n1.hi, n1.lo, n2.hi, n2.lo);
+        }
         double a0, a1, b0, b1;
         box_distance_bounds(tx, g->grid_origin, g->grid_step_x, g->grid_step_y, g->grid_step_z, tx_tiles * 32 - 1.0,
                             ty_tiles * 32 - 1.0, nz - 1.0, &a0, &a1);
@@ -162,10 +183,14 @@ extern "C" int sar_adjoint_from_profiles_noalloc(const sar_geometry* g, const vo
     PulseGeom* d_table = reinterpret_cast<PulseGeom*>(scratch + off_table);
     float2* d_w = reinterpret_cast<float2*>(scratch + off_w);
     float4* d_pairs = reinterpret_cast<float4*>(scratch + off_pairs);
+    double* d_steps = reinterpret_cast<double*>(scratch + off_steps);
+    float4* d_a2 = reinterpret_cast<float4*>(scratch + off_a2);
 
     cudaError_t e = cudaMemsetAsync(flags, 0, sizeof(unsigned), st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_table, table.data(), S * sizeof(PulseGeom), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_w, wfac.data(), S * sizeof(float2), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_steps, steps, sizeof steps, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_a2, a2.data(), S * sizeof(float4), cudaMemcpyHostToDevice, st);
     // Pairs over the caller's span: with M = span and first bin 0 the unpack kernel reads column
     // w and w + 1 of each row (the last column's difference wraps; it lies in the margin).
     if (e == cudaSuccess)
@@ -182,6 +207,9 @@ extern "C" int sar_adjoint_from_profiles_noalloc(const sar_geometry* g, const vo
         a.bg0 = (int)first_bin;
         a.wwin = wwin;
         a.accumulate = 0;
+        a.nearest = linear ? 0 : 1;
+        a.steps = d_steps;
+        a.alpha2 = d_a2;
         a.lanes_y = choose_lanes_y(g->transmit_posns, g->receive_posns, S, g->grid_origin, g->grid_step_x,
                                    g->grid_step_y, g->grid_step_z, nx, ny, nz);
         a.pb = 32;

@@ -5,6 +5,9 @@
     python -m sarsolver_gb300.workloads resample   # 8192 x 8192 phase history, factors 2 x 2
     python -m sarsolver_gb300.workloads cphd       # 8192 x 8192 CI4 CPHD file -> device
     python -m sarsolver_gb300.workloads pdhg       # 100 PDHG iterations, 512^2 x 1024 x 1024
+    python -m sarsolver_gb300.workloads settings   # one backprojection + one forward projection at
+                                                   # 2048^2 x 4096 x 4096 per interpolation mode,
+                                                   # upsample factor and collection direction
 
 Each prints one JSON line with CUDA-event times of the timed call (after one warm-up call).
 """
@@ -170,13 +173,48 @@ def cphd_workload() -> dict:
     return out
 
 
+def settings_workload() -> list:
+    """The benchmark scene under other operator settings: linear / nearest_ref interpolation, upsample
+    8 / 128 (the reference's default), and the collection turned by 90 degrees (range along y).
+    Mean of 3 calls after one warm-up, CUDA events around each operator call."""
+    from .plan import SarPlan
+    from .scenes import config_workload
+    out = []
+    for case, interp, U in (("config2", "linear", 8.0), ("config2_turned", "linear", 8.0),
+                            ("config2", "nearest_ref", 8.0), ("config2", "linear", 128.0),
+                            ("config2", "nearest_ref", 128.0)):
+        aperture, scene, _, _ = config_workload(case)
+        plan = SarPlan(scene, aperture, upsample_ratio=U, interp=interp)
+        g = torch.Generator(device="cuda")
+        g.manual_seed(1)
+        y = torch.complex(torch.randn(plan.num_slow_times, plan.num_freqs, device="cuda", generator=g),
+                          torch.randn(plan.num_slow_times, plan.num_freqs, device="cuda", generator=g))
+        x = torch.complex(torch.randn(plan.num_scatterers, device="cuda", generator=g),
+                          torch.randn(plan.num_scatterers, device="cuda", generator=g))
+        row = {"workload": "settings", "case": case, "interp": interp, "upsample": U, "grid_path": plan.is_grid,
+               "tile_window": plan.tile_window, "strip_window": plan.strip_window,
+               "gather_lanes_y": plan.gather_lanes_y, "scatter_lanes_y": plan.scatter_lanes_y}
+        for name, fn in (("adjoint_ms", lambda: plan.adjoint(y)), ("forward_ms", lambda: plan.forward(x))):
+            times = [_time(fn, warmup=1 if i == 0 else 0)[1] for i in range(3)]
+            row[name] = sum(times) / len(times)
+        assert plan.device_flags() == 0
+        plan.close()
+        del y, x
+        torch.cuda.empty_cache()
+        print(json.dumps(row), flush=True)
+        out.append(row)
+    return out
+
+
 def main(argv=None) -> None:
     argv = sys.argv[1:] if argv is None else argv
     name = argv[0] if argv else "cgls"
     torch.cuda.set_device(0)
     fn = {"cgls": cgls_workload, "autofocus": autofocus_workload, "resample": resample_workload,
-          "cphd": cphd_workload, "pdhg": pdhg_workload}[name]
-    print(json.dumps(fn()))
+          "cphd": cphd_workload, "pdhg": pdhg_workload, "settings": settings_workload}[name]
+    res = fn()
+    if not isinstance(res, list):   # the settings workload prints one line per setting itself
+        print(json.dumps(res))
 
 
 if __name__ == "__main__":
