@@ -370,9 +370,8 @@ int validate_geometry(const sar_geometry* g) {
     return SAR_OK;
 }
 
-// Tile window (bins) of the grid gather and whether it stages in shared memory: the grid paths
-// take nearest_ref by default only then (the wide-window fallback reads global memory and is
-// slower than the per-pixel kernel at the reference's default upsampling).
+// Tile window (bins) of the grid gather, or -1 where the grid spacing is too coarse for the
+// range sampling (the grid kernels then do not apply).
 static int grid_tile_window(const sar_geometry* g, double s_r) {
     const double* ex = g->grid_step_x;
     const double* ey = g->grid_step_y;
@@ -391,14 +390,12 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
     // A grid routed to the per-pixel path is expanded into explicit positions.
     sar_geometry expanded;
     std::vector<double> grid_positions;
-    bool nearest_staged = false;
-    if (grid && g->path == SAR_PATH_AUTO && g->interp == SAR_INTERP_NEAREST_REF && g->c_eff > 0.0 && N > 0) {
-        const int ww = grid_tile_window(g, g->sample_frequency * (double)M / ((double)N * g->c_eff));
-        nearest_staged = ww > 0 && bp_grid_ws_smem_bytes(ww, 8) <= kBpSmemBudget;
-    }
-    const bool to_points =
-        grid && (g->path == SAR_PATH_POINTS ||
-                 (g->path == SAR_PATH_AUTO && g->interp == SAR_INTERP_NEAREST_REF && !nearest_staged));
+    // nearest_ref takes the grid kernels by default too (their nearest bins are decided exactly near
+    // rounding boundaries); only grids too coarse for them go to the per-pixel kernels
+    bool grid_ok = true;
+    if (grid && g->path == SAR_PATH_AUTO && g->interp == SAR_INTERP_NEAREST_REF && g->c_eff > 0.0 && N > 0)
+        grid_ok = grid_tile_window(g, g->sample_frequency * (double)M / ((double)N * g->c_eff)) > 0;
+    const bool to_points = grid && (g->path == SAR_PATH_POINTS || !grid_ok);
     if (to_points) {
         const size_t nz = g->grid_shape[0], ny = g->grid_shape[1], nx = g->grid_shape[2];
         grid_positions.resize(3 * P);

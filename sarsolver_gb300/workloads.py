@@ -180,18 +180,19 @@ def settings_workload() -> list:
     from .plan import SarPlan
     from .scenes import config_workload
     out = []
-    for case, interp, U in (("config2", "linear", 8.0), ("config2_turned", "linear", 8.0),
-                            ("config2", "nearest_ref", 8.0), ("config2", "linear", 128.0),
-                            ("config2", "nearest_ref", 128.0)):
+    for case, interp, U, path in (("config2", "linear", 8.0, "auto"), ("config2_turned", "linear", 8.0, "auto"),
+                                  ("config2", "nearest_ref", 8.0, "auto"), ("config2", "linear", 128.0, "auto"),
+                                  ("config2", "nearest_ref", 128.0, "auto"), ("config2", "nearest_ref", 128.0, "grid")):
         aperture, scene, _, _ = config_workload(case)
-        plan = SarPlan(scene, aperture, upsample_ratio=U, interp=interp)
+        plan = SarPlan(scene, aperture, upsample_ratio=U, interp=interp, path=path)
         g = torch.Generator(device="cuda")
         g.manual_seed(1)
         y = torch.complex(torch.randn(plan.num_slow_times, plan.num_freqs, device="cuda", generator=g),
                           torch.randn(plan.num_slow_times, plan.num_freqs, device="cuda", generator=g))
         x = torch.complex(torch.randn(plan.num_scatterers, device="cuda", generator=g),
                           torch.randn(plan.num_scatterers, device="cuda", generator=g))
-        row = {"workload": "settings", "case": case, "interp": interp, "upsample": U, "grid_path": plan.is_grid,
+        row = {"workload": "settings", "case": case, "interp": interp, "upsample": U, "path": path,
+               "grid_path": plan.is_grid,
                "tile_window": plan.tile_window, "strip_window": plan.strip_window,
                "gather_lanes_y": plan.gather_lanes_y, "scatter_lanes_y": plan.scatter_lanes_y}
         for name, fn in (("adjoint_ms", lambda: plan.adjoint(y)), ("forward_ms", lambda: plan.forward(x))):

@@ -1,7 +1,7 @@
 """Range-profile FFTs with cuFFT load/store callbacks (sar_fft_callbacks.cu, opt-in with
 SAR_FFT_CALLBACKS=1) against the packing kernels and the FP64 oracle: even N with a power-of-two
-working length, odd N with a non-power-of-two length, nearest_ref on the per-pixel path, pulse
-blocks (other batch sizes).  Where cuFFT cannot build plans with JIT callbacks (GB300 with the
+working length, odd N with a non-power-of-two length, nearest_ref, pulse blocks (other batch
+sizes).  Where cuFFT cannot build plans with JIT callbacks (GB300 with the
 cuFFT of CUDA 13.0 returns CUFFT_INTERNAL_ERROR), plan creation reports that and the tests skip;
 the default plans never use callbacks."""
 import os
