@@ -479,27 +479,33 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
                 p->staged = true;
                 break;
             }
-        // Forward strips: tile columns split into segments whose window fits shared memory.
+        // Forward strips: lines of tiles along the axis the scatter walks (columns along y; rows
+        // along x for the transposed scatter, the gather's lanes along x), split into segments
+        // whose window fits shared memory.
+        const bool strips_x = !p->lanes_y;
+        const int lines = strips_x ? ty_tiles : tx_tiles, along = strips_x ? tx_tiles : ty_tiles;
         p->forward_points = true;
         for (int pbf : {16, 8}) {
-            int seg = ty_tiles;
+            int seg = along;
             while (true) {
-                const int segs = (ty_tiles + seg - 1) / seg;
-                const size_t n_strips = (size_t)nz * tx_tiles * segs;
+                const int segs = (along + seg - 1) / seg;
+                const size_t n_strips = (size_t)nz * lines * segs;
                 std::vector<int> starts(n_strips * S);
                 int need = 0;
                 for (int k = 0; k < nz; ++k)
-                    for (int ti = 0; ti < tx_tiles; ++ti)
+                    for (int ln = 0; ln < lines; ++ln)
                         for (int sg = 0; sg < segs; ++sg) {
-                            const int tj0 = sg * seg, tj1 = std::min(tj0 + seg, ty_tiles);
+                            const int t0 = sg * seg, t1 = std::min(t0 + seg, along);
+                            const int ti0 = strips_x ? t0 : ln, tj0 = strips_x ? ln : t0;
+                            const double nu = strips_x ? (t1 - t0) * kTile - 1.0 : kTile - 1.0;
+                            const double nv = strips_x ? kTile - 1.0 : (t1 - t0) * kTile - 1.0;
                             double o[3];
                             for (int c = 0; c < 3; ++c)
-                                o[c] = origin[c] + ti * kTile * ex[c] + tj0 * kTile * ey[c] + k * ez[c];
-                            const size_t strip = ((size_t)k * tx_tiles + ti) * segs + sg;
+                                o[c] = origin[c] + ti0 * kTile * ex[c] + tj0 * kTile * ey[c] + k * ez[c];
+                            const size_t strip = ((size_t)k * lines + ln) * segs + sg;
                             for (size_t s = 0; s < S; ++s) {
                                 double lo, hi;
-                                region_range(tx + 3 * s, rx + 3 * s, srp + 3 * s, o, ex, ey, ez, kTile - 1.0,
-                                             (tj1 - tj0) * kTile - 1.0, 0.0, &lo, &hi);
+                                region_range(tx + 3 * s, rx + 3 * s, srp + 3 * s, o, ex, ey, ez, nu, nv, 0.0, &lo, &hi);
                                 const long b0 = (long)std::floor(lo * s_r) - 3;
                                 const long b1 = (long)std::ceil(hi * s_r) + 4;
                                 starts[strip * S + s] = (int)b0;

@@ -1014,16 +1014,19 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
     df3* anchors_all = reinterpret_cast<df3*>(fsm + L.anchors);
 
     const GridConst& g = a.g;
+    // Strips are lines of tiles along the walked axis: columns along y, or rows along x when
+    // TRANSPOSED (range bins change slowly along them, so their windows stay short).
+    const int lines = TRANSPOSED ? g.tiles_y : g.tiles_x, along = TRANSPOSED ? g.tiles_x : g.tiles_y;
     int bidx = blockIdx.x;
     const int seg = bidx % a.segs_per_column;
     bidx /= a.segs_per_column;
-    const int ti = bidx % g.tiles_x;
-    const int k = bidx / g.tiles_x;
-    const int strip = (k * g.tiles_x + ti) * a.segs_per_column + seg;
+    const int line = bidx % lines;
+    const int k = bidx / lines;
+    const int strip = (k * lines + line) * a.segs_per_column + seg;
     const int s0 = blockIdx.y * pbf;
     const int npb = min(pbf, a.S - s0);
-    const int tj0 = seg * a.seg_tiles;
-    const int ntile = min(a.seg_tiles, g.tiles_y - tj0);
+    const int t0 = seg * a.seg_tiles;
+    const int ntile = min(a.seg_tiles, along - t0);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     for (int e = threadIdx.x; e < pbf * wslots; e += blockDim.x) win[e] = make_float2(0.f, 0.f);
@@ -1047,7 +1050,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                 if (lane == 0) raise_flag(a.flags, FLAG_WAIT_TIMEOUT);
                 return;   // the gathering warps time out on "full" and leave as well
             }
-            const int tj = tj0 + t;
+            const int ti = TRANSPOSED ? t0 + t : line, tj = TRANSPOSED ? line : t0 + t;
             if (lane < 4) anchors[lane] = subtile_anchor(ti, tj, k, lane, g);
             // this warp's half of the tile's image values (rows 16 pw .. 16 pw + 15)
             float2* xt = xt0 + b * kTile * kXtStride;
@@ -1163,8 +1166,8 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                         nc.sr_lo = g.s_r.lo;
                         nc.bg0 = a.bg0;
                         nc.transposed = TRANSPOSED;
-                        nc.i0 = ti * kTile + (TRANSPOSED ? 16 * half : 0);
-                        nc.j0 = (tj0 + t) * kTile + (TRANSPOSED ? 0 : 16 * half);
+                        nc.i0 = (TRANSPOSED ? t0 + t : line) * kTile + (TRANSPOSED ? 16 * half : 0);
+                        nc.j0 = (TRANSPOSED ? line : t0 + t) * kTile + (TRANSPOSED ? 0 : 16 * half);
                         nc.k = k;
                         nc.sp = s0 + p;
                         nc.sq = s0 + pq;
@@ -1209,7 +1212,8 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
 template <bool LINEAR, bool PRECISE, bool TRANSPOSED>
 static cudaError_t launch_fp_grid_ws_t(const FpGridArgs& a, cudaStream_t st) {
     const size_t smem = fp_grid_ws_smem_bytes(a.ws, a.pbf);
-    const dim3 grid((unsigned)(a.segs_per_column * a.g.tiles_x * a.g.nz), (unsigned)((a.S + a.pbf - 1) / a.pbf));
+    const int lines = TRANSPOSED ? a.g.tiles_y : a.g.tiles_x;
+    const dim3 grid((unsigned)(a.segs_per_column * lines * a.g.nz), (unsigned)((a.S + a.pbf - 1) / a.pbf));
     cudaError_t e = cudaFuncSetAttribute(fp_grid_ws_kernel<LINEAR, PRECISE, TRANSPOSED>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

@@ -56,8 +56,8 @@ struct FpGridArgs {
     const int* strip_start;    // [n_strips][S] first bin of each strip window
     unsigned* flags;
     int S, Lg, bg0;
-    int seg_tiles;             // tiles per strip segment (along y)
-    int segs_per_column;       // ceil(tiles_y / seg_tiles)
+    int seg_tiles;             // tiles per strip segment (along y; along x when transposed)
+    int segs_per_column;       // segments per strip line: ceil(tiles along it / seg_tiles)
     int ws;                    // strip window length (bins), multiple of 32
     int pbf;                   // pulses per CTA (multiple of 8, <= 32)
     int linear;                // 1: linear interpolation weights; 0: nearest bin

@@ -182,7 +182,7 @@ def settings_workload() -> list:
     out = []
     for case, interp, U, path in (("config2", "linear", 8.0, "auto"), ("config2_turned", "linear", 8.0, "auto"),
                                   ("config2", "nearest_ref", 8.0, "auto"), ("config2", "linear", 128.0, "auto"),
-                                  ("config2", "nearest_ref", 128.0, "auto"), ("config2", "nearest_ref", 128.0, "grid")):
+                                  ("config2", "nearest_ref", 128.0, "auto"), ("config2", "nearest_ref", 128.0, "points")):
         aperture, scene, _, _ = config_workload(case)
         plan = SarPlan(scene, aperture, upsample_ratio=U, interp=interp, path=path)
         g = torch.Generator(device="cuda")
