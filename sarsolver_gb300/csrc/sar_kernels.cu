@@ -1,11 +1,16 @@
 // sar_kernels.cu -- sm_103a kernels of the SAR operator pair.
 //
-//   K1  upsample_pairs (fused, N = 4096) or pack_adjoint / cuFFT / unpack_pairs
+//   K1  upsample_pairs (fused, N = 1024, 2048, 4096) or pack_adjoint / cuFFT / unpack_pairs
 //                                      range-profile upsampling (replaces sarsolver_cxx.cpp:331-344)
 //   K2  bp_grid_ws_pair / bp_grid / bp_points
 //                                      backprojection gather (replaces :345-350)
 //   K3  fp_grid_ws / fp_points         forward scatter, the exact transpose of K2 (:284-291)
-//   K4  pack_forward / extract_forward range-profile downsampling around the FFT (:292-307)
+//   K4  downsample_forward (fused) or pack_forward / cuFFT / extract_forward
+//                                      range-profile downsampling around the FFT (:292-307)
+//
+// Nearest-bin sampling (the reference's rule) on the grid kernels uses split bins and decides
+// every bin within 5e-5 of a rounding boundary again in double-float (exact_grid_bin), so the
+// bins equal those of FP64 rounding; the per-pixel kernels compute every bin that way.
 //
 // Layout in HBM: images are complex64 [nz][ny][nx]; phase histories complex64 [S][N] with
 // fast time fftshifted (the Python API's convention, forward.py:44); range profiles are kept
