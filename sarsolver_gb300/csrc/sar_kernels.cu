@@ -246,15 +246,28 @@ __global__ void __launch_bounds__(kThreads, 2) bp_grid_kernel(const BpGridArgs a
             const ColumnTerms ct = load_column<PRECISE>(coef + (pi * 4 + tt.q) * kSetF4, tt, c9, w9, ib);
             const float4* gp = a.pairs + (size_t)(s0 + pi) * a.Lg;
             const int bb = base[pi] - a.bg0;
+            // bins of the thread's four pixels first, the rare exact re-decisions next, then the four
+            // loads: the loads are not held behind the (non-inlined) re-decision call
+            PixelEval e4[4];
+            int gi4[4];
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
-                const PixelEval e = eval_pixel<PRECISE>(ct, c9, w9, ib, tt, r);
-                int gi = min(max(bb + e.n, 0), a.Lg - 1);
-                if (NEAREST && fabsf(e.sf) > kNearEdge)
-                    gi = min(max(exact_grid_bin(a.steps, a.pulses, a.alpha2, g.s_r.hi, g.s_r.lo, a.bg0,
-                                                BIN_ADJ_NEAREST, ti * kTile + (threadIdx.x & 31),
-                                                tj * kTile + 4 * (threadIdx.x >> 5) + r, k, s0 + pi),
-                                 0), a.Lg - 1);
+                e4[r] = eval_pixel<PRECISE>(ct, c9, w9, ib, tt, r);
+                gi4[r] = min(max(bb + e4[r].n, 0), a.Lg - 1);
+            }
+            if (NEAREST) {
+#pragma unroll
+                for (int r = 0; r < 4; ++r)
+                    if (fabsf(e4[r].sf) > kNearEdge)
+                        gi4[r] = min(max(exact_grid_bin(a.steps, a.pulses, a.alpha2, g.s_r.hi, g.s_r.lo, a.bg0,
+                                                        BIN_ADJ_NEAREST, ti * kTile + (threadIdx.x & 31),
+                                                        tj * kTile + 4 * (threadIdx.x >> 5) + r, k, s0 + pi),
+                                         0), a.Lg - 1);
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const PixelEval e = e4[r];
+                const int gi = gi4[r];
                 const float4 pv = __ldg(gp + gi);
                 const float re = fmaf(e.sf, pv.z, pv.x);
                 const float im = fmaf(e.sf, pv.w, pv.y);

@@ -181,6 +181,7 @@ def settings_workload() -> list:
     from .scenes import config_workload
     out = []
     for case, interp, U, path in (("config2", "linear", 8.0, "auto"), ("config2_turned", "linear", 8.0, "auto"),
+                                  ("config2_diagonal", "linear", 8.0, "auto"),
                                   ("config2", "nearest_ref", 8.0, "auto"), ("config2", "linear", 128.0, "auto"),
                                   ("config2", "nearest_ref", 128.0, "auto"), ("config2", "nearest_ref", 128.0, "points")):
         aperture, scene, _, _ = config_workload(case)
@@ -196,8 +197,14 @@ def settings_workload() -> list:
                "tile_window": plan.tile_window, "strip_window": plan.strip_window,
                "gather_lanes_y": plan.gather_lanes_y, "scatter_lanes_y": plan.scatter_lanes_y}
         for name, fn in (("adjoint_ms", lambda: plan.adjoint(y)), ("forward_ms", lambda: plan.forward(x))):
-            times = [_time(fn, warmup=1 if i == 0 else 0)[1] for i in range(3)]
+            fn()
+            plan.enable_stage_timing(True)
+            times = [_time(fn, warmup=0)[1] for _ in range(3)]
+            stages, calls = plan.stage_times()
+            plan.enable_stage_timing(False)
             row[name] = sum(times) / len(times)
+            # [FFT side before, main kernel, FFT side after] per call
+            row[name.replace("_ms", "_stages_ms")] = [round(v / max(calls, 1), 3) for v in stages]
         assert plan.device_flags() == 0
         plan.close()
         del y, x
