@@ -161,7 +161,7 @@ def test_linear_matches_fp64_oracle(kind):
 
 
 @pytest.mark.parametrize("mode", ["linear", "nearest_ref"])
-@pytest.mark.parametrize("turn", [0, 1])
+@pytest.mark.parametrize("turn", [0, 1, 0.5])
 def test_gather_lane_layouts_match_oracle(turn, mode):
     """The grid backprojection runs its lanes along the axis where range bins change slowly:
     along y for a collection looking along x, along x once the collection is turned by 90
@@ -170,17 +170,20 @@ def test_gather_lane_layouts_match_oracle(turn, mode):
     the grid path.  The forward projection of the same plans runs its lanes the other way (along
     the axis where bins change fast, walking the slow one): lanes along x, then lanes along y on
     a transposed tile once turned, with register run windows (linear) and single-bin
-    read-modify-writes (nearest) in both layouts."""
-    rng = np.random.default_rng(21 + turn)
+    read-modify-writes (nearest) in both layouts.  turn = 0.5: looking along the grid diagonal,
+    where bins change alike along both axes (no run windows; two-phase read-modify-writes)."""
+    rng = np.random.default_rng(21 + int(2 * turn))
     case = spotlight_case(37, 96, 70, 0.3, 4.0, weights=np.exp(1j * rng.uniform(-3, 3, 37)))
     if turn:
-        rot = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+        c, s_ = np.cos(turn * np.pi / 2), np.sin(turn * np.pi / 2)
+        rot = np.array([[c, -s_, 0.0], [s_, c, 0.0], [0.0, 0.0, 1.0]])
         ap = case.aperture
         case.aperture = NumpySimpleSarAperture(ap.transmitter_positions @ rot.T, ap.receiver_positions @ rot.T,
                                                ap.stab_ref_posns, ap.centre_frequency, ap.sample_bandwidth,
                                                num_freqs=ap.num_freqs, slow_time_weighting=ap.slow_time_weighting)
     plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp=mode, path="grid")
-    assert plan.gather_lanes_y == (turn == 0) and plan.scatter_lanes_y == (turn == 1)
+    if turn != 0.5:
+        assert plan.gather_lanes_y == (turn == 0) and plan.scatter_lanes_y == (turn == 1)
     y = crandn(rng, 37, 96)
     tol = LINEAR_TOL   # nearest bins too: those near a rounding boundary are decided exactly
     e_a = rel_l2(gpu_adjoint(plan, y), oracle.adjoint(case.problem(), y, mode, threads=8))
@@ -247,7 +250,7 @@ def test_backproject_reads_pinned_host_input_in_place():
     assert op.plan.device_flags() == 0
 
 
-@pytest.mark.parametrize("kind", ["grid", "points", "bistatic", "turned"])
+@pytest.mark.parametrize("kind", ["grid", "points", "bistatic", "turned", "diagonal"])
 def test_dot_product_adjoint(kind):
     rng = np.random.default_rng(2)
     if kind == "points":
@@ -255,9 +258,10 @@ def test_dot_product_adjoint(kind):
     else:
         case = spotlight_case(96, 256, 100, 0.5, 5.0, bistatic=(kind == "bistatic"),
                               weights=np.exp(1j * rng.uniform(-2, 2, 96)))
-    if kind == "turned":   # looking along y: the scatter walks x on a transposed tile
+    if kind in ("turned", "diagonal"):   # looking along y (the scatter walks x), or the diagonal
         ap = case.aperture
-        rot = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+        c, s_ = (0.0, 1.0) if kind == "turned" else (np.sqrt(0.5), np.sqrt(0.5))
+        rot = np.array([[c, -s_, 0.0], [s_, c, 0.0], [0.0, 0.0, 1.0]])
         case.aperture = NumpySimpleSarAperture(ap.transmitter_positions @ rot.T, ap.receiver_positions @ rot.T,
                                                ap.stab_ref_posns, ap.centre_frequency, ap.sample_bandwidth,
                                                num_freqs=ap.num_freqs, slow_time_weighting=ap.slow_time_weighting)
