@@ -223,6 +223,8 @@ def load_host() -> ctypes.CDLL:
         lib.sar_geom_host_eval.argtypes = [P, P, P, P, c_int, c_int, c_int, c_size_t, P, P, P, c_double, c_double,
                                            ctypes.c_float, c_int, P, P]
         lib.sar_geom_host_eval_transposed.argtypes = lib.sar_geom_host_eval.argtypes
+        lib.sar_tile_halfspan_host.argtypes = [P, P, c_size_t, P, P, P, P, c_int, c_int, c_int, c_double]
+        lib.sar_tile_halfspan_host.restype = c_double
         lib.sar_geom_host_eval_points.argtypes = [P, c_size_t, P, c_size_t, P, P, P, c_double, c_double,
                                                   ctypes.c_float, P, P]
         _HOST = lib

@@ -138,3 +138,11 @@ extern "C" int sar_geom_host_eval_points(const double* origin, size_t num_points
     }
     return 0;
 }
+
+// Half-span (bins) of the gather's tile window from the look directions, as the plan computes it
+// (tile_halfspan_directional); -1 where an antenna is not clear of the scene.
+extern "C" double sar_tile_halfspan_host(const double* tx, const double* rx, size_t num_pulses, const double* origin,
+                                         const double* ex, const double* ey, const double* ez, int tiles_x,
+                                         int tiles_y, int nz, double s_r) {
+    return tile_halfspan_directional(tx, rx, num_pulses, origin, ex, ey, ez, 32, tiles_x, tiles_y, nz, s_r);
+}

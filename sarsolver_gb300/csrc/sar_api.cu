@@ -382,51 +382,6 @@ static int grid_tile_window(const sar_geometry* g, double s_r) {
     return (2 * ((int)std::ceil(h) + 3) + 3) & ~3;
 }
 
-// Half-span (bins) of a tile's window from the look directions: for a pixel at d = di ex + dj ey
-// from its tile's centre c (|di|, |dj| <= 16) and an antenna a, | |a - p| - |a - c| | <=
-// |u.d| + |d|^2 / (2 R) with u the unit vector from c to a and R the antenna's distance from the
-// scene; u at a tile centre differs from u0 at the scene centre by at most D / R (D: the
-// scene's half-extent; c is the mean of the tile's sub-tile anchors, the point the window is
-// centred on), so per antenna the change is at most 16 (|u0.ex| + |u0.ey|) +
-// 16 (|ex| + |ey|) D / R + (16 (|ex| + |ey|))^2 / (2 R).  Returns -1 when an antenna is not
-// clear of the scene (the isotropic bound 16 (|ex| + |ey|) per antenna then applies).
-static double tile_halfspan_directional(const double* tx, const double* rx, size_t S, const double* origin,
-                                        const double* ex, const double* ey, const double* ez, int tiles_x,
-                                        int tiles_y, int nz, double s_r) {
-    const double nex = std::sqrt(ex[0] * ex[0] + ex[1] * ex[1] + ex[2] * ex[2]);
-    const double ney = std::sqrt(ey[0] * ey[0] + ey[1] * ey[1] + ey[2] * ey[2]);
-    const double nez = std::sqrt(ez[0] * ez[0] + ez[1] * ez[1] + ez[2] * ez[2]);
-    double c0[3];
-    for (int c = 0; c < 3; ++c)
-        c0[c] = origin[c] + 0.5 * (tiles_x * kTile - 1) * ex[c] + 0.5 * (tiles_y * kTile - 1) * ey[c] +
-                0.5 * (nz - 1) * ez[c];
-    const double D = 0.5 * (tiles_x * kTile * nex + tiles_y * kTile * ney + nz * nez);
-    const double reach = 16.0 * (nex + ney);
-    double worst = 0.0;
-    for (size_t s = 0; s < S; ++s) {
-        double h = 0.0;
-        for (int ant = 0; ant < 2; ++ant) {
-            const double* a = (ant ? rx : tx) + 3 * s;
-            double u[3], r = 0.0;
-            for (int c = 0; c < 3; ++c) {
-                u[c] = a[c] - c0[c];
-                r += u[c] * u[c];
-            }
-            r = std::sqrt(r);
-            const double R = r - D - reach;
-            if (!(R > 0.0)) return -1.0;
-            double ux = 0.0, uy = 0.0;
-            for (int c = 0; c < 3; ++c) {
-                ux += u[c] * ex[c] / r;
-                uy += u[c] * ey[c] / r;
-            }
-            h += 16.0 * (std::fabs(ux) + std::fabs(uy)) + reach * D / R + reach * reach / (2.0 * R);
-        }
-        worst = std::max(worst, h);
-    }
-    return worst * s_r;
-}
-
 int build_plan(const sar_geometry* g_in, sar_plan* p) {
     const sar_geometry* g = g_in;
     const size_t N = g->num_fast_times, S = g->num_slow_times, P = g->num_scatterers;
@@ -507,7 +462,7 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
         p->wwin = grid_tile_window(g, s_r);
         if (p->wwin < 0) return fail(SAR_ERR_NOT_SUPPORTED, "grid spacing too coarse for the range sampling");
         {
-            const double hd = tile_halfspan_directional(tx, rx, S, origin, ex, ey, ez, p->gc_adj.tiles_x,
+            const double hd = tile_halfspan_directional(tx, rx, S, origin, ex, ey, ez, kTile, p->gc_adj.tiles_x,
                                                         p->gc_adj.tiles_y, nz, s_r);
             if (hd >= 0.0) p->wwin = std::min(p->wwin, (2 * ((int)std::ceil(hd) + 3) + 3) & ~3);
         }

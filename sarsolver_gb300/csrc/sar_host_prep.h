@@ -134,4 +134,49 @@ static inline int choose_lanes_y(const double* tx, const double* rx, size_t S, c
     return rate_y < rate_x ? 1 : 0;
 }
 
+// Half-span (bins) of a tile's window from the look directions: for a pixel at d = di ex + dj ey
+// from its tile's centre c (|di|, |dj| <= tile / 2 = 16) and an antenna a, | |a - p| - |a - c| | <=
+// |u.d| + |d|^2 / (2 R) with u the unit vector from c to a and R the antenna's distance from the
+// scene; u at a tile centre differs from u0 at the scene centre by at most D / R (D: the
+// scene's half-extent; c is the mean of the tile's sub-tile anchors, the point the window is
+// centred on), so per antenna the change is at most 16 (|u0.ex| + |u0.ey|) +
+// 16 (|ex| + |ey|) D / R + (16 (|ex| + |ey|))^2 / (2 R).  Returns -1 when an antenna is not
+// clear of the scene (the isotropic bound 16 (|ex| + |ey|) per antenna then applies).
+static inline double tile_halfspan_directional(const double* tx, const double* rx, size_t S, const double* origin,
+                                               const double* ex, const double* ey, const double* ez, int tile,
+                                               int tiles_x, int tiles_y, int nz, double s_r) {
+    const double nex = sqrt(ex[0] * ex[0] + ex[1] * ex[1] + ex[2] * ex[2]);
+    const double ney = sqrt(ey[0] * ey[0] + ey[1] * ey[1] + ey[2] * ey[2]);
+    const double nez = sqrt(ez[0] * ez[0] + ez[1] * ez[1] + ez[2] * ez[2]);
+    double c0[3];
+    for (int c = 0; c < 3; ++c)
+        c0[c] = origin[c] + 0.5 * (tiles_x * tile - 1) * ex[c] + 0.5 * (tiles_y * tile - 1) * ey[c] +
+                0.5 * (nz - 1) * ez[c];
+    const double D = 0.5 * (tiles_x * tile * nex + tiles_y * tile * ney + nz * nez);
+    const double half = 0.5 * tile, reach = half * (nex + ney);
+    double worst = 0.0;
+    for (size_t s = 0; s < S; ++s) {
+        double h = 0.0;
+        for (int ant = 0; ant < 2; ++ant) {
+            const double* a = (ant ? rx : tx) + 3 * s;
+            double u[3], r = 0.0;
+            for (int c = 0; c < 3; ++c) {
+                u[c] = a[c] - c0[c];
+                r += u[c] * u[c];
+            }
+            r = sqrt(r);
+            const double R = r - D - reach;
+            if (!(R > 0.0)) return -1.0;
+            double ux = 0.0, uy = 0.0;
+            for (int c = 0; c < 3; ++c) {
+                ux += u[c] * ex[c] / r;
+                uy += u[c] * ey[c] / r;
+            }
+            h += half * (fabs(ux) + fabs(uy)) + reach * D / R + reach * reach / (2.0 * R);
+        }
+        if (h > worst) worst = h;
+    }
+    return worst * s_r;
+}
+
 }  // namespace sar

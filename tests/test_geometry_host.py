@@ -94,6 +94,62 @@ def test_turned_collection_precision_in_both_layouts(transposed):
         assert pmax < 1.0e-5 and prms < 1.5e-6 and bmax < 5.0e-5, (pmax, prms, bmax)
 
 
+def tile_halfspan_bruteforce(scene, tx, rx, s_r, rng, samples=300):
+    """Largest |R(p) - R(c)| * s_r over sampled (tile, pulse) pairs (every corner tile, the rest
+    at random), R the bistatic range and c the mean of the tile's sub-tile anchors."""
+    shape, origin, ex, ey, ez = grid_axes(scene)
+    nz, ny, nx = shape
+    tx_t, ty_t = -(-nx // 32), -(-ny // 32)
+    di, dj = np.meshgrid(np.arange(-16, 16), np.arange(-16, 16))
+    off = di[..., None] * ex + dj[..., None] * ey
+    corners = [(0, 0), (tx_t - 1, 0), (0, ty_t - 1), (tx_t - 1, ty_t - 1)]
+    worst = 0.0
+    for n in range(samples):
+        ti, tj = corners[n] if n < 4 else (rng.integers(tx_t), rng.integers(ty_t))
+        k, s = rng.integers(nz), rng.integers(tx.shape[0])
+        c = origin + (32 * ti + 16) * ex + (32 * tj + 16) * ey + k * ez
+        r = np.linalg.norm(tx[s] - (c + off), axis=-1) + np.linalg.norm(rx[s] - (c + off), axis=-1)
+        rc = np.linalg.norm(tx[s] - c) + np.linalg.norm(rx[s] - c)
+        worst = max(worst, float(np.abs(r - rc).max()) * s_r)
+    return worst
+
+
+def host_halfspan(scene, tx, rx, s_r):
+    shape, origin, ex, ey, ez = grid_axes(scene)
+    nz, ny, nx = shape
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (tx, rx, origin, ex, ey, ez)]
+    return _lib.load_host().sar_tile_halfspan_host(arrs[0].ctypes.data, arrs[1].ctypes.data, tx.shape[0],
+                                                   *[a.ctypes.data for a in arrs[2:]], -(-nx // 32), -(-ny // 32),
+                                                   nz, s_r)
+
+
+@pytest.mark.parametrize("name", ["benchmark", "turned", "diagonal", "bistatic_odd", "little"])
+def test_gather_window_bound_covers_every_tile(name):
+    """The backprojection stages, per (tile, pulse), a window of bins centred on the tile's base
+    bin whose half-span comes from the look directions (sar_host_prep.h); a bin outside it would
+    be clamped.  The bound must exceed the largest sampled span in every geometry, and at the
+    benchmark geometry be about half the isotropic 16 (|ex| + |ey|) per antenna."""
+    rng = np.random.default_rng(11)
+    if name in ("bistatic_odd", "little"):
+        case = load_golden(name)
+        ap, scene = case.aperture, case.scene
+        tx, rx = ap.transmitter_positions, ap.receiver_positions
+        s_r = ap.sample_bandwidth * case.upsample_ratio / ap.c_eff
+    else:
+        az = {"benchmark": 0.0, "turned": 90.0, "diagonal": 45.0}[name]
+        tx = spotlight(4096, 5.0, centre_az_deg=az)
+        rx = tx
+        scene = GridSarScene([1, 2048, 2048], [0.0, 0.25 * 2047, 0.25 * 2047])
+        s_r = 200.0e6 * 8 / C
+    bound = host_halfspan(scene, tx, rx, s_r)
+    brute = tile_halfspan_bruteforce(scene, tx, rx, s_r, rng)
+    _, _, ex, ey, _ = grid_axes(scene)
+    iso = s_r * 2 * 16 * (np.linalg.norm(ex) + np.linalg.norm(ey))
+    assert 0 < brute <= bound <= iso * 1.001, (brute, bound, iso)
+    if name == "benchmark":
+        assert bound < 0.55 * iso
+
+
 def test_bistatic_rotated_grid_precision():
     case = load_golden("bistatic_odd")
     ap = case.aperture
