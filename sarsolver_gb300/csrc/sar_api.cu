@@ -482,7 +482,7 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
         // from global memory directly.
         p->staged = false;
         p->pb = 32;
-        for (int pb = 32; pb >= 8; pb /= 2)   // stages the two producer warps split evenly
+        for (int pb = 32; pb >= 2; pb /= 2)   // stages the two producer warps split evenly
             if (bp_grid_ws_smem_bytes(p->wwin, pb) <= kBpSmemBudget) {
                 p->pb = pb;
                 p->staged = true;
