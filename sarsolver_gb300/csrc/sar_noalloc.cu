@@ -124,9 +124,18 @@ extern "C" int sar_adjoint_from_profiles_noalloc(const sar_geometry* g, const vo
                                  g->grid_step_y[2] * g->grid_step_y[2]);
     const double h = s_r * 2.0 * 16.0 * (nex + ney);
     if (!(h < 1.0e6)) return noalloc_fail(SAR_ERR_NOT_SUPPORTED, "grid spacing too coarse for the range sampling");
-    const int wwin = (2 * ((int)std::ceil(h) + 3) + 3) & ~3;
+    const int wwin_iso = (2 * ((int)std::ceil(h) + 3) + 3) & ~3;
+    // staged window from the look directions, as a plan's (tile_halfspan_directional); the span
+    // check below keeps the isotropic margins
+    int wwin = wwin_iso;
+    {
+        const double hd = tile_halfspan_directional(g->transmit_posns, g->receive_posns, S, g->grid_origin,
+                                                    g->grid_step_x, g->grid_step_y, g->grid_step_z, 32, gc.tiles_x,
+                                                    gc.tiles_y, nz, s_r);
+        if (hd >= 0.0) wwin = std::min(wwin, (2 * ((int)std::ceil(hd) + 3) + 3) & ~3);
+    }
     gc.precise_bins = (!linear || wwin > 256) ? 1 : 0;
-    if (span < (size_t)wwin) return noalloc_fail(SAR_ERR_INVALID_ARGUMENT, "span shorter than a tile window");
+    if (span < (size_t)wwin_iso) return noalloc_fail(SAR_ERR_INVALID_ARGUMENT, "span shorter than a tile window");
 
     std::vector<PulseGeom> table(S);
     std::vector<float2> wfac(S);
@@ -169,8 +178,8 @@ extern "C" int sar_adjoint_from_profiles_noalloc(const sar_geometry* g, const vo
         wfac[s] = make_float2((float)w.real(), (float)w.imag());
     }
     // The caller's profile span must cover every staged window.
-    const double lo_needed = std::floor(vmin) - wwin / 2 - 1;
-    const double hi_needed = std::ceil(vmax) + wwin / 2 + 2;
+    const double lo_needed = std::floor(vmin) - wwin_iso / 2 - 1;
+    const double hi_needed = std::ceil(vmax) + wwin_iso / 2 + 2;
     if ((double)first_bin > lo_needed || (double)first_bin + (double)span < hi_needed)
         return noalloc_fail(SAR_ERR_INVALID_ARGUMENT, "the profile span does not cover the scene's range bins");
 
@@ -214,7 +223,7 @@ extern "C" int sar_adjoint_from_profiles_noalloc(const sar_geometry* g, const vo
                                    g->grid_step_y, g->grid_step_z, nx, ny, nz);
         a.pb = 32;
         a.staged = 0;
-        for (int pb = 32; pb >= 8; pb -= 8)
+        for (int pb = 32; pb >= 2; pb /= 2)
             if (bp_grid_ws_smem_bytes(wwin, pb) <= 110 * 1024) {
                 a.pb = pb;
                 a.staged = 1;
