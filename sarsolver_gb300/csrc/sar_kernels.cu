@@ -415,9 +415,15 @@ __device__ __forceinline__ void producer_coeffs(const GridConst& g, const PulseG
     }
 }
 
+// Pair-interleaved coefficient set of one (pulse pair, sub-tile): 2 kSetF4 float4 plus one float4
+// of padding, so that consecutive sets start 20 banks apart (48 words would put every second set
+// on the same banks and the producers' scalar stores 8-way on four banks; 52 words: 2-way).
+constexpr int kPairSetF4 = 2 * kSetF4 + 1;
+__host__ __device__ inline size_t pair_coef_f4(int pb) { return (size_t)((pb + 1) / 2) * 4 * kPairSetF4; }
+
 size_t bp_grid_ws_smem_bytes(int wwin, int pb) {
-    // windows [2][pb][wwin] + coefficient sets [2][pb][4] + base bins [2][pb] + 4 mbarriers + 4 anchors
-    return sizeof(float4) * ((size_t)2 * pb * wwin + (size_t)2 * pb * 4 * kSetF4) + sizeof(int) * 2 * pb +
+    // windows [2][pb][wwin] + coefficient sets [2][pb/2][4] + base bins [2][pb] + 4 mbarriers + 4 anchors
+    return sizeof(float4) * ((size_t)2 * pb * wwin + 2 * pair_coef_f4(pb)) + sizeof(int) * 2 * pb +
            4 * sizeof(uint64_t) + 4 * sizeof(df3);
 }
 
@@ -425,7 +431,7 @@ size_t bp_grid_ws_smem_bytes(int wwin, int pb) {
 // The same pipeline with the consumers' arithmetic on FP32 pairs (fma.rn.f32x2 and friends,
 // one instruction for two values, each rounded as the scalar operation): the two values are
 // the same pixel for two consecutive pulses p (even) and p + 1.  Coefficient sets are stored
-// pair-interleaved, kSetF4 * 2 float4 per (pulse pair, sub-tile):
+// pair-interleaved, kSetF4 * 2 float4 per (pulse pair, sub-tile) (+ one float4 of padding):
 //   [c0 c0' c1 c1'] [c2 c2' c3 c3'] [c4 c4' c5 c5'] [c6 c6' c7 c7'] [c8 c8' c9 c9']
 //   [v0 v0' v1 v1'] [v2 v2' v3 v3'] [v4 v4' v5 v5']
 //   [ia ia' ib ib'] [w0 w0' w1 w1'] [w2 w2' w3 w3'] [i0 i0' - -]  (primed: pulse p + 1; the last
@@ -463,7 +469,7 @@ __device__ __forceinline__ void producer_coeffs_pair(const GridConst& g, const P
     b = __shfl_sync(all, b, lane & ~3);
     if (valid) bin_coeffs(ae, vb, b, g, co);
     if (valid || pad) {   // the padding pulse stores zeros (co = {})
-        float* dst = reinterpret_cast<float*>(coef + ((pi >> 1) * 4 + q) * (2 * kSetF4)) + (pi & 1);
+        float* dst = reinterpret_cast<float*>(coef + ((pi >> 1) * 4 + q) * kPairSetF4) + (pi & 1);
         const float vals[24] = {co.c[0], co.c[1], co.c[2], co.c[3], co.c[4], co.c[5], co.c[6], co.c[7],
                                 co.c[8], co.c[9], co.v[0], co.v[1], co.v[2], co.v[3], co.v[4], co.v[5],
                                 co.ia,   co.ib,   co.w[0], co.w[1], co.w[2], co.w[3], co.i0,   0.f};
@@ -484,7 +490,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
     const int pb = a.pb, ww = a.wwin;
     float4* win0 = smem;
     float4* coef0 = win0 + 2 * pb * ww;
-    int* base0 = reinterpret_cast<int*>(coef0 + 2 * pb * 4 * kSetF4);
+    int* base0 = reinterpret_cast<int*>(coef0 + 2 * pair_coef_f4(pb));
     uint64_t* bars = reinterpret_cast<uint64_t*>(base0 + 2 * pb);   // full[0..1], empty[2..3]
     df3* anchors = reinterpret_cast<df3*>(bars + 4);
 
@@ -518,7 +524,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
                 break;
             }
             const int s0 = st * pb, npb = min(pb, a.S - s0);
-            float4* coef = coef0 + b * pb * 4 * kSetF4;
+            float4* coef = coef0 + b * pair_coef_f4(pb);
             int* base = base0 + b * pb;
             float4* win = win0 + (size_t)b * pb * ww;
             int mine = 0;   // pulses of this stage staged by this warp
@@ -580,13 +586,13 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
             break;
         }
         const int npp = (min(pb, a.S - st * pb) + 1) >> 1;
-        const float4* coef = coef0 + b * pb * 4 * kSetF4 + q * (2 * kSetF4);
+        const float4* coef = coef0 + b * pair_coef_f4(pb) + q * kPairSetF4;
         const float4* win = win0 + (size_t)b * pb * ww;
         float2* st_re = acc2_re;
         float2* st_im = acc2_im;
 #pragma unroll 1
         for (int pp = 0; pp < npp; ++pp) {
-            const float4* cs = coef + pp * (8 * kSetF4);
+            const float4* cs = coef + pp * (4 * kPairSetF4);
             const float4 A = cs[0], B = cs[1], C = cs[2], D = cs[3], E = cs[4], F = cs[5], G = cs[6], H = cs[7];
             // The thread's terms of both pulses: ph = cph + b1 d + b2 d^2 + c9 d^3 and
             // v = cv + bv1 d + bv2 d^2 in the offset d along the warp's axis (sar_geom.cuh Coeffs:
