@@ -94,9 +94,11 @@ typedef struct sar_geometry {
      * grid_shape = {nz, ny, nx}.  All-zero grid_shape selects the unstructured path. */
     size_t grid_shape[3];
     double grid_origin[3], grid_step_x[3], grid_step_y[3], grid_step_z[3];
-    /* Kernel path for grids: SAR_PATH_AUTO picks the grid fast path for SAR_INTERP_LINEAR and the
-     * per-pixel double-float path for SAR_INTERP_NEAREST_REF (nearest-bin decisions then match
-     * FP64 ranges); SAR_PATH_GRID / SAR_PATH_POINTS force one. */
+    /* Kernel path for grids: SAR_PATH_AUTO picks the grid fast path (for SAR_INTERP_NEAREST_REF
+     * too: bins within 5e-5 of a rounding boundary are decided again with the per-pixel
+     * double-float range, so the nearest-bin decisions match FP64 ranges on both paths), and the
+     * per-pixel path only for grids too coarse for the range sampling; SAR_PATH_GRID /
+     * SAR_PATH_POINTS force one. */
     int path;
 } sar_geometry;
 
