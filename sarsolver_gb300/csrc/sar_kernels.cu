@@ -495,7 +495,8 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
     df3* anchors = reinterpret_cast<df3*>(bars + 4);
 
     const GridConst& g = a.g;
-    int tile = blockIdx.x;
+    int tile = blockIdx.x / a.parts;
+    const int part = blockIdx.x % a.parts;
     const int tj = tile % g.tiles_y;
     tile /= g.tiles_y;
     const int ti = tile % g.tiles_x;
@@ -510,7 +511,9 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
         mbar_fence_init();
     }
     __syncthreads();
-    const int nst = (a.S + pb - 1) / pb;
+    // this CTA's share of the pulse stages: global stage st0 + st for local stage st
+    const int nst_all = (a.S + pb - 1) / pb;
+    const int st0 = part * nst_all / a.parts, nst = (part + 1) * nst_all / a.parts - st0;
 
     if (warp >= kWsConsumers / 32) {
         // ----------------------------------------------------------- producers
@@ -523,7 +526,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
                 ok = false;
                 break;
             }
-            const int s0 = st * pb, npb = min(pb, a.S - s0);
+            const int s0 = (st0 + st) * pb, npb = min(pb, a.S - s0);
             float4* coef = coef0 + b * pair_coef_f4(pb);
             int* base = base0 + b * pb;
             float4* win = win0 + (size_t)b * pb * ww;
@@ -585,7 +588,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
             ok = false;
             break;
         }
-        const int npp = (min(pb, a.S - st * pb) + 1) >> 1;
+        const int npp = (min(pb, a.S - (st0 + st) * pb) + 1) >> 1;
         const float4* coef = coef0 + b * pair_coef_f4(pb) + q * kPairSetF4;
         const float4* win = win0 + (size_t)b * pb * ww;
         float2* st_re = acc2_re;
@@ -657,7 +660,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
                     // near a rounding boundary: the exact bin, as a window index of the pulse
                     const int px = ti * kTile + (LANES_Y ? 4 * warp + r : lane);
                     const int py = tj * kTile + (LANES_Y ? lane : 4 * warp + r);
-                    const int sp = st * pb + 2 * pp;
+                    const int sp = (st0 + st) * pb + 2 * pp;
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
                         if (fabsf(h ? s.y : s.x) <= kNearEdge || sp + h >= a.S) continue;
@@ -697,6 +700,11 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
         const int j = tj * kTile + (LANES_Y ? lane : 4 * warp + r);
         if (i < g.nx && j < g.ny) {
             const size_t p = ((size_t)k * g.ny + j) * g.nx + i;
+            if (a.parts > 1) {   // the image was zeroed (or holds the sum to accumulate onto)
+                atomicAdd(&a.x[p].x, acc_re[r]);
+                atomicAdd(&a.x[p].y, acc_im[r]);
+                continue;
+            }
             float2 o = make_float2(acc_re[r], acc_im[r]);
             if (a.accumulate) {
                 const float2 old = a.x[p];
@@ -708,10 +716,32 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
     }
 }
 
-cudaError_t launch_bp_grid_ws(const BpGridArgs& a, cudaStream_t st) {
-    if (a.pb < 1 || a.pb > 32 || a.wwin < 4 || (a.wwin & 3)) return cudaErrorInvalidValue;
+// CTAs per tile: two CTAs (each over half of the pulse stages) when that fills the last wave of
+// the two-CTAs-per-SM grid clearly better (4096 tiles on 152 SMs: 13.5 waves, 96 % of the last
+// one idle-free time; 8192 CTAs: 27.0 waves, 99.8 %).  Two partial sums added to a zeroed image
+// give the same bits in either order.
+static int ws_parts(long tiles, int nst) {
+    int dev = 0, sms = 0;
+    if (nst < 4 || cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return 1;
+    const double w1 = (double)tiles / (2.0 * sms), w2 = 2.0 * w1;
+    const double e1 = w1 / std::ceil(w1), e2 = w2 / std::ceil(w2);
+    return e2 > e1 + 0.02 ? 2 : 1;
+}
+
+cudaError_t launch_bp_grid_ws(const BpGridArgs& a_in, cudaStream_t st) {
+    if (a_in.pb < 1 || a_in.pb > 32 || a_in.wwin < 4 || (a_in.wwin & 3)) return cudaErrorInvalidValue;
+    BpGridArgs a = a_in;
+    const long tiles = (long)a.g.tiles_x * a.g.tiles_y * a.g.nz;
+    a.parts = ws_parts(tiles, (a.S + a.pb - 1) / a.pb);
+    if (a.parts > 1 && !a.accumulate) {
+        const cudaError_t z =
+            cudaMemsetAsync(a.x, 0, sizeof(float2) * (size_t)a.g.nx * a.g.ny * a.g.nz, st);
+        if (z != cudaSuccess) return z;
+    }
     const size_t smem = bp_grid_ws_smem_bytes(a.wwin, a.pb);
-    const unsigned blocks = (unsigned)(a.g.tiles_x * a.g.tiles_y * a.g.nz);
+    const unsigned blocks = (unsigned)(tiles * a.parts);
     cudaError_t e;
     auto go = [&](auto kernel) -> cudaError_t {
         cudaError_t err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

@@ -39,6 +39,8 @@ struct BpGridArgs {
                                //    with the per-pixel double-float range (needs steps, alpha2)
     const double* steps;       // [9] grid steps ex, ey, ez (FP64), for those exact decisions
     const float4* alpha2;      // [S] |tx-o|^2, |rx-o|^2 as (hi, lo) pairs, the same
+    int parts;                 // set by the staged launcher: CTAs per tile, each over a share of the
+                               //    pulse stages, adding into the image with atomics when > 1
 };
 size_t bp_grid_smem_bytes(int wwin, int pb, int staged);
 cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st);
