@@ -4,12 +4,16 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--case config2]
 
 One step = one backprojection x = A^H y of the 2048^2-pixel x 4096-pulse x 4096-sample workload
-(upsample 8, linear interpolation): range-profile upsampling (pack + cuFFT + unpack) followed by
-the tiled gather kernel, with y resident in HBM.  The metric is pixel-pulses per second.
+(upsample 8, linear interpolation): the fused range-profile upsampling kernel followed by the
+tiled gather kernel, with y resident in HBM.  The metric is pixel-pulses per second.  The roofline
+denominator comes from the arithmetic-pipe rates measured on the same GPU in the same run
+(sar_measure_pipe_rates); the CPU-baseline leg also checks the GPU image against the FP64 oracle
+on a 256^2 patch over all pulses.
 
 Prints one JSON line (rank 0).  ``--impl reference`` times the reference algorithm on the host
-cores instead: the C restatement in oracle/ (bit-identical to the reference kernel where that
-kernel can be compiled), on a bounded pulse sample of the same workload, all host threads.
+cores instead: the C restatement in oracle/ in the reference's own nearest-bin arithmetic
+(bit-identical to the reference kernel where that kernel can be compiled), on a bounded pulse
+sample of the same workload, all host threads.
 """
 from __future__ import annotations
 
@@ -180,6 +184,9 @@ def run_ours(args):
     plan.enable_stage_timing(False)
     ms = reduce_max(ms, world, dev)
     value = job_throughput(P * S, world, ms)
+    flags = plan.device_flags()   # every bounded wait and window check of the timed calls
+    if flags:
+        raise RuntimeError(f"device check flags {flags:#x} raised during the timed backprojections")
 
     # ---- forward projection y = A x (same workload), device-resident, stage-timed
     y_out = torch.empty((S, N), dtype=torch.complex64, device=dev)
@@ -209,11 +216,18 @@ def run_ours(args):
     barrier()
     e2e_ms = reduce_max(e0.elapsed_time(e1) / args.steps, world, dev)
 
-    # ---- roofline of the gather kernel (SFU bound: 3 MUFU per pixel-pulse, 16 MUFU/clk/SM)
+    # ---- roofline of the gather kernel: 28 FP32 flops + 3 special-function ops per pixel-pulse
+    # (canonical work: range 10 + 1 sqrt, bin 3, interpolation 6, phase 1 + sin + cos, MAC 8), on the
+    # FP32 and SFU rates measured on this GPU now
     props = torch.cuda.get_device_properties(dev)
     peaks = measured_peaks()
     sm_max = float(peaks.get("sm_max_mhz", 0.0)) or float((clocks or {}).get("sm_max_mhz", 0.0)) or 2070.0
-    r_roof = props.multi_processor_count * sm_max * 1e6 * 16.0 / 3.0
+    rates = pipe_rates(dev)
+    fp32_units = 2.0 * rates["ffma_per_clk_sm"] / 28.0
+    sfu_units = rates["sfu_sincos_per_clk_sm"] / 3.0
+    units_per_clk = min(fp32_units, sfu_units)
+    bound = "fp32" if fp32_units <= sfu_units else "sfu"
+    r_roof = props.multi_processor_count * sm_max * 1e6 * units_per_clk
     k2_ms = stage_ms[1] / max(calls, 1)
     fft_ms = stage_ms[0] / max(calls, 1)
     achieved = P * S / (k2_ms * 1e-3)
@@ -235,10 +249,16 @@ def run_ours(args):
                                   "scatter_kernel": fstage[1] / max(fcalls, 1),
                                   "downsample_fft_side": fstage[2] / max(fcalls, 1)},
                     "note": "y = A x on the same workload (fp_grid_ws_kernel + FFT downsampling), not the headline"},
-        "roofline": {"bound": "sfu", "kernel": "bp_grid_ws_pair_kernel", "achieved": achieved, "peak": r_roof,
+        "roofline": {"bound": bound, "kernel": "bp_grid_ws_pair_kernel", "achieved": achieved, "peak": r_roof,
                      "unit": "px*pulse/s", "frac": achieved / r_roof, "traffic": traffic,
-                     "peak_basis": f"{props.multi_processor_count} SMs x {sm_max:.0f} MHz x 16 MUFU/clk/SM / "
-                                   "3 MUFU per px*pulse (sm_max_mhz of MEASURED_PEAKS.json)"},
+                     "traffic_source": "from profile: ncu dram__bytes_read.sum + dram__bytes_write.sum per "
+                                       "full-size launch, profiles/bp_grid_ws_pair_kernel_config2.md",
+                     "peak_basis": f"{props.multi_processor_count} SMs x {sm_max:.0f} MHz (sm_max_mhz of "
+                                   f"MEASURED_PEAKS.json) x min(2 x {rates['ffma_per_clk_sm']:.1f} FFMA/clk/SM / 28 "
+                                   f"FP32 flops, {rates['sfu_sincos_per_clk_sm']:.1f} sin+cos/clk/SM / 3 SFU ops) "
+                                   "per px*pulse; pipe rates measured in this run (sar_measure_pipe_rates)",
+                     "pipe_rates": rates},
+        "device_flags": flags,
         "e2e": {"value": job_throughput(P * S, world, e2e_ms), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": S * N * 8, "d2h_bytes_per_step": P * 8,
                 "api": "NumpySimpleSarOperator.backproject(pinned host complex64 tensor) -> pinned host copy"},
@@ -251,6 +271,11 @@ def run_ours(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(aperture, scene, upsample, y, args.cpu_pulses, steps=1)
+        check = oracle_check(aperture, scene, upsample, y, x)
+        result["oracle_rel_l2"] = check["rel_l2"]
+        result["cpu_baseline"]["oracle_check"] = check
+        result["cpu_baseline"]["config1"] = config1_cpu_gpu(dev)
+        result["cpu_baseline"]["config4_lsqr"] = config4_lsqr_reference()
     if rank == 0 and not args.no_cgls:
         result["cgls"] = learned_vs_plain(args.cgls_scenes)
     if world > 1:
@@ -302,6 +327,22 @@ def learned_vs_plain(scenes: int) -> dict:
     return out
 
 
+def pipe_rates(dev) -> dict:
+    """Per-SM arithmetic-pipe rates of this GPU (sar_measure_pipe_rates, include/sargpu.h)."""
+    import ctypes
+    import torch
+    from sarsolver_gb300 import _lib
+
+    lib = _lib.load()
+    r = _lib.SarPipeRates()
+    with torch.cuda.device(dev):
+        _lib.check(lib.sar_measure_pipe_rates(ctypes.byref(r), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+                   "sar_measure_pipe_rates")
+    return {"sfu_sincos_per_clk_sm": r.sfu_sincos_per_clk_sm, "frnd_per_clk_sm": r.frnd_per_clk_sm,
+            "ffma_per_clk_sm": r.ffma_per_clk_sm, "ffma2_lanes_per_clk_sm": r.ffma2_per_clk_sm,
+            "sms": r.num_sms, "probe_sm_mhz": r.sm_mhz}
+
+
 def plan_chunk(plan) -> int:
     # one FFT chunk covers all pulses for every configuration here (4 GiB of rows)
     return plan.num_slow_times
@@ -334,17 +375,158 @@ def cpu_baseline(aperture, scene, upsample, y, pulses, steps=1):
     prob = oracle.Problem(aperture.transmitter_positions[sel], aperture.receiver_positions[sel],
                           aperture.stab_ref_posns[sel], scene.positions, aperture.centre_frequency,
                           aperture.sample_bandwidth, aperture.num_freqs, upsample_ratio=upsample)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        oracle.adjoint(prob, y_np, "linear", threads=threads)
-    dt = (time.perf_counter() - t0) / steps
     units = scene.num_scatterers * pulses
+    secs = {}
+    for mode in ("linear", "nearest_ref"):
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            oracle.adjoint(prob, y_np, mode, threads=threads)
+        secs[mode] = (time.perf_counter() - t0) / steps
+    dt = secs["linear"]
     return {"value": units / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "nearest_ref_value": units / secs["nearest_ref"],
             "sample": f"full {scene.num_scatterers}-pixel image x {pulses} of {S} pulses "
-                      f"({units:.3g} px*pulses), FP64, linear interpolation, {dt:.2f} s per sample"}
+                      f"({units:.3g} px*pulses), FP64, linear interpolation (value; the GPU path's arithmetic) "
+                      f"{dt:.2f} s and nearest_ref (nearest_ref_value; the reference kernel's arithmetic) "
+                      f"{secs['nearest_ref']:.2f} s per sample"}
+
+
+def oracle_check(aperture, scene, upsample, y, x_gpu):
+    """FP64-oracle error of the timed workload's GPU image: the exact 256^2-pixel patch at the
+    scene centre over all pulses (CPU-baseline leg; the oracle only checks, it is not timed as ours)."""
+    import oracle
+
+    S, N = aperture.num_slow_times, aperture.num_freqs
+    n = scene.grid_shape[2]
+    j0 = i0 = n // 2 - 128
+    patch = np.asarray(scene.positions).reshape(n, n, 3)[j0:j0 + 256, i0:i0 + 256].reshape(-1, 3)
+    prob = oracle.Problem(aperture.transmitter_positions, aperture.receiver_positions, aperture.stab_ref_posns,
+                          patch, aperture.centre_frequency, aperture.sample_bandwidth, N, upsample_ratio=upsample)
+    t0 = time.perf_counter()
+    ref = oracle.adjoint(prob, y.cpu().numpy(), "linear", threads=oracle.default_threads())
+    dt = time.perf_counter() - t0
+    got = x_gpu.reshape(n, n)[j0:j0 + 256, i0:i0 + 256].reshape(-1).cpu().numpy().astype(np.complex128)
+    err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+    return {"rel_l2": err, "pixels": int(patch.shape[0]), "pulses": S, "oracle_seconds": dt,
+            "what": "GPU backprojection of the timed workload vs the FP64 oracle (linear), 256^2 patch at the "
+                    "scene centre, all pulses; target 1e-5"}
+
+
+def config1_cpu_gpu(dev) -> dict:
+    """Configuration 1 (128 pulses x 512 samples, U=8, 256^2 at 0.5 m, 3 deg): full forward and
+    backprojection on the host cores (the oracle port, FP64, reference nearest-bin arithmetic and
+    linear) and on the GPU, with the FP64-oracle error of the GPU results."""
+    import oracle
+    import torch
+    from sarsolver_gb300 import SarPlan
+    from sarsolver_gb300.scenes import add_noise, config_workload, reflectivity
+
+    aperture, scene, upsample, desc = config_workload("config1")
+    S, N, P = aperture.num_slow_times, aperture.num_freqs, scene.num_scatterers
+    x = reflectivity(scene.grid_shape[2], 20, 8.0, SEED + 7, device=dev, clutter_level=0.0)
+    plan = SarPlan(scene, aperture, upsample_ratio=upsample, interp="linear", device=dev)
+    y = add_noise(plan.forward(x), 20.0, SEED + 8)
+    prob = oracle.Problem(aperture.transmitter_positions, aperture.receiver_positions, aperture.stab_ref_posns,
+                          scene.positions, aperture.centre_frequency, aperture.sample_bandwidth, N,
+                          upsample_ratio=upsample)
+    threads = oracle.default_threads()
+    xn, yn = x.cpu().numpy(), y.cpu().numpy()
+    out = {"workload": desc, "cores": threads, "units": P * S}
+    for mode in ("nearest_ref", "linear"):
+        t0 = time.perf_counter()
+        yf = oracle.forward(prob, xn, mode, threads=threads)
+        t1 = time.perf_counter()
+        xa = oracle.adjoint(prob, yn, mode, threads=threads)
+        t2 = time.perf_counter()
+        out[f"cpu_{mode}_forward_s"] = t1 - t0
+        out[f"cpu_{mode}_adjoint_s"] = t2 - t1
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for name, fn in (("forward", lambda: plan.forward(x)), ("adjoint", lambda: plan.adjoint(y))):
+        for _ in range(3):
+            fn()
+        e0.record()
+        for _ in range(20):
+            r = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        out[f"gpu_linear_{name}_ms"] = e0.elapsed_time(e1) / 20
+    out["gpu_forward_rel_l2"] = float(np.linalg.norm(plan.forward(x).cpu().numpy() - yf) / np.linalg.norm(yf))
+    out["gpu_adjoint_rel_l2"] = float(np.linalg.norm(plan.adjoint(y).cpu().numpy() - xa) / np.linalg.norm(xa))
+    plan.close()
+    return out
+
+
+def config4_lsqr_reference(n: int = 128, pulses: int = 256) -> dict:
+    """CPU reference point of the learned-solver configuration at reduced size: scipy lsqr on the
+    oracle port's operator pair (FP64, linear, all host threads) to the normal-equations residual
+    ||A^H (y - A x)|| / ||A^H y|| <= 1e-3, as the GPU CGLS stops."""
+    import oracle
+    from scipy.sparse.linalg import LinearOperator, lsqr
+    from sarsolver_gb300.scenes import grid_scene, spotlight_aperture
+
+    aperture = spotlight_aperture(pulses, pulses, 4.0)
+    scene = grid_scene(n, 0.25)
+    P, S, N = scene.num_scatterers, pulses, pulses
+    prob = oracle.Problem(aperture.transmitter_positions, aperture.receiver_positions, aperture.stab_ref_posns,
+                          scene.positions, aperture.centre_frequency, aperture.sample_bandwidth, N, upsample_ratio=8.0)
+    threads = oracle.default_threads()
+    rng = np.random.default_rng(SEED + 4)
+    x_true = np.zeros(P, np.complex128)
+    idx = rng.choice(P, 40, replace=False)
+    x_true[idx] = rng.standard_normal(40) + 1j * rng.standard_normal(40)
+    y = oracle.forward(prob, x_true, "linear", threads=threads).reshape(-1)
+    noise = rng.standard_normal(y.size) + 1j * rng.standard_normal(y.size)
+    y = y + noise * np.sqrt(np.mean(np.abs(y) ** 2) / 10 ** (20 / 10) / 2)
+    op = LinearOperator((S * N, P), dtype=np.complex128,
+                        matvec=lambda v: oracle.forward(prob, v, "linear", threads=threads).reshape(-1),
+                        rmatvec=lambda v: oracle.adjoint(prob, v.reshape(S, N), "linear", threads=threads))
+    ahy = np.linalg.norm(op.rmatvec(y))
+
+    def normal_residual(x):
+        return float(np.linalg.norm(op.rmatvec(y - op.matvec(x))) / ahy)
+
+    # lsqr has no stopping rule on ||A^H r|| / ||A^H y||.  It is CGLS in exact arithmetic, so CGLS
+    # (numpy, the GPU solver's recurrence and stopping rule) finds the iteration count, then lsqr
+    # runs that many iterations (one more pair at a time while the rule does not hold yet)
+    t0 = time.perf_counter()
+    x = np.zeros(P, np.complex128)
+    r = y.copy()
+    s_ = op.rmatvec(r)
+    p_ = s_.copy()
+    gamma = np.vdot(s_, s_).real
+    k = 0
+    while np.sqrt(gamma) / ahy > 1e-3 and k < 200:
+        q = op.matvec(p_)
+        alpha = gamma / np.vdot(q, q).real
+        x += alpha * p_
+        r -= alpha * q
+        s_ = op.rmatvec(r)
+        g_new = np.vdot(s_, s_).real
+        p_ = s_ + (g_new / gamma) * p_
+        gamma = g_new
+        k += 1
+    t_cgls = time.perf_counter() - t0
+    it = max(k, 1)
+    while True:
+        t0 = time.perf_counter()
+        x = lsqr(op, y, atol=0.0, btol=0.0, conlim=0.0, iter_lim=it)[0]
+        dt = time.perf_counter() - t0
+        resid = normal_residual(x)
+        if resid <= 1e-3 or it >= 200:
+            break
+        it += 1
+    return {"workload": f"{n}^2 at 0.25 m, {pulses} pulses x {pulses} samples, U=8, 4 deg, 40 points, 20 dB "
+                        "(reduced size)", "iterations": it, "normal_residual": resid, "seconds": dt,
+            "cgls_iterations": k, "cgls_seconds": t_cgls, "cores": threads,
+            "solver": "scipy.sparse.linalg.lsqr on the FP64 oracle port (linear); CGLS (numpy) beside it"}
 
 
 def run_reference(args):
+    """The reference's own CPU arithmetic for this path, on the host cores: the oracle port in the
+    nearest-bin mode (the reference kernel's only mode, sarsolver_cxx.cpp:319-353; the port is
+    bit-identical to it where the reference compiles), all host threads, on a pulse sample of the
+    benchmark workload.  Its phase history is the sample's forward projection (oracle, FP64) of a
+    seeded scene of the benchmark's statistics plus 20 dB noise."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
@@ -358,24 +540,31 @@ def run_reference(args):
     threads = oracle.default_threads()
     rng = np.random.default_rng(SEED)
     sel = np.linspace(0, S - 1, pulses).round().astype(int)
-    y = (rng.standard_normal((pulses, N)) + 1j * rng.standard_normal((pulses, N))) / np.sqrt(2.0)
     prob = oracle.Problem(aperture.transmitter_positions[sel], aperture.receiver_positions[sel],
                           aperture.stab_ref_posns[sel], scene.positions, aperture.centre_frequency,
                           aperture.sample_bandwidth, N, upsample_ratio=upsample)
+    x = 0.3 * (rng.standard_normal(P) + 1j * rng.standard_normal(P)) / np.sqrt(2.0)
+    pts = rng.choice(P, 500, replace=False)
+    x[pts] += (rng.standard_normal(500) + 1j * rng.standard_normal(500)) / np.sqrt(2.0)
+    y = oracle.forward(prob, x, "nearest_ref", threads=threads)
+    y += np.sqrt(np.mean(np.abs(y) ** 2) / 100.0 / 2.0) * (rng.standard_normal(y.shape) + 1j * rng.standard_normal(y.shape))
     for _ in range(args.warmup):
-        oracle.adjoint(prob, y, "linear", threads=threads)
+        oracle.adjoint(prob, y, "nearest_ref", threads=threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        oracle.adjoint(prob, y, "linear", threads=threads)
+        oracle.adjoint(prob, y, "nearest_ref", threads=threads)
     dt = (time.perf_counter() - t0) / args.steps
     value = P * pulses / dt
-    sample = (f"full {P}-pixel image x {pulses} of {S} pulses per step ({P * pulses:.3g} px*pulses), "
-              "FP64, linear interpolation")
+    sample = (f"full {P}-pixel image x {pulses} of {S} pulses per step ({P * pulses:.3g} px*pulses), FP64, "
+              "nearest_ref (the reference kernel's arithmetic)")
     print(json.dumps({
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128 (fp64)", "data": "synthetic, seeded",
-        "config": {"workload": f"{args.case}: backprojection, {desc}, linear interpolation (CPU pulse sample)"},
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128 (fp64)",
+        "data": "synthetic, seeded: 500 point scatterers + complex Gaussian clutter, forward-projected by the "
+                "oracle, 20 dB noise",
+        "config": {"workload": f"{args.case}: backprojection, {desc}, CPU pulse sample, nearest-bin sampling "
+                               "(the reference has no linear interpolation)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }))

@@ -47,9 +47,11 @@ extern "C" {
 #define SAR_INTERP_LINEAR 1      /* linear interpolation; forward and adjoint exact transposes */
 
 /* Device check flags reported by sar_device_flags(). */
-#define SAR_FLAG_TILE_WINDOW 1u
-#define SAR_FLAG_STRIP_WINDOW 2u
-#define SAR_FLAG_WAIT_TIMEOUT 8u /* a bounded in-kernel wait expired; that call's result is invalid */
+#define SAR_FLAG_TILE_WINDOW 1u   /* a tile's staged window left the stored profile span */
+#define SAR_FLAG_STRIP_WINDOW 2u  /* a forward strip window left the stored profile span */
+#define SAR_FLAG_WAIT_TIMEOUT 8u  /* a bounded in-kernel wait expired; that call's result is invalid */
+#define SAR_FLAG_GATHER_WINDOW 16u /* a pixel's range bin could fall outside its tile's staged window
+                                      (window narrower than the tile's bin extent); result suspect */
 
 /* ------------------------------------------------------------ 1. drop-in boundary */
 
@@ -317,6 +319,14 @@ int sar_stage_times(sar_plan *plan, float *ms /* [3] */, int *calls);
 /* Synchronise the plan's last stream, return and clear the device check flags. */
 int sar_device_flags(sar_plan *plan, unsigned *flags);
 
+/* Wait budget of the backprojection gather's in-kernel waits between its warp roles, in SM clock
+ * cycles (0 = the default, about 2 s at 2 GHz).  When a wait runs out the kernel stops that tile,
+ * raises SAR_FLAG_WAIT_TIMEOUT and returns, and the plan stays usable.  hold_first_stage != 0 is a
+ * test aid: the gather's producer warps never publish the first pulse stage, so its consumers'
+ * first wait can only run out -- a way to check that an expired wait is reported without faulting
+ * or hanging the GPU.  New (no counterpart in the reference, which has no device code). */
+int sar_plan_set_wait_budget(sar_plan *plan, long long cycles, int hold_first_stage);
+
 /* Backprojection x = A^H y from upsampled range profiles, without allocating device memory.
  * No counterpart in the reference (its kernel allocates host buffers per call and has no GPU).
  *
@@ -331,13 +341,22 @@ int sar_device_flags(sar_plan *plan, unsigned *flags);
  * Output: x_dev, complex64 [P].  Asynchronous on `stream`.
  *
  * Scratch lives in one fixed 32 MiB device array inside the library (every GPU that loads the
- * library holds it until exit): pulses x span x 16 bytes of profile pairs plus 72 bytes per pulse
- * must fit, otherwise SAR_ERR_INVALID_ARGUMENT with a message (sar_last_error).  The array is
- * shared by all calls and keeps the last call's contents; calls that overlap on the GPU race on
- * it, so order them on one stream.  The first call on each device resolves the array's device
- * address (cudaGetSymbolAddress, with that device current); make it before any stream capture. */
+ * library holds it until exit): pulses x span x 16 bytes of profile pairs plus about 88 bytes per
+ * pulse of tables (64 pulse geometry, 8 weight, 16 antenna norms, each table rounded up to 256
+ * bytes) and 512 bytes of flags and grid steps must fit, otherwise SAR_ERR_INVALID_ARGUMENT with a
+ * message (sar_last_error).  The array is shared by all calls and keeps the last call's contents;
+ * calls that overlap on the GPU race on it, so order them on one stream.  The first call on each
+ * device resolves the array's device address (cudaGetSymbolAddress, with that device current);
+ * make it before any stream capture.  Each call clears the device check flags in the array at its
+ * start; read them with sar_noalloc_flags. */
 int sar_adjoint_from_profiles_noalloc(const sar_geometry *geom, const void *prof_dev, long first_bin,
                                       size_t span, void *x_dev, void *stream);
+
+/* Device check flags (SAR_FLAG_*) of the last sar_adjoint_from_profiles_noalloc call on the
+ * current device: waits for `stream` (the stream that call ran on), copies the flag word into
+ * *flags and clears it.  Allocates nothing.  A non-zero SAR_FLAG_WAIT_TIMEOUT means that call's
+ * image is invalid. */
+int sar_noalloc_flags(unsigned *flags, void *stream);
 
 /* Device address of page-locked, mapped host memory (cudaHostGetDevicePointer), for passing a
  * pinned host buffer to a call that reads it on the device -- e.g. the phase history of
@@ -347,6 +366,23 @@ int sar_adjoint_from_profiles_noalloc(const sar_geometry *geom, const void *prof
  * device cannot address the memory (on systems whose GPU translates host page tables, e.g. over a
  * chip-to-chip link, pageable memory is addressable too and comes back at its host address). */
 int sar_host_device_pointer(const void *host_ptr, void **dev_ptr);
+
+/* Throughput of the arithmetic pipes the backprojection gather uses, measured on the current
+ * device: operations per clock per SM (median SM; every thread of a full wave of CTAs runs
+ * independent chains of one operation, timed with the SM's own cycle counter), for
+ *   sfu_sincos_per_clk_sm  special-function sine and cosine (__sincosf: two operations each call)
+ *   frnd_per_clk_sm        FP32 round to integer (rintf)
+ *   ffma_per_clk_sm        FP32 fused multiply-add
+ *   ffma2_per_clk_sm       FP32 fused multiply-adds issued as pairs (two per instruction)
+ * and the SM clock that held meanwhile (cycles over event time, a lower bound).  The roofline of
+ * the gather is SMs x clock x min(FP32 lanes / FP32 ops, SFU rate / SFU ops) per pixel·pulse.
+ * A measurement aid with no counterpart in the reference; allocates a few bytes. */
+typedef struct sar_pipe_rates {
+    double sfu_sincos_per_clk_sm, frnd_per_clk_sm, ffma_per_clk_sm, ffma2_per_clk_sm;
+    int num_sms;
+    double sm_mhz;
+} sar_pipe_rates;
+int sar_measure_pipe_rates(sar_pipe_rates *out, void *stream);
 
 /* Last error message of the calling thread (empty if none); returns its full length. */
 size_t sar_last_error(char *buf, size_t len);

@@ -34,7 +34,10 @@ EXPORTED = (
     "sar_unet_create", "sar_unet_destroy", "sar_unet_info", "sar_unet_set_params", "sar_unet_get_params",
     "sar_unet_get_grads", "sar_unet_zero_grad", "sar_unet_forward", "sar_unet_backward", "sar_unet_adam_step",
     "sar_unet_flags", "sar_conv2d_forward_bf16", "sar_conv2d_wgrad_bf16",
+    "sar_noalloc_flags", "sar_plan_set_wait_budget", "sar_measure_pipe_rates",
 )
+
+SAR_FLAG_TILE_WINDOW, SAR_FLAG_STRIP_WINDOW, SAR_FLAG_WAIT_TIMEOUT, SAR_FLAG_GATHER_WINDOW = 1, 2, 8, 16
 
 SAR_UNET_LAYERS = 15
 SAR_CPHD_CI2, SAR_CPHD_CI4, SAR_CPHD_CF8 = 1, 2, 3
@@ -75,6 +78,13 @@ class SarPdhgResult(ctypes.Structure):
 
     _fields_ = [("iterations", c_int), ("sigma", c_double), ("tau", c_double), ("theta", c_double),
                 ("operator_norm", c_double)]
+
+
+class SarPipeRates(ctypes.Structure):
+    """Mirror of ``sar_pipe_rates``."""
+    _fields_ = [("sfu_sincos_per_clk_sm", ctypes.c_double), ("frnd_per_clk_sm", ctypes.c_double),
+                ("ffma_per_clk_sm", ctypes.c_double), ("ffma2_per_clk_sm", ctypes.c_double),
+                ("num_sms", c_int), ("sm_mhz", ctypes.c_double)]
 
 
 class SarPlanInfo(ctypes.Structure):
@@ -143,6 +153,12 @@ def load() -> ctypes.CDLL:
     lib.sar_host_device_pointer.restype = c_int
     lib.sar_adjoint_pulse_block.argtypes = [c_void_p, c_void_p, c_size_t, c_size_t, c_void_p, c_int, c_void_p]
     lib.sar_adjoint_pulse_block.restype = c_int
+    lib.sar_noalloc_flags.argtypes = [POINTER(c_uint), c_void_p]
+    lib.sar_noalloc_flags.restype = c_int
+    lib.sar_plan_set_wait_budget.argtypes = [c_void_p, ctypes.c_longlong, c_int]
+    lib.sar_plan_set_wait_budget.restype = c_int
+    lib.sar_measure_pipe_rates.argtypes = [POINTER(SarPipeRates), c_void_p]
+    lib.sar_measure_pipe_rates.restype = c_int
     lib.sar_move_srps.argtypes = [c_void_p, c_void_p, c_size_t, c_size_t, c_void_p, c_double, c_double, c_double,
                                   c_double, c_void_p]
     lib.sar_move_srps.restype = c_int
@@ -227,5 +243,11 @@ def load_host() -> ctypes.CDLL:
         lib.sar_tile_halfspan_host.restype = c_double
         lib.sar_geom_host_eval_points.argtypes = [P, c_size_t, P, c_size_t, P, P, P, c_double, c_double,
                                                   ctypes.c_float, P, P]
+        lib.sar_gather_window_check_host.argtypes = [P, P, P, P, c_int, c_int, c_int, c_size_t, P, P, P, c_double,
+                                                     c_double, ctypes.c_float, c_int, c_int, P]
+        lib.sar_gather_window_check_host.restype = c_long
+        lib.sar_bin_extent_host.argtypes = [P, P, P, P, c_int, c_int, c_int, P, P, P, c_double, c_double,
+                                            ctypes.c_float, c_int, c_int, c_int, c_int, c_int, P]
+        lib.sar_bin_extent_host.restype = c_int
         _HOST = lib
     return _HOST

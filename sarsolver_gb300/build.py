@@ -21,7 +21,7 @@ INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fno-fast-math"]
-CUDA_UNITS = ["sar_kernels.cu", "sar_api.cu", "sar_noalloc.cu", "sar_cgls.cu", "sar_unet.cu", "sar_resample.cu", "sar_cphd.cu", "sar_pdhg.cu"]
+CUDA_UNITS = ["sar_kernels.cu", "sar_api.cu", "sar_noalloc.cu", "sar_cgls.cu", "sar_unet.cu", "sar_resample.cu", "sar_cphd.cu", "sar_pdhg.cu", "sar_probe.cu"]
 HEADERS = ["sar_geom.cuh", "sar_host_prep.h", "sar_kernels.cuh", "unet_tc.cuh", "sar_fft_cb.h", "sar_solver_common.cuh"]
 # cuFFT load/store callbacks: compiled to LTO-IR, embedded in the library as a byte array and
 # handed to cufftXtSetJITCallback at plan creation.

@@ -146,3 +146,93 @@ extern "C" double sar_tile_halfspan_host(const double* tx, const double* rx, siz
                                          int tiles_y, int nz, double s_r) {
     return tile_halfspan_directional(tx, rx, num_pulses, origin, ex, ey, ez, 32, tiles_x, tiles_y, nz, s_r);
 }
+
+// The gather producer's window check on the host: for every (tile, pulse) pair of the given pulses,
+// the sub-tile coefficient sets and base bin exactly as the kernel forms them, then bin_extent
+// against a staged window of ww bins.  Returns the number of sets that would raise
+// FLAG_GATHER_WINDOW, and in *needed_half the smallest half-window (bins) that covers them all.
+extern "C" long sar_gather_window_check_host(const double* origin, const double* ex, const double* ey,
+                                             const double* ez, int nx, int ny, int nz, size_t num_pulses,
+                                             const double* tx, const double* rx, const double* srp, double kappa,
+                                             double s_r, float bin_offset, int precise_bins, int ww,
+                                             double* needed_half) {
+    if (nx <= 0 || ny <= 0 || nz <= 0) return -1;
+    GridConst g = make_grid_const(ex, ey, ez, kappa, s_r, bin_offset, nx, ny, nz);
+    g.precise_bins = precise_bins;
+    const float half = 0.5f * (float)ww;
+    long bad = 0;
+    double need = 0.0;
+    for (size_t s = 0; s < num_pulses; ++s) {
+        PulseGeom pg = make_pulse_geom(tx + 3 * s, rx + 3 * s, srp + 3 * s, origin);
+        for (int k = 0; k < nz; ++k)
+            for (int tj = 0; tj < g.tiles_y; ++tj)
+                for (int ti = 0; ti < g.tiles_x; ++ti) {
+                    Coeffs co[4];
+                    AnchorExpansion ae[4];
+                    df vb[4];
+                    df vsum = df_make(0.0f, 0.0f);
+                    for (int q = 0; q < 4; ++q) {
+                        df3 anchor = pixel_position(ti * 32 + 8 + 16 * (q & 1), tj * 32 + 8 + 16 * (q >> 1), k, g);
+                        ae[q] = expand_anchor(anchor, pg, g);
+                        vb[q] = anchor_bin(ae[q], g);
+                        vsum = df_add(vsum, vb[q]);
+                    }
+                    const int base = base_bin_of(vsum, 4.0f);
+                    for (int q = 0; q < 4; ++q) {
+                        co[q] = Coeffs{};
+                        bin_coeffs(ae[q], vb[q], base, g, co[q]);
+                        float lo, hi;
+                        bin_extent(co[q], &lo, &hi);
+                        if (!(lo >= -half - 0.49f && hi <= half - 0.51f)) ++bad;
+                        need = fmax(need, fmax(-(double)lo - 0.49, (double)hi + 0.51));
+                    }
+                }
+    }
+    if (needed_half) *needed_half = need;
+    return bad;
+}
+
+// bin_extent of the coefficient set of sub-tile q of tile (ti, tj, k) for one pulse (lo, hi), and
+// the extreme bins the kernels' per-pixel evaluation actually forms over that sub-tile (both
+// relative to the tile's base bin), to check that the bound holds.
+extern "C" int sar_bin_extent_host(const double* origin, const double* ex, const double* ey, const double* ez,
+                                   int nx, int ny, int nz, const double* tx, const double* rx, const double* srp,
+                                   double kappa, double s_r, float bin_offset, int precise_bins, int ti, int tj,
+                                   int k, int q, double* out4) {
+    GridConst g = make_grid_const(ex, ey, ez, kappa, s_r, bin_offset, nx, ny, nz);
+    g.precise_bins = precise_bins;
+    PulseGeom pg = make_pulse_geom(tx, rx, srp, origin);
+    AnchorExpansion ae[4];
+    df vb[4];
+    df vsum = df_make(0.0f, 0.0f);
+    for (int r = 0; r < 4; ++r) {
+        df3 anchor = pixel_position(ti * 32 + 8 + 16 * (r & 1), tj * 32 + 8 + 16 * (r >> 1), k, g);
+        ae[r] = expand_anchor(anchor, pg, g);
+        vb[r] = anchor_bin(ae[r], g);
+        vsum = df_add(vsum, vb[r]);
+    }
+    const int base = base_bin_of(vsum, 4.0f);
+    Coeffs co{};
+    phase_coeffs(ae[q], g, co.c);
+    bin_coeffs(ae[q], vb[q], base, g, co);
+    float lo, hi;
+    bin_extent(co, &lo, &hi);
+    double vmin = 1e300, vmax = -1e300;
+    const bool pr = precise_bins != 0;
+    for (int a = -8; a < 8; ++a)
+        for (int b = -8; b < 8; ++b) {
+            const float di = (float)a, dj = (float)b;
+            ColumnTerms ct = pr ? column_terms<true>(co, di, di * di, di * di * di)
+                                : column_terms<false>(co, di, di * di, di * di * di);
+            const float v = pr ? pixel_bin<true>(ct, co.w[3], dj, dj * dj, dj * dj * dj)
+                               : pixel_bin<false>(ct, 0.0f, dj, dj * dj, dj * dj * dj);
+            const double tot = (double)v + (pr ? (double)fmaf(co.ib, dj, ct.ci) : 0.0);
+            vmin = fmin(vmin, tot);
+            vmax = fmax(vmax, tot);
+        }
+    out4[0] = lo;
+    out4[1] = hi;
+    out4[2] = vmin;
+    out4[3] = vmax;
+    return 0;
+}

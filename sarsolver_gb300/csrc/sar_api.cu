@@ -128,6 +128,8 @@ struct sar_plan {
     float4* d_prof = nullptr;   // [S][Lg] pairs (adjoint) / float2 accumulator (forward)
     int* d_strip = nullptr;
     unsigned* d_flags = nullptr;
+    long long wait_budget = kDefaultWaitBudgetCycles;   // bounded in-kernel waits of the gather
+    int hold_first_stage = 0;                           // test aid (sar_plan_set_wait_budget)
     size_t device_bytes = 0;
     cufftHandle fft_full = 0, fft_tail = 0;
     bool have_full = false, have_tail = false;
@@ -894,12 +896,11 @@ int sar_adjoint(sar_plan* p, const void* y_dev, void* x_dev, void* stream) {
         a.staged = p->staged;
         a.accumulate = 0;
         a.lanes_y = p->lanes_y;
-    a.nearest = p->interp == SAR_INTERP_NEAREST_REF;
-    a.steps = p->d_steps;
-    a.alpha2 = p->d_alpha2;
         a.nearest = p->interp == SAR_INTERP_NEAREST_REF;
         a.steps = p->d_steps;
         a.alpha2 = p->d_alpha2;
+        a.wait_budget = p->wait_budget;
+        a.hold_first_stage = p->hold_first_stage;
         SAR_CUDA(p->staged ? launch_bp_grid_ws(a, st) : launch_bp_grid(a, st), "backprojection");
     } else {
         SAR_CUDA(launch_bp_points(point_args(p, p->interp == SAR_INTERP_LINEAR ? BIN_LINEAR : BIN_ADJ_NEAREST), p->d_prof, (float2*)x_dev, 0, st),
@@ -1014,6 +1015,8 @@ int sar_adjoint_pulse_block(sar_plan* p, const void* y_block_dev, size_t first_p
     a.nearest = p->interp == SAR_INTERP_NEAREST_REF;
     a.steps = p->d_steps;
     a.alpha2 = p->d_alpha2;
+    a.wait_budget = p->wait_budget;
+    a.hold_first_stage = p->hold_first_stage;
     SAR_CUDA(p->staged ? launch_bp_grid_ws(a, st) : launch_bp_grid(a, st), "backprojection");
     return SAR_OK;
 }
@@ -1095,6 +1098,15 @@ int sar_stage_times(sar_plan* p, float* ms, int* calls) {
         }
     }
     *calls = (int)p->events_used;
+    return SAR_OK;
+}
+
+int sar_plan_set_wait_budget(sar_plan* p, long long cycles, int hold_first_stage) {
+    if (!p) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    if (cycles < 0) return fail(SAR_ERR_INVALID_ARGUMENT, "negative wait budget");
+    std::lock_guard<std::mutex> lock(p->mu);
+    p->wait_budget = cycles ? cycles : kDefaultWaitBudgetCycles;
+    p->hold_first_stage = hold_first_stage ? 1 : 0;
     return SAR_OK;
 }
 

@@ -347,6 +347,27 @@ SAR_HD void bin_coeffs(const AnchorExpansion& a, df vbin, int base_bin, const Gr
     co.v[5] = sr * a.q[2];
 }
 
+// Range [lo, hi] of the bin polynomial of a coefficient set (relative to the tile's base bin,
+// including the exact integer part) over the pixel offsets di, dj in [-8, 7] of a 16x16 sub-tile:
+// each monomial's extreme values over that box, summed term by term (an upper bound of the true
+// extent, tight for the linear terms that dominate it).  The gather uses it to prove that every
+// pixel's bin lies inside its tile's staged window.
+SAR_HD void bin_extent(const Coeffs& co, float* lo, float* hi) {
+    // monomials di, dj, di^2, di dj, dj^2, di^3, di^2 dj, di dj^2, dj^3 over [-8, 7]^2
+    const float mlo[9] = {-8.f, -8.f, 0.f, -56.f, 0.f, -512.f, -512.f, -512.f, -512.f};
+    const float mhi[9] = {7.f, 7.f, 64.f, 64.f, 64.f, 343.f, 448.f, 448.f, 343.f};
+    const float cf[9] = {co.v[1] + co.ia, co.v[2] + co.ib, co.v[3], co.v[4], co.v[5],
+                         co.w[0], co.w[1], co.w[2], co.w[3]};
+    float l = co.v[0] + co.i0, h = l;
+    for (int t = 0; t < 9; ++t) {
+        const float a = cf[t] * mlo[t], b = cf[t] * mhi[t];
+        l += fminf(a, b);
+        h += fmaxf(a, b);
+    }
+    *lo = l;
+    *hi = h;
+}
+
 // Anchor position of pixel (i, j, k) relative to the grid origin.
 SAR_HD df3 pixel_position(int i, int j, int k, const GridConst& g) {
     df3 p = df3_scale_int(g.ex, (float)i);

@@ -331,7 +331,7 @@ cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st) {
 constexpr int kWsConsumers = 256;
 constexpr int kWsProducers = 2;   // producer warps; producer w handles pulse passes 8w, 8w + 16, ...
 constexpr int kWsThreads = kWsConsumers + 32 * kWsProducers;
-constexpr long long kWaitBudgetCycles = 4000000000ll;   // ~2 s at 2 GHz
+constexpr long long kWaitBudgetCycles = kDefaultWaitBudgetCycles;
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -361,15 +361,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 // Bounded wait for completion of the barrier phase with the given parity.  Between polls the
 // warp sleeps with exponential backoff (first_ns doubling up to max_ns), so waiting warps leave
 // the issue slots to the gathering warps and poll only a few times per wait; the wait gives up
-// after kWaitBudgetCycles.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned first_ns, unsigned max_ns) {
+// after `budget` clock cycles (kWaitBudgetCycles unless the launch sets its own).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned first_ns, unsigned max_ns,
+                                          long long budget = kWaitBudgetCycles) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     unsigned ns = first_ns;
     while (true) {
         __nanosleep(ns);
         if (mbar_try_wait(bar, parity)) return true;
-        if (clock64() - t0 > kWaitBudgetCycles) return false;
+        if (clock64() - t0 > budget) return false;
         ns = min(2 * ns, max_ns);
     }
 }
@@ -449,7 +450,7 @@ __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a
 
 __device__ __forceinline__ void producer_coeffs_pair(const GridConst& g, const PulseGeom* __restrict__ pulses, int s0,
                                                      int npb, int pass, const df3* anchors, float4* coef, int* base,
-                                                     int lane) {
+                                                     int lane, int ww, unsigned* flags) {
     const int pi = pass + (lane >> 2), q = lane & 3;
     const bool valid = pi < npb;
     const bool pad = pi == npb && (npb & 1);   // partner of the last pulse of an odd stage
@@ -467,7 +468,15 @@ __device__ __forceinline__ void producer_coeffs_pair(const GridConst& g, const P
     sum = df_add(sum, df_make(__shfl_xor_sync(all, sum.hi, 2), __shfl_xor_sync(all, sum.lo, 2)));
     int b = base_bin_of(sum, 4.0f);
     b = __shfl_sync(all, b, lane & ~3);
-    if (valid) bin_coeffs(ae, vb, b, g, co);
+    if (valid) {
+        bin_coeffs(ae, vb, b, g, co);
+        // every pixel's bin must fall inside the tile's staged window: index rint(v) + ww / 2 in
+        // [0, ww - 1] (the consumers clamp, so an undersized window would otherwise pass silently)
+        float lo, hi;
+        bin_extent(co, &lo, &hi);
+        const float half = 0.5f * (float)ww;
+        if (!(lo >= -half - 0.49f && hi <= half - 0.51f)) raise_flag(flags, FLAG_GATHER_WINDOW);
+    }
     if (valid || pad) {   // the padding pulse stores zeros (co = {})
         float* dst = reinterpret_cast<float*>(coef + ((pi >> 1) * 4 + q) * kPairSetF4) + (pi & 1);
         const float vals[24] = {co.c[0], co.c[1], co.c[2], co.c[3], co.c[4], co.c[5], co.c[6], co.c[7],
@@ -522,9 +531,13 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
         int issued = 0;
         for (int st = 0; st < nst; ++st) {
             const int b = st & 1;
-            if (st >= 2 && !mbar_wait(&bars[2 + b], ((st - 2) >> 1) & 1, 128, 2048)) {
+            if (st >= 2 && !mbar_wait(&bars[2 + b], ((st - 2) >> 1) & 1, 128, 2048, a.wait_budget)) {
                 ok = false;
                 break;
+            }
+            if (st == 0 && a.hold_first_stage) {   // nothing computed, copied or arrived for it
+                issued = 1;
+                continue;
             }
             const int s0 = (st0 + st) * pb, npb = min(pb, a.S - s0);
             float4* coef = coef0 + b * pair_coef_f4(pb);
@@ -532,7 +545,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
             float4* win = win0 + (size_t)b * pb * ww;
             int mine = 0;   // pulses of this stage staged by this warp
             for (int pass = 8 * pw; pass < npb; pass += 8 * kWsProducers) {
-                producer_coeffs_pair(g, a.pulses, s0, npb, pass, anchors, coef, base, lane);
+                producer_coeffs_pair(g, a.pulses, s0, npb, pass, anchors, coef, base, lane, ww, a.flags);
                 mine += min(8, npb - pass);
                 if ((npb & 1) && npb - pass < 8) {   // this pass holds the padding pulse: zero its window
                     float4* pw_ = win + (size_t)npb * ww;
@@ -556,8 +569,10 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
             }
             issued = st + 1;
         }
+        // drain: wait (with the full budget) for this warp's own copies of the last two stages, so
+        // that no bulk copy into this CTA's shared memory is in flight when it exits
         for (int st = max(0, issued - 2); st < issued; ++st)
-            if (!mbar_wait(&bars[st & 1], (st >> 1) & 1, 128, 2048)) ok = false;
+            if (!(st == 0 && a.hold_first_stage) && !mbar_wait(&bars[st & 1], (st >> 1) & 1, 128, 2048)) ok = false;
         if (!ok && lane == 0) raise_flag(a.flags, FLAG_WAIT_TIMEOUT);
         return;
     }
@@ -584,7 +599,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
     bool ok = true;
     for (int st = 0; st < nst; ++st) {
         const int b = st & 1;
-        if (!mbar_wait(&bars[b], (st >> 1) & 1, 32, 256)) {
+        if (!mbar_wait(&bars[b], (st >> 1) & 1, 32, 256, a.wait_budget)) {
             ok = false;
             break;
         }
@@ -700,7 +715,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
         const int j = tj * kTile + (LANES_Y ? lane : 4 * warp + r);
         if (i < g.nx && j < g.ny) {
             const size_t p = ((size_t)k * g.ny + j) * g.nx + i;
-            if (a.parts > 1) {   // the image was zeroed (or holds the sum to accumulate onto)
+            if (a.parts > 1) {   // the image was zeroed by the launcher (parts > 1 never accumulates)
                 atomicAdd(&a.x[p].x, acc_re[r]);
                 atomicAdd(&a.x[p].y, acc_im[r]);
                 continue;
@@ -719,10 +734,11 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
 // CTAs per tile: two CTAs (each over half of the pulse stages) when that fills the last wave of
 // the two-CTAs-per-SM grid clearly better (4096 tiles on 152 SMs: 13.5 waves, 96 % of the last
 // one idle-free time; 8192 CTAs: 27.0 waves, 99.8 %).  Two partial sums added to a zeroed image
-// give the same bits in either order.
-static int ws_parts(long tiles, int nst) {
+// give the same bits in either order; added onto an image that already holds a sum (accumulate)
+// they would be three terms in run-dependent order, so accumulating launches use one CTA per tile.
+static int ws_parts(long tiles, int nst, int accumulate) {
     int dev = 0, sms = 0;
-    if (nst < 4 || cudaGetDevice(&dev) != cudaSuccess ||
+    if (accumulate || nst < 4 || cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
         return 1;
     const double w1 = (double)tiles / (2.0 * sms), w2 = 2.0 * w1;
@@ -734,8 +750,8 @@ cudaError_t launch_bp_grid_ws(const BpGridArgs& a_in, cudaStream_t st) {
     if (a_in.pb < 1 || a_in.pb > 32 || a_in.wwin < 4 || (a_in.wwin & 3)) return cudaErrorInvalidValue;
     BpGridArgs a = a_in;
     const long tiles = (long)a.g.tiles_x * a.g.tiles_y * a.g.nz;
-    a.parts = ws_parts(tiles, (a.S + a.pb - 1) / a.pb);
-    if (a.parts > 1 && !a.accumulate) {
+    a.parts = ws_parts(tiles, (a.S + a.pb - 1) / a.pb, a.accumulate);
+    if (a.parts > 1) {
         const cudaError_t z =
             cudaMemsetAsync(a.x, 0, sizeof(float2) * (size_t)a.g.nx * a.g.ny * a.g.nz, st);
         if (z != cudaSuccess) return z;

@@ -14,7 +14,11 @@ enum : unsigned {
     FLAG_STRIP_WINDOW = 2u,   // a forward strip window left the stored profile span
     FLAG_BIN_CLAMP = 4u,      // a per-pixel bin index was clamped (debug builds only)
     FLAG_WAIT_TIMEOUT = 8u,   // a bounded mbarrier wait gave up (the result is invalid)
+    FLAG_GATHER_WINDOW = 16u, // a sub-tile's bin extent exceeded its tile's staged window
 };
+
+// Clock budget of a bounded in-kernel wait (about 2 s at 2 GHz) unless a launch sets its own.
+constexpr long long kDefaultWaitBudgetCycles = 4000000000ll;
 
 constexpr int kTile = 32;          // pixels per tile side
 constexpr int kThreads = 256;      // threads per tile CTA: 32 columns x 8 warps, 4 rows each
@@ -30,7 +34,8 @@ struct BpGridArgs {
     unsigned* flags;
     int S, Lg, bg0;            // stored profile span: bins [bg0, bg0 + Lg)
     int wwin;                  // staged window per (tile, pulse), multiple of 4
-    int pb;                    // pulses per stage (multiple of 8, <= 32)
+    int pb;                    // pulses per stage: a power of two from 2 to 32 (odd last stages are
+                               //    padded with a zero pulse by the paired kernel)
     int staged;                // 1: stage windows in shared memory; 0: read global directly
     int accumulate;            // 1: x += result
     int lanes_y;               // 1: lanes of a warp run along y (chosen when bins change more slowly
@@ -41,6 +46,10 @@ struct BpGridArgs {
     const float4* alpha2;      // [S] |tx-o|^2, |rx-o|^2 as (hi, lo) pairs, the same
     int parts;                 // set by the staged launcher: CTAs per tile, each over a share of the
                                //    pulse stages, adding into the image with atomics when > 1
+    long long wait_budget = kDefaultWaitBudgetCycles;   // clock cycles a staged-kernel wait on the
+                               //    other warp role may take before it gives up (FLAG_WAIT_TIMEOUT)
+    int hold_first_stage = 0;  // test aid: the producers never publish the first pulse stage, so the
+                               //    consumers' first wait can only run out (nothing is copied for it)
 };
 size_t bp_grid_smem_bytes(int wwin, int pb, int staged);
 cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st);

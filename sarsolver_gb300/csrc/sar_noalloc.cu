@@ -9,7 +9,7 @@
 //
 // Scratch: `g_noalloc_scratch`, a file-scope __device__ array of kScratchBytes (32 MiB).  Every
 // GPU that loads the library holds it until the process exits.  Layout per call:
-//   [0, 256)            device check flags (cleared by every call)
+//   [0, 256)            device check flags (cleared by every call, read by sar_noalloc_flags)
 //   pulse table         S x 64 bytes (PulseGeom, double-float antenna positions)
 //   pulse factors       S x 8 bytes (slow-time weight, conjugated for linear interpolation)
 //   grid steps          9 doubles, and antenna norms S x 16 bytes (nearest-bin decisions near a
@@ -231,6 +231,23 @@ extern "C" int sar_adjoint_from_profiles_noalloc(const sar_geometry* g, const vo
             }
         e = a.staged ? launch_bp_grid_ws(a, st) : launch_bp_grid(a, st);
     }
+    if (e != cudaSuccess) return noalloc_fail(SAR_ERR_CUDA, cudaGetErrorString(e));
+    return SAR_OK;
+}
+
+// Flag word of the last call on the current device (the first 4 bytes of the array): read after
+// `stream` has passed that call, then cleared, with no allocation.
+extern "C" int sar_noalloc_flags(unsigned* flags, void* stream) {
+    sar_internal_set_error("");
+    if (!flags) return noalloc_fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    void* base = nullptr;
+    int rc = scratch_address(&base);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaMemcpy(flags, base, sizeof(unsigned), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemsetAsync(base, 0, sizeof(unsigned), st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return noalloc_fail(SAR_ERR_CUDA, cudaGetErrorString(e));
     return SAR_OK;
 }

@@ -12,25 +12,62 @@ and ``adjoint_evaluate`` are libsargpu.so's drop-in entry points with the refere
 """
 from __future__ import annotations
 
+import hashlib
+from collections import OrderedDict
 from typing import Optional
 
 import numpy as np
 
 from . import _lib
 from ._lib import SarCalculationInfo  # noqa: F401  (re-exported, reference layout)
+from .geometry import grid_axes
 from .plan import SarPlan
 
-_PLAN_CACHE: dict = {}
+_PLAN_CACHE: "OrderedDict[tuple, SarPlan]" = OrderedDict()
+_PLAN_CACHE_SIZE = 8
+
+
+def geometry_fingerprint(scene, measurements) -> str:
+    """Digest of everything a plan copies from the scene and the aperture: antenna and SRP
+    positions, waveform, slow-time weighting, frequencies, c_eff, sign, and the grid (origin,
+    steps, shape) or the scatterer positions.  Two calls share a plan only when these agree, so
+    a new or mutated aperture (e.g. a new slow_time_weighting) never reuses stale device tables."""
+    h = hashlib.blake2b(digest_size=20)
+
+    def add(a, dtype):
+        arr = np.ascontiguousarray(np.asarray(a, dtype=dtype))
+        h.update(str(arr.shape).encode())
+        h.update(arr.tobytes())
+
+    ap = measurements
+    for a in (ap.transmitter_positions, ap.receiver_positions, ap.stab_ref_posns):
+        add(a, np.float64)
+    add(ap.waveform_fft, np.complex128)
+    add(ap.slow_time_weighting, np.complex128)
+    add([ap.centre_frequency, ap.sample_bandwidth, ap.c_eff, ap.sign_multiplier, ap.num_freqs], np.float64)
+    axes = grid_axes(scene)
+    if axes is not None:
+        shape, origin, ex, ey, ez = axes
+        h.update(b"grid")
+        add(list(shape), np.float64)
+        for a in (origin, ex, ey, ez):
+            add(a, np.float64)
+    else:
+        h.update(b"points")
+        add(scene.positions, np.float64)
+    return h.hexdigest()
 
 
 def _plan_for(scene, measurements, upsample_ratio: float, interp: str) -> SarPlan:
-    key = (id(scene), id(measurements), float(upsample_ratio), interp)
+    key = (geometry_fingerprint(scene, measurements), float(upsample_ratio), interp)
     plan = _PLAN_CACHE.get(key)
     if plan is None:
-        if len(_PLAN_CACHE) > 8:
-            _PLAN_CACHE.clear()
+        while len(_PLAN_CACHE) >= _PLAN_CACHE_SIZE:
+            _PLAN_CACHE.popitem(last=False)
         plan = SarPlan(scene, measurements, upsample_ratio=upsample_ratio, interp=interp)
         _PLAN_CACHE[key] = plan
+    else:
+        _PLAN_CACHE.move_to_end(key)
     return plan
 
 

@@ -253,6 +253,13 @@ class SarPlan:
         _lib.check(self._lib.sar_stage_times(self._handle, ms, ctypes.byref(calls)), "sar_stage_times")
         return [float(v) for v in ms], int(calls.value)
 
+    def set_wait_budget(self, cycles: int = 0, hold_first_stage: bool = False) -> None:
+        """Clock-cycle budget of the gather's bounded in-kernel waits (0: the default, ~2 s).
+        ``hold_first_stage`` is a test aid that makes the first wait run out (see
+        sar_plan_set_wait_budget); the expiry shows up as SAR_FLAG_WAIT_TIMEOUT in device_flags()."""
+        _lib.check(self._lib.sar_plan_set_wait_budget(self._handle, int(cycles), int(bool(hold_first_stage))),
+                   "sar_plan_set_wait_budget")
+
     def device_flags(self) -> int:
         """Synchronise and return (then clear) the device check flags; 0 means no check fired."""
         f = ctypes.c_uint(0)

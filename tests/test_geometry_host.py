@@ -269,3 +269,86 @@ def test_wgs84_up_is_the_ellipsoid_normal():
     n = WGS84_A / np.sqrt(1 - e2 * np.sin(lat) ** 2)
     p = np.array([(n + h) * np.cos(lat) * np.cos(lon), (n + h) * np.cos(lat) * np.sin(lon), (n * (1 - e2) + h) * np.sin(lat)])
     np.testing.assert_allclose(wgs84_up(p), [np.cos(lat) * np.cos(lon), np.cos(lat) * np.sin(lon), np.sin(lat)], atol=1e-12)
+
+
+def plan_tile_window(scene, tx, rx, s_r):
+    """Staged window (bins) the plan gives a tile, as build_plan sizes it: the isotropic bound,
+    narrowed to the look-direction bound where that is smaller (both with 3 bins of margin)."""
+    _, _, ex, ey, _ = grid_axes(scene)
+    iso = s_r * 2.0 * 16.0 * (np.linalg.norm(ex) + np.linalg.norm(ey))
+    w = (2 * (int(np.ceil(iso)) + 3) + 3) & ~3
+    hd = host_halfspan(scene, tx, rx, s_r)
+    if hd >= 0:
+        w = min(w, (2 * (int(np.ceil(hd)) + 3) + 3) & ~3)
+    return w
+
+
+def window_check(scene, tx, rx, srp, kappa, s_r, bin_offset, precise, ww):
+    shape, origin, ex, ey, ez = grid_axes(scene)
+    nz, ny, nx = shape
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (origin, ex, ey, ez, tx, rx, srp)]
+    need = np.zeros(1)
+    bad = _lib.load_host().sar_gather_window_check_host(*[a.ctypes.data for a in arrs[:4]], nx, ny, nz,
+                                                        tx.shape[0], *[a.ctypes.data for a in arrs[4:]], kappa,
+                                                        s_r, bin_offset, precise, ww, need.ctypes.data)
+    return bad, float(need[0])
+
+
+@pytest.mark.parametrize("name", ["benchmark", "turned", "diagonal"])
+@pytest.mark.parametrize("interp", ["linear", "nearest_ref"])
+def test_gather_window_flag_silent_on_headline_geometries(name, interp):
+    """The gather's producers raise SAR_FLAG_GATHER_WINDOW when a sub-tile's bin extent (a bound
+    over its 16x16 pixels) leaves the staged window.  On the 2048^2 x 4096-pulse headline geometry
+    in all three orientations it must stay silent with the window the plan picks (every 64th
+    pulse, every tile), or the headline would run flagged."""
+    az = {"benchmark": 0.0, "turned": 90.0, "diagonal": 45.0}[name]
+    tx = spotlight(4096, 5.0, centre_az_deg=az)[::64]
+    srp = np.zeros_like(tx)
+    scene = GridSarScene([1, 2048, 2048], [0.0, 0.25 * 2047, 0.25 * 2047])
+    s_r = 200.0e6 * 8 / C
+    kappa = 10.0e9 / C
+    ww = plan_tile_window(scene, spotlight(4096, 5.0, centre_az_deg=az), spotlight(4096, 5.0, centre_az_deg=az), s_r)
+    precise = 1 if interp == "nearest_ref" or ww > 256 else 0
+    bin_offset = -0.5 if interp == "linear" else 0.5
+    bad, need = window_check(scene, tx, tx, srp, kappa, s_r, bin_offset, precise, ww)
+    assert bad == 0, (bad, need, ww)
+    assert need <= 0.5 * ww
+
+
+def test_gather_window_flag_fires_on_an_undersized_window():
+    """The same check with a window 16 bins narrower than the plan's must report violations."""
+    tx = spotlight(4096, 5.0)[::256]
+    scene = GridSarScene([1, 512, 512], [0.0, 0.25 * 511, 0.25 * 511])
+    s_r = 200.0e6 * 8 / C
+    ww = plan_tile_window(scene, spotlight(4096, 5.0), spotlight(4096, 5.0), s_r)
+    bad_ok, need = window_check(scene, tx, tx, np.zeros_like(tx), 10.0e9 / C, s_r, -0.5, 0, ww)
+    bad, _ = window_check(scene, tx, tx, np.zeros_like(tx), 10.0e9 / C, s_r, -0.5, 0, ww - 16)
+    assert bad_ok == 0 and bad > 0 and need > 0.5 * (ww - 16)
+
+
+@pytest.mark.parametrize("precise", [0, 1])
+def test_bin_extent_bounds_every_pixel_bin(precise):
+    """bin_extent (sar_geom.cuh) must contain every bin the kernels' per-pixel evaluation forms
+    over the sub-tile, for sub-tiles at the grid corners and centre, several pulses, both bin
+    modes, and a bistatic short-range geometry where the quadratic and cubic terms matter."""
+    lib = _lib.load_host()
+    cases = [(spotlight(64, 5.0), None, 200.0e6 * 8 / C, GridSarScene([1, 2048, 2048], [0.0, 511.75, 511.75])),
+             (spotlight(16, 20.0, radius=2.0e3, altitude=1.0e3), spotlight(16, 35.0, radius=2.5e3, altitude=0.5e3),
+              200.0e6 * 128 / C, GridSarScene([1, 256, 256], [0.0, 63.75, 63.75]))]
+    for tx, rx, s_r, scene in cases:
+        rx = tx if rx is None else rx
+        shape, origin, ex, ey, ez = grid_axes(scene)
+        nz, ny, nx = shape
+        base = [np.ascontiguousarray(a, dtype=np.float64) for a in (origin, ex, ey, ez)]
+        tiles = [(0, 0), (nx // 32 - 1, ny // 32 - 1), (nx // 64, ny // 64), (0, ny // 32 - 1)]
+        out = np.zeros(4)
+        for s in range(0, tx.shape[0], 5):
+            t, r, o = (np.ascontiguousarray(a, dtype=np.float64) for a in (tx[s], rx[s], np.zeros(3)))
+            for ti, tj in tiles:
+                for q in range(4):
+                    assert lib.sar_bin_extent_host(*[a.ctypes.data for a in base], nx, ny, nz, t.ctypes.data,
+                                                   r.ctypes.data, o.ctypes.data, 10.0e9 / C, s_r, -0.5, precise,
+                                                   ti, tj, 0, q, out.ctypes.data) == 0
+                    lo, hi, vmin, vmax = out
+                    assert lo - 1e-3 <= vmin and vmax <= hi + 1e-3, (s, ti, tj, q, out)
+                    assert hi - lo < 1.2 * (vmax - vmin) + 4.0   # tight: the linear terms dominate

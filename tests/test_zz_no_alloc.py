@@ -4,7 +4,8 @@ It exists for callers that may not allocate device memory while they run (code i
 runtime's memory pool, real-time loops, hosts whose allocator belongs to another framework): all
 its scratch lives in one fixed device array inside the library.  This checks, through the C ABI,
 that two calls in a row reproduce the regular backprojection (sar_adjoint) from the profiles
-sar_profiles() writes, and that a problem too large for the fixed array is refused.
+sar_profiles() writes, with no device check flag raised (sar_noalloc_flags), and that a problem too
+large for the fixed array is refused.
 
 The file name sorts last so that a run stopping at the first failure has run every other test.
 """
@@ -71,6 +72,11 @@ def test_noalloc_backprojection_matches_plan_twice(interp):
         assert rc == 0, _lib.last_error()
         torch.cuda.synchronize()
         assert rel_l2(x.cpu().numpy(), ref) < TOL
+        # the call's device check flags (bounded waits, window bounds), read without allocating
+        flags = ctypes.c_uint(0xFFFFFFFF)
+        rc = lib.sar_noalloc_flags(ctypes.byref(flags), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        assert rc == 0, _lib.last_error()
+        assert flags.value == 0
 
 
 def test_noalloc_rejects_problems_beyond_its_array():
