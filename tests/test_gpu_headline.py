@@ -49,9 +49,9 @@ def test_headline_against_fp64_oracle(case, interp):
     n = scene.grid_shape[2]
     S, N = aperture.num_slow_times, aperture.num_freqs
     plan = SarPlan(scene, aperture, upsample_ratio=upsample, interp=interp)
-    assert plan.is_grid and plan.fused_upsampling and plan.fused_downsampling
-    if case == "config2":
-        assert plan.tile_window == 96
+    assert plan.is_grid
+    if case == "config2":   # the benchmark path: fused up/downsampling, 96-bin look-direction windows
+        assert plan.fused_upsampling and plan.fused_downsampling and plan.tile_window == 96
     x = reflectivity(n, 500, 8.0, SEED)
     y_clean = plan.forward(x)
     y = add_noise(y_clean, 20.0, SEED + 1)
