@@ -25,6 +25,15 @@ Fixtures written:
   bistatic_odd.npz   -- bistatic, odd N = 63, complex weights, a waveform, sign -1,
                         rotated 2-plane grid off the SRP, upsample 8.
   points.npz         -- unstructured scatterer positions (SimpleSarScene), upsample 4.
+  little_pdhg.npz    -- the reference's PDHG artifact tests/artifacts/little_soln.npy (CIL PDHG with
+                        f = L2NormSquared(b = little_noisy_meas), g = ZeroFunction, from zero, the
+                        operator norm pinned to 756.6231381576064 by tests/conftest.py:93-96, then
+                        run(3), tests/test_cil.py:25-37), with that norm.  Checked on generation:
+                        two PDHG updates in CIL's order (sigma = tau = 1 / norm, theta = 1) on the
+                        oracle's nearest-bin operator (bit-identical to the reference kernel)
+                        reproduce it to 1e-12; three updates are 4.6 % away, so that run(3) applied
+                        two updates (its run loop counts the set-up step as iteration 0).
+                        ``--only little_pdhg`` writes just this file.
 """
 from __future__ import annotations
 
@@ -98,11 +107,45 @@ def run_case(sn, scene, ap, x, y, upsample, threads):
     return fwd, adj
 
 
+def little_pdhg(ref_root: str):
+    """little_pdhg.npz from the reference's artifact, checked against two oracle PDHG updates."""
+    sys.path.insert(0, REPO)
+    sys.path.insert(0, os.path.dirname(HERE))
+    import oracle
+    from cases import load_golden
+
+    arts = os.path.join(ref_root, "tests", "artifacts")
+    soln = np.load(os.path.join(arts, "little_soln.npy"))
+    norm = 756.6231381576064                      # tests/conftest.py:95
+    case = load_golden("little")
+    prob, b = case.problem(), case.data["y"]
+    th = oracle.default_threads()
+    fwd = lambda v: oracle.forward(prob, v, "nearest_ref", threads=th)
+    adj = lambda v: oracle.adjoint(prob, v, "nearest_ref", threads=th)
+    sigma = tau = 1.0 / norm
+    x_prev = x = np.zeros(prob.num_scatterers, np.complex128)
+    yd = np.zeros_like(b)
+    errs = []
+    for _ in range(3):
+        xbar = 2.0 * x - x_prev
+        yd = (yd + sigma * fwd(xbar) - sigma * b) / (1.0 + sigma / 2.0)
+        x_prev, x = x, x - tau * adj(yd)
+        errs.append(np.linalg.norm(x - soln.reshape(-1)) / np.linalg.norm(soln))
+    print("little_pdhg: rel L2 of 1, 2, 3 updates vs little_soln.npy:", ", ".join(f"{e:.3e}" for e in errs))
+    assert errs[1] < 1e-12, errs
+    np.savez(os.path.join(HERE, "little_pdhg.npz"), soln=soln.reshape(-1), operator_norm=np.float64(norm),
+             updates=np.int64(2))
+
+
 def main():
     ap_ = argparse.ArgumentParser()
     ap_.add_argument("--reference", default="/root/reference")
     ap_.add_argument("--threads", type=int, default=4)
+    ap_.add_argument("--only", choices=["little_pdhg"], default=None)
     args = ap_.parse_args()
+    little_pdhg(args.reference)
+    if args.only:
+        return
     work = tempfile.mkdtemp(prefix="sar_golden_")
     try:
         sn = import_reference(args.reference, work)

@@ -84,3 +84,19 @@ def test_cgls_three_iterations(cil):
         gam = g
     assert rel_l2(solver.x.array.reshape(-1), x) < 1e-4
     assert solver.residuals[-1] < solver.residuals[0]
+
+
+def test_pdhg_meets_reference_artifact(cil):
+    """The reference's test_pdhg (tests/test_cil.py:25-37) on the GPU operator: CIL's PDHG interface
+    (the fake's; it applies two updates for run(3), as the CIL release that made the artifact did),
+    f = L2NormSquared(b), g = ZeroFunction, the norm pinned as in tests/conftest.py:93-96."""
+    import os
+    from cases import GOLDEN
+    case, op, meas = little_operator(cil)
+    op._norm = 756.6231381576064
+    solver = fake_cil.PDHG(initial=op.domain.allocate(), operator=op, f=fake_cil.L2NormSquared(b=meas),
+                           g=fake_cil.ZeroFunction())
+    solver.run(3)
+    soln = np.load(os.path.join(GOLDEN, "little_pdhg.npz"))["soln"].reshape(solver.x.array.shape)
+    assert solver.x.array == pytest.approx(soln, rel=1.0e-3)
+

@@ -156,3 +156,27 @@ def test_pdhg_argument_errors(problem):
     x0 = torch.ones(plan.num_scatterers, dtype=torch.complex64, device="cuda")
     x1, info = pdhg(plan, b, iterations=0, x0=x0, sigma=0.1, tau=0.1)
     assert info.iterations == 0 and torch.equal(x1, x0)
+
+
+def test_pdhg_reproduces_the_reference_artifact():
+    """The reference's only solver artifact (tests/artifacts/little_soln.npy: CIL PDHG, f =
+    ||K x - b||^2, g = 0, norm pinned to 756.6231381576064, run(3) = two updates) from sar_pdhg on
+    the little case with the reference's operator settings (nearest_ref, upsample 128), held to the
+    reference test's own elementwise criterion (rel 1e-3, tests/test_cil.py:37) and 1e-5 in L2."""
+    import os
+    from cases import GOLDEN, load_golden
+    from sarsolver_gb300 import SarPlan
+    from sarsolver_gb300.solvers import pdhg
+
+    g = dict(np.load(os.path.join(GOLDEN, "little_pdhg.npz")))
+    case = load_golden("little")
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp="nearest_ref")
+    step = 1.0 / float(g["operator_norm"])
+    x, info = pdhg(plan, torch.from_numpy(case.data["y"]), iterations=int(g["updates"]), sigma=step, tau=step)
+    got = x.cpu().numpy().astype(np.complex128)
+    rel = np.linalg.norm(got - g["soln"]) / np.linalg.norm(g["soln"])
+    print(f"little PDHG (2 updates) vs little_soln.npy: rel L2 {rel:.2e}")
+    assert rel < 1e-5
+    assert got == pytest.approx(g["soln"], rel=1.0e-3)
+    assert plan.device_flags() == 0
+
