@@ -128,10 +128,22 @@ typedef struct sar_plan_info {
                                    kernel (N = 1024, 2048 or 4096, M a multiple of N), 0: cuFFT */
     int scatter_lanes_y;        /* 1: the grid forward scatter runs warp lanes along y and walks the
                                    tile along x (bins change more slowly along x), 0: lanes along x */
+    size_t block_pulses;        /* streamed plan: pulses per block (0: resident plan) */
 } sar_plan_info;
 
 /* Create a plan on `device` (-1: the current device).  Copies all host inputs. */
 int sar_plan_create(const sar_geometry *geom, int device, sar_plan **plan_out);
+
+/* A plan whose device memory is bounded by a block of pulses instead of the whole aperture:
+ * its range-profile buffer holds two blocks of block_pulses pulses ([2][block][profile_length]
+ * pairs; a resident plan holds [S][profile_length]) and its FFT rows at most one block.  sar_adjoint
+ * and sar_forward then run block by block (upsample a block into a ring slot, gather it onto the
+ * image; clear a block's accumulator, scatter, downsample), and sar_adjoint_pulse_block takes blocks
+ * of at most block_pulses pulses -- so a phase history streamed from the host in blocks never needs
+ * device memory for all S pulses.  Replaces the reference's slow-time blocking, whose purpose is
+ * bounding memory (num_calculation_blocks, cxx_binding/forward.py:66-96, adjoint.py:66-94).
+ * Regular-grid plans only.  block_pulses >= S gives a resident plan. */
+int sar_plan_create_streamed(const sar_geometry *geom, int device, size_t block_pulses, sar_plan **plan_out);
 int sar_plan_destroy(sar_plan *plan);
 int sar_plan_get_info(const sar_plan *plan, sar_plan_info *info);
 
@@ -142,8 +154,9 @@ int sar_adjoint(sar_plan *plan, const void *y_dev, void *x_dev, void *stream);
 /* Backprojection of one block of pulses, for streaming a phase history through the device:
  * y_block_dev holds rows first_pulse .. first_pulse + count - 1 (complex64 [count][N], fftshifted
  * like y); x_dev = (accumulate ? x_dev : 0) + contribution of those pulses.  Summing the blocks of a
- * partition of [0, S) in order reproduces sar_adjoint (up to FP32 summation order).  Regular-grid
- * plans only.  Replaces the reference's slow-time blocking (num_calculation_blocks,
+ * partition of [0, S) in order reproduces sar_adjoint (up to FP32 summation order); accumulating
+ * calls run one CTA per image tile, so a given partition gives the same bits on every run.
+ * Regular-grid plans only (count <= block_pulses for a streamed plan).  Replaces the reference's slow-time blocking (num_calculation_blocks,
  * cxx_binding/adjoint.py:66-94) with device-side accumulation. */
 int sar_adjoint_pulse_block(sar_plan *plan, const void *y_block_dev, size_t first_pulse, size_t count,
                             void *x_dev, int accumulate, void *stream);

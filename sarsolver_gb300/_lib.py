@@ -34,7 +34,7 @@ EXPORTED = (
     "sar_unet_create", "sar_unet_destroy", "sar_unet_info", "sar_unet_set_params", "sar_unet_get_params",
     "sar_unet_get_grads", "sar_unet_zero_grad", "sar_unet_forward", "sar_unet_backward", "sar_unet_adam_step",
     "sar_unet_flags", "sar_conv2d_forward_bf16", "sar_conv2d_wgrad_bf16",
-    "sar_noalloc_flags", "sar_plan_set_wait_budget", "sar_measure_pipe_rates",
+    "sar_noalloc_flags", "sar_plan_set_wait_budget", "sar_measure_pipe_rates", "sar_plan_create_streamed",
 )
 
 SAR_FLAG_TILE_WINDOW, SAR_FLAG_STRIP_WINDOW, SAR_FLAG_WAIT_TIMEOUT, SAR_FLAG_GATHER_WINDOW = 1, 2, 8, 16
@@ -95,7 +95,7 @@ class SarPlanInfo(ctypes.Structure):
         ("tile_window", c_size_t), ("strip_window", c_size_t), ("device_bytes", c_size_t), ("grid", c_int),
         ("interp", c_int), ("num_fast_times", c_size_t), ("num_slow_times", c_size_t), ("num_scatterers", c_size_t),
         ("device", c_int), ("fft_callbacks", c_int), ("gather_lanes_y", c_int), ("fused_upsampling", c_int), ("fused_downsampling", c_int),
-        ("scatter_lanes_y", c_int),
+        ("scatter_lanes_y", c_int), ("block_pulses", c_size_t),
     ]
 
 
@@ -128,6 +128,8 @@ def load() -> ctypes.CDLL:
         raise RuntimeError(f"libsargpu.so is not built ({GPU_LIB}); run sarsolver_gb300.build.build()")
     lib = ctypes.CDLL(GPU_LIB)
     lib.sar_plan_create.argtypes = [POINTER(SarGeometry), c_int, POINTER(c_void_p)]
+    lib.sar_plan_create_streamed.argtypes = [POINTER(SarGeometry), c_int, c_size_t, POINTER(c_void_p)]
+    lib.sar_plan_create_streamed.restype = c_int
     lib.sar_plan_destroy.argtypes = [c_void_p]
     lib.sar_plan_get_info.argtypes = [c_void_p, POINTER(SarPlanInfo)]
     for name in ("sar_forward", "sar_adjoint", "sar_profiles"):

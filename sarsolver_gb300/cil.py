@@ -5,8 +5,9 @@ Mirrors src/sarsolver/cil/operator.py:11-111 (``CpuSarOperator``), cil/base.py:1
 (``CilSarGridGeometry``) and cil/measurement.py:9-71 (``SimpleCilSarGeometry``): same names,
 constructor arguments, shapes (image ``grid_shape`` (z, y, x), measurement ``[S, N]``), complex128
 containers, and ``direct`` / ``adjoint`` that replace ``out.array`` wholesale.  The products run on
-the GPU through one ``SarPlan`` built on first use; ``num_threads`` and ``num_calculation_blocks``
-are accepted and ignored.
+the GPU through one ``SarPlan`` built on first use; ``num_threads`` is accepted and ignored, and
+``num_calculation_blocks`` > 1 makes that plan a streamed one (device memory bounded by two blocks
+of ceil(S / num_calculation_blocks) pulses).
 
 When CCPi CIL is installed its ``DataContainer``, ``LinearOperator`` and ``FillType`` are used, so
 CIL's solvers (CGLS, PDHG, ...) run on this operator unchanged.  Without CIL a minimal stand-in of
@@ -30,7 +31,7 @@ except Exception:   # pragma: no cover - depends on the environment
     from ._cil_fallback import DataContainer, FillType, LinearOperator
     HAVE_CIL = False
 
-from .plan import SarPlan
+from .plan import SarPlan, block_pulses_for
 
 
 class GenericCilGeometry:
@@ -162,8 +163,11 @@ class GpuCilSarOperator(LinearOperator):
     @property
     def plan(self) -> SarPlan:
         if self._plan is None:
-            self._plan = SarPlan(self._domain_geometry.scene, self._range_geometry.aperture,
-                                 upsample_ratio=self._upsample_ratio, interp=self._interp, device=self._device)
+            scene, aperture = self._domain_geometry.scene, self._range_geometry.aperture
+            self._plan = SarPlan(scene, aperture, upsample_ratio=self._upsample_ratio, interp=self._interp,
+                                 device=self._device,
+                                 block_pulses=block_pulses_for(scene, aperture.num_slow_times,
+                                                               self._num_calculation_blocks))
         return self._plan
 
     @property

@@ -128,6 +128,7 @@ struct sar_plan {
     float4* d_prof = nullptr;   // [S][Lg] pairs (adjoint) / float2 accumulator (forward)
     int* d_strip = nullptr;
     unsigned* d_flags = nullptr;
+    size_t block = 0;   // streamed plan: profile buffer of two blocks of this many pulses (0: all S)
     long long wait_budget = kDefaultWaitBudgetCycles;   // bounded in-kernel waits of the gather
     int hold_first_stage = 0;                           // test aid (sar_plan_set_wait_budget)
     size_t device_bytes = 0;
@@ -653,12 +654,16 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
     if ((rc = upload_weights(p, nullptr, true))) return rc;
     if ((rc = p->alloc(&p->d_flags, 1, "flags"))) return rc;
     SAR_CUDA(cudaMemset(p->d_flags, 0, sizeof(unsigned)), "flags");
-    if ((rc = p->alloc(&p->d_prof, (size_t)S * p->Lg, "range profiles"))) return rc;
+    if (p->block && (!grid || p->forward_points))
+        return fail(SAR_ERR_NOT_SUPPORTED, "streamed plans need the regular-grid kernels (forward and backprojection)");
+    // resident: profiles of all S pulses; streamed: a ring of two blocks (the forward's accumulator
+    // of one block, [block][Lg] float2, fits in half of one slot)
+    if ((rc = p->alloc(&p->d_prof, (size_t)(p->block ? 2 * p->block : S) * p->Lg, "range profiles"))) return rc;
 
     // ---- FFT work rows
     p->fft_double = !smooth_length(M);
     const size_t elem = p->fft_double ? sizeof(double2) : sizeof(float2);
-    p->chunk = (int)std::min<size_t>(S, std::max<size_t>(1, kSpecBudget / (M * elem)));
+    p->chunk = (int)std::min<size_t>(p->block ? p->block : S, std::max<size_t>(1, kSpecBudget / (M * elem)));
     {
         double2* spec = nullptr;
         if ((rc = p->alloc(&spec, ((size_t)p->chunk * M * elem + sizeof(double2) - 1) / sizeof(double2), "FFT rows")))
@@ -698,7 +703,7 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
     // the default; when forced on, a plan that cannot link the callbacks reports why.
     {
         const char* env = getenv("SAR_FFT_CALLBACKS");
-        const bool want = !p->fft_double && env && env[0] == '1';
+        const bool want = !p->fft_double && !p->block && env && env[0] == '1';
         if (want) {
             p->Lc = (int)std::min<size_t>((size_t)p->Lg + 1, M);
             cufftHandle h = 0;
@@ -757,7 +762,18 @@ int sar_host_device_pointer(const void* host_ptr, void** dev_ptr) {
     return SAR_OK;
 }
 
+static int plan_create(const sar_geometry* geom, int device, size_t block_pulses, sar_plan** plan_out);
+
 int sar_plan_create(const sar_geometry* geom, int device, sar_plan** plan_out) {
+    return plan_create(geom, device, 0, plan_out);
+}
+
+int sar_plan_create_streamed(const sar_geometry* geom, int device, size_t block_pulses, sar_plan** plan_out) {
+    if (!block_pulses) return fail(SAR_ERR_INVALID_ARGUMENT, "block_pulses must be positive");
+    return plan_create(geom, device, block_pulses, plan_out);
+}
+
+static int plan_create(const sar_geometry* geom, int device, size_t block_pulses, sar_plan** plan_out) {
     g_last_error.clear();
     if (!geom || !plan_out) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
     *plan_out = nullptr;
@@ -770,6 +786,7 @@ int sar_plan_create(const sar_geometry* geom, int device, sar_plan** plan_out) {
     sar_plan* p = new (std::nothrow) sar_plan();
     if (!p) return fail(SAR_ERR_OUT_OF_MEMORY, "host allocation");
     p->device = dev;
+    p->block = block_pulses < geom->num_slow_times ? block_pulses : 0;
     const int rc = build_plan(geom, p);
     if (rc != SAR_OK) {
         delete p;
@@ -803,17 +820,21 @@ int sar_plan_get_info(const sar_plan* p, sar_plan_info* info) {
     info->fused_upsampling = p->fused_up ? 1 : 0;
     info->fused_downsampling = p->fused_down ? 1 : 0;
     info->scatter_lanes_y = (p->grid && !p->forward_points && !p->lanes_y) ? 1 : 0;
+    info->block_pulses = p->block;
     return SAR_OK;
 }
 
-// Upsampled profiles of pulses [begin, end): y row s is read at y + s * N.
+// Upsampled profiles of pulses [begin, end): y row s is read at y + s * N; with pairs_out the
+// (value, difference) pairs of pulse s go to pairs_rows + s * Lg (the plan's buffer for a resident
+// plan; a ring slot, addressed from the block's first pulse, for a streamed one).
 static int upsample_rows(sar_plan* p, const float2* y, size_t begin, size_t end, cudaStream_t st, bool pairs_out,
-                         float2* prof) {
+                         float2* prof, float4* pairs_rows = nullptr) {
+    if (!pairs_rows) pairs_rows = p->d_prof;
     for (size_t first = begin; first < end; first += (size_t)p->chunk) {
         const int rows = (int)std::min<size_t>(p->chunk, end - first);
         const int dbl = p->fft_double;
         if (pairs_out && p->fused_up) {
-            SAR_CUDA(launch_upsample_pairs_fused(y, p->d_wave, p->d_wadj, p->d_tw_n, p->d_tw_m, p->d_prof, (int)p->N,
+            SAR_CUDA(launch_upsample_pairs_fused(y, p->d_wave, p->d_wadj, p->d_tw_n, p->d_tw_m, pairs_rows, (int)p->N,
                                                  (long)p->M, p->Lg, p->bg0, rows, (int)first,
                                                  p->interp == SAR_INTERP_LINEAR, st),
                      "fused upsampling");
@@ -838,7 +859,7 @@ static int upsample_rows(sar_plan* p, const float2* y, size_t begin, size_t end,
         int rc = run_fft(p, p->d_spec, rows, CUFFT_INVERSE, st);
         if (rc) return rc;
         if (pairs_out)
-            SAR_CUDA(launch_unpack_pairs(p->d_spec, dbl, p->d_wadj, p->d_prof, (long)p->M, p->Lg, p->bg0, rows,
+            SAR_CUDA(launch_unpack_pairs(p->d_spec, dbl, p->d_wadj, pairs_rows, (long)p->M, p->Lg, p->bg0, rows,
                                          (int)first, p->interp == SAR_INTERP_LINEAR, st),
                      "unpack");
         else
@@ -869,140 +890,14 @@ static PointArgs point_args(sar_plan* p, int bin_rule) {
     return a;
 }
 
-int sar_adjoint(sar_plan* p, const void* y_dev, void* x_dev, void* stream) {
-    if (!p || !y_dev || !x_dev) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
-    std::lock_guard<std::mutex> lock(p->mu);
-    DeviceGuard guard(p->device);
-    if (guard.status != cudaSuccess) return cuda_fail(guard.status, "select device");
-    cudaStream_t st = (cudaStream_t)stream;
-    p->last_stream = st;
-    cudaEvent_t* ev = p->timing_slot();
-    mark(ev, 0, st);
-    int rc = upsample_into_pairs(p, (const float2*)y_dev, st, true, nullptr);
-    if (rc) return rc;
-    mark(ev, 1, st);
-    if (p->grid) {
-        BpGridArgs a;
-        a.g = p->gc_adj;
-        a.pulses = p->d_pulses;
-        a.pairs = p->d_prof;
-        a.x = (float2*)x_dev;
-        a.flags = p->d_flags;
-        a.S = (int)p->S;
-        a.Lg = p->Lg;
-        a.bg0 = (int)p->bg0;
-        a.wwin = p->wwin;
-        a.pb = p->pb;
-        a.staged = p->staged;
-        a.accumulate = 0;
-        a.lanes_y = p->lanes_y;
-        a.nearest = p->interp == SAR_INTERP_NEAREST_REF;
-        a.steps = p->d_steps;
-        a.alpha2 = p->d_alpha2;
-        a.wait_budget = p->wait_budget;
-        a.hold_first_stage = p->hold_first_stage;
-        SAR_CUDA(p->staged ? launch_bp_grid_ws(a, st) : launch_bp_grid(a, st), "backprojection");
-    } else {
-        SAR_CUDA(launch_bp_points(point_args(p, p->interp == SAR_INTERP_LINEAR ? BIN_LINEAR : BIN_ADJ_NEAREST), p->d_prof, (float2*)x_dev, 0, st),
-                 "backprojection");
-    }
-    mark(ev, 2, st);
-    mark(ev, 3, st);
-    return SAR_OK;
-}
-
-int sar_forward(sar_plan* p, const void* x_dev, void* y_dev, void* stream) {
-    if (!p || !y_dev || !x_dev) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
-    std::lock_guard<std::mutex> lock(p->mu);
-    DeviceGuard guard(p->device);
-    if (guard.status != cudaSuccess) return cuda_fail(guard.status, "select device");
-    cudaStream_t st = (cudaStream_t)stream;
-    p->last_stream = st;
-    float2* acc = reinterpret_cast<float2*>(p->d_prof);
-    cudaEvent_t* ev = p->timing_slot();
-    mark(ev, 0, st);
-    SAR_CUDA(cudaMemsetAsync(acc, 0, sizeof(float2) * p->S * (size_t)p->Lg, st), "zero accumulator");
-    mark(ev, 1, st);
-    if (p->grid && !p->forward_points) {
-        FpGridArgs a;
-        a.g = p->gc_fwd;
-        a.pulses = p->d_pulses;
-        a.x = (const float2*)x_dev;
-        a.acc = acc;
-        a.strip_start = p->d_strip;
-        a.flags = p->d_flags;
-        a.S = (int)p->S;
-        a.Lg = p->Lg;
-        a.bg0 = (int)p->bg0;
-        a.seg_tiles = p->seg_tiles;
-        a.segs_per_column = p->segs_per_column;
-        a.ws = p->ws;
-        a.pbf = p->pbf;
-        a.linear = p->interp == SAR_INTERP_LINEAR;
-        // the scatter walks the axis along which bins change slowly: the transpose of the gather's
-        // lane choice
-        a.transposed = p->lanes_y ? 0 : 1;
-        a.steps = p->d_steps;
-        a.alpha2 = p->d_alpha2;
-        SAR_CUDA(launch_fp_grid_ws(a, st), "forward scatter");
-    } else {
-        SAR_CUDA(launch_fp_points(point_args(p, p->interp == SAR_INTERP_LINEAR ? BIN_LINEAR : BIN_FWD_NEAREST), (const float2*)x_dev, acc, st),
-                 "forward scatter");
-    }
-    mark(ev, 2, st);
-    for (size_t first = 0; first < p->S; first += (size_t)p->chunk) {
-        const int rows = (int)std::min<size_t>(p->chunk, p->S - first);
-        if (p->fused_down) {
-            SAR_CUDA(launch_downsample_forward_fused(acc, p->d_wave, p->d_wfwd, p->d_tw_n, p->d_tw_m, (float2*)y_dev,
-                                                     (int)p->N, (long)p->M, p->Lg, p->bg0, rows, (int)first, st),
-                     "fused downsampling");
-            continue;
-        }
-        if (p->fft_cb) {
-            cufftHandle h = 0;
-            int rc = cb_plan(p, rows, false, &h);
-            if (rc) return rc;
-            if ((rc = set_cb_info(p, nullptr, (float2*)y_dev, (int)first, st))) return rc;
-            SAR_CUFFT(cufftSetStream(h, st), "cufftSetStream");
-            SAR_CUFFT(cufftExecC2C(h, reinterpret_cast<cufftComplex*>(p->d_spec), reinterpret_cast<cufftComplex*>(p->d_spec),
-                                   CUFFT_FORWARD),
-                      "cufftExecC2C (callbacks)");
-            continue;
-        }
-        SAR_CUDA(launch_pack_forward(acc, p->d_spec, p->fft_double, (long)p->M, p->Lg, p->bg0, rows, (int)first, st),
-                 "pack");
-        int rc = run_fft(p, p->d_spec, rows, CUFFT_FORWARD, st);
-        if (rc) return rc;
-        SAR_CUDA(launch_extract_forward(p->d_spec, p->fft_double, p->d_wave, p->d_wfwd, (float2*)y_dev, (int)p->N,
-                                        (long)p->M, rows, (int)first, st),
-                 "extract");
-    }
-    mark(ev, 3, st);
-    return SAR_OK;
-}
-
-int sar_adjoint_pulse_block(sar_plan* p, const void* y_block_dev, size_t first_pulse, size_t count, void* x_dev,
-                            int accumulate, void* stream) {
-    if (!p || !y_block_dev || !x_dev) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
-    if (!count || first_pulse >= p->S || count > p->S - first_pulse)
-        return fail(SAR_ERR_INVALID_ARGUMENT, "pulse block [%zu, %zu) outside [0, %zu)", first_pulse,
-                    first_pulse + count, p->S);
-    if (!p->grid) return fail(SAR_ERR_NOT_SUPPORTED, "pulse blocks need a regular-grid plan");
-    std::lock_guard<std::mutex> lock(p->mu);
-    DeviceGuard guard(p->device);
-    if (guard.status != cudaSuccess) return cuda_fail(guard.status, "select device");
-    cudaStream_t st = (cudaStream_t)stream;
-    p->last_stream = st;
-    // The block holds rows first_pulse .. first_pulse + count - 1; the pack kernel addresses row s
-    // at y + s * N, so the base is moved back by first_pulse rows (only rows of the block are read).
-    const float2* y = reinterpret_cast<const float2*>(y_block_dev) - first_pulse * p->N;
-    int rc = upsample_rows(p, y, first_pulse, first_pulse + count, st, true, nullptr);
-    if (rc) return rc;
+// Grid gather of pulses [first, first + count) from pairs rows `pairs` (row 0 = pulse `first`).
+static int gather_pulses(sar_plan* p, const float4* pairs, size_t first, size_t count, float2* x, int accumulate,
+                         cudaStream_t st) {
     BpGridArgs a;
     a.g = p->gc_adj;
-    a.pulses = p->d_pulses + first_pulse;
-    a.pairs = p->d_prof + first_pulse * (size_t)p->Lg;
-    a.x = (float2*)x_dev;
+    a.pulses = p->d_pulses + first;
+    a.pairs = pairs;
+    a.x = x;
     a.flags = p->d_flags;
     a.S = (int)count;
     a.Lg = p->Lg;
@@ -1014,11 +909,186 @@ int sar_adjoint_pulse_block(sar_plan* p, const void* y_block_dev, size_t first_p
     a.lanes_y = p->lanes_y;
     a.nearest = p->interp == SAR_INTERP_NEAREST_REF;
     a.steps = p->d_steps;
-    a.alpha2 = p->d_alpha2;
+    a.alpha2 = p->d_alpha2 ? p->d_alpha2 + first : nullptr;   // indexed by block-relative pulse
     a.wait_budget = p->wait_budget;
     a.hold_first_stage = p->hold_first_stage;
     SAR_CUDA(p->staged ? launch_bp_grid_ws(a, st) : launch_bp_grid(a, st), "backprojection");
     return SAR_OK;
+}
+
+// Ring slot of a streamed plan for the block starting at pulse `first`.
+static float4* ring_slot(sar_plan* p, size_t first) {
+    return p->d_prof + ((first / p->block) & 1) * p->block * (size_t)p->Lg;
+}
+
+int sar_adjoint(sar_plan* p, const void* y_dev, void* x_dev, void* stream) {
+    if (!p || !y_dev || !x_dev) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(p->mu);
+    DeviceGuard guard(p->device);
+    if (guard.status != cudaSuccess) return cuda_fail(guard.status, "select device");
+    cudaStream_t st = (cudaStream_t)stream;
+    p->last_stream = st;
+    cudaEvent_t* ev = p->timing_slot();
+    if (p->block) {
+        // streamed plan: per block of pulses, upsample into a ring slot and gather, adding the
+        // blocks after the first onto the image (stage times: upsampling in [0], gathers in [1])
+        mark(ev, 0, st);
+        mark(ev, 1, st);
+        for (size_t first = 0; first < p->S; first += p->block) {
+            const size_t count = std::min(p->block, p->S - first);
+            float4* slot = ring_slot(p, first);
+            int rc = upsample_rows(p, (const float2*)y_dev, first, first + count, st, true, nullptr,
+                                   slot - first * (size_t)p->Lg);
+            if (rc) return rc;
+            if ((rc = gather_pulses(p, slot, first, count, (float2*)x_dev, first > 0, st))) return rc;
+        }
+        mark(ev, 2, st);
+        mark(ev, 3, st);
+        return SAR_OK;
+    }
+    mark(ev, 0, st);
+    int rc = upsample_into_pairs(p, (const float2*)y_dev, st, true, nullptr);
+    if (rc) return rc;
+    mark(ev, 1, st);
+    if (p->grid) {
+        if ((rc = gather_pulses(p, p->d_prof, 0, p->S, (float2*)x_dev, 0, st))) return rc;
+    } else {
+        SAR_CUDA(launch_bp_points(point_args(p, p->interp == SAR_INTERP_LINEAR ? BIN_LINEAR : BIN_ADJ_NEAREST), p->d_prof, (float2*)x_dev, 0, st),
+                 "backprojection");
+    }
+    mark(ev, 2, st);
+    mark(ev, 3, st);
+    return SAR_OK;
+}
+
+// Grid scatter of pulses [first, first + count) into accumulator rows `acc` (row 0 = pulse `first`).
+static int scatter_pulses(sar_plan* p, const float2* x, float2* acc, size_t first, size_t count, cudaStream_t st) {
+    FpGridArgs a;
+    a.g = p->gc_fwd;
+    a.pulses = p->d_pulses + first;
+    a.x = x;
+    a.acc = acc;
+    a.strip_start = p->d_strip + first;
+    a.strip_stride = (int)p->S;
+    a.flags = p->d_flags;
+    a.S = (int)count;
+    a.Lg = p->Lg;
+    a.bg0 = (int)p->bg0;
+    a.seg_tiles = p->seg_tiles;
+    a.segs_per_column = p->segs_per_column;
+    a.ws = p->ws;
+    a.pbf = p->pbf;
+    a.linear = p->interp == SAR_INTERP_LINEAR;
+    // the scatter walks the axis along which bins change slowly: the transpose of the gather's
+    // lane choice
+    a.transposed = p->lanes_y ? 0 : 1;
+    a.steps = p->d_steps;
+    a.alpha2 = p->d_alpha2 ? p->d_alpha2 + first : nullptr;
+    SAR_CUDA(launch_fp_grid_ws(a, st), "forward scatter");
+    return SAR_OK;
+}
+
+// FFT side of the forward projection for pulses [begin, end): accumulator row of pulse s at
+// acc_rows + s * Lg, output rows of y.
+static int downsample_rows(sar_plan* p, const float2* acc_rows, float2* y, size_t begin, size_t end,
+                           cudaStream_t st) {
+    for (size_t first = begin; first < end; first += (size_t)p->chunk) {
+        const int rows = (int)std::min<size_t>(p->chunk, end - first);
+        if (p->fused_down) {
+            SAR_CUDA(launch_downsample_forward_fused(acc_rows, p->d_wave, p->d_wfwd, p->d_tw_n, p->d_tw_m, y,
+                                                     (int)p->N, (long)p->M, p->Lg, p->bg0, rows, (int)first, st),
+                     "fused downsampling");
+            continue;
+        }
+        if (p->fft_cb) {
+            cufftHandle h = 0;
+            int rc = cb_plan(p, rows, false, &h);
+            if (rc) return rc;
+            if ((rc = set_cb_info(p, nullptr, y, (int)first, st))) return rc;
+            SAR_CUFFT(cufftSetStream(h, st), "cufftSetStream");
+            SAR_CUFFT(cufftExecC2C(h, reinterpret_cast<cufftComplex*>(p->d_spec), reinterpret_cast<cufftComplex*>(p->d_spec),
+                                   CUFFT_FORWARD),
+                      "cufftExecC2C (callbacks)");
+            continue;
+        }
+        SAR_CUDA(launch_pack_forward(acc_rows, p->d_spec, p->fft_double, (long)p->M, p->Lg, p->bg0, rows, (int)first,
+                                     st),
+                 "pack");
+        int rc = run_fft(p, p->d_spec, rows, CUFFT_FORWARD, st);
+        if (rc) return rc;
+        SAR_CUDA(launch_extract_forward(p->d_spec, p->fft_double, p->d_wave, p->d_wfwd, y, (int)p->N, (long)p->M, rows,
+                                        (int)first, st),
+                 "extract");
+    }
+    return SAR_OK;
+}
+
+int sar_forward(sar_plan* p, const void* x_dev, void* y_dev, void* stream) {
+    if (!p || !y_dev || !x_dev) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    std::lock_guard<std::mutex> lock(p->mu);
+    DeviceGuard guard(p->device);
+    if (guard.status != cudaSuccess) return cuda_fail(guard.status, "select device");
+    cudaStream_t st = (cudaStream_t)stream;
+    p->last_stream = st;
+    cudaEvent_t* ev = p->timing_slot();
+    if (p->block) {
+        // streamed plan: per block, clear its accumulator (half of a ring slot), scatter the block's
+        // pulses, downsample its rows (stage times: the whole loop in [1])
+        mark(ev, 0, st);
+        mark(ev, 1, st);
+        for (size_t first = 0; first < p->S; first += p->block) {
+            const size_t count = std::min(p->block, p->S - first);
+            float2* acc = reinterpret_cast<float2*>(ring_slot(p, first));
+            SAR_CUDA(cudaMemsetAsync(acc, 0, sizeof(float2) * count * (size_t)p->Lg, st), "zero accumulator");
+            int rc = scatter_pulses(p, (const float2*)x_dev, acc, first, count, st);
+            if (!rc) rc = downsample_rows(p, acc - first * (size_t)p->Lg, (float2*)y_dev, first, first + count, st);
+            if (rc) return rc;
+        }
+        mark(ev, 2, st);
+        mark(ev, 3, st);
+        return SAR_OK;
+    }
+    float2* acc = reinterpret_cast<float2*>(p->d_prof);
+    mark(ev, 0, st);
+    SAR_CUDA(cudaMemsetAsync(acc, 0, sizeof(float2) * p->S * (size_t)p->Lg, st), "zero accumulator");
+    mark(ev, 1, st);
+    if (p->grid && !p->forward_points) {
+        int rc = scatter_pulses(p, (const float2*)x_dev, acc, 0, p->S, st);
+        if (rc) return rc;
+    } else {
+        SAR_CUDA(launch_fp_points(point_args(p, p->interp == SAR_INTERP_LINEAR ? BIN_LINEAR : BIN_FWD_NEAREST), (const float2*)x_dev, acc, st),
+                 "forward scatter");
+    }
+    mark(ev, 2, st);
+    int rc = downsample_rows(p, acc, (float2*)y_dev, 0, p->S, st);
+    if (rc) return rc;
+    mark(ev, 3, st);
+    return SAR_OK;
+}
+
+int sar_adjoint_pulse_block(sar_plan* p, const void* y_block_dev, size_t first_pulse, size_t count, void* x_dev,
+                            int accumulate, void* stream) {
+    if (!p || !y_block_dev || !x_dev) return fail(SAR_ERR_INVALID_ARGUMENT, "null argument");
+    if (!count || first_pulse >= p->S || count > p->S - first_pulse)
+        return fail(SAR_ERR_INVALID_ARGUMENT, "pulse block [%zu, %zu) outside [0, %zu)", first_pulse,
+                    first_pulse + count, p->S);
+    if (!p->grid) return fail(SAR_ERR_NOT_SUPPORTED, "pulse blocks need a regular-grid plan");
+    if (p->block && count > p->block)
+        return fail(SAR_ERR_INVALID_ARGUMENT, "a streamed plan takes pulse blocks of at most %zu pulses", p->block);
+    std::lock_guard<std::mutex> lock(p->mu);
+    DeviceGuard guard(p->device);
+    if (guard.status != cudaSuccess) return cuda_fail(guard.status, "select device");
+    cudaStream_t st = (cudaStream_t)stream;
+    p->last_stream = st;
+    // The block holds rows first_pulse .. first_pulse + count - 1; the upsampling addresses row s
+    // at y + s * N, so the base is moved back by first_pulse rows (only rows of the block are read).
+    const float2* y = reinterpret_cast<const float2*>(y_block_dev) - first_pulse * p->N;
+    // profile pairs: the resident buffer's rows of these pulses, or the streamed plan's ring slot
+    float4* pairs = p->block ? ring_slot(p, first_pulse) : p->d_prof + first_pulse * (size_t)p->Lg;
+    int rc = upsample_rows(p, y, first_pulse, first_pulse + count, st, true, nullptr,
+                           pairs - first_pulse * (size_t)p->Lg);
+    if (rc) return rc;
+    return gather_pulses(p, pairs, first_pulse, count, (float2*)x_dev, accumulate, st);
 }
 
 int sar_profiles(sar_plan* p, const void* y_dev, void* prof_dev, void* stream) {

@@ -1100,7 +1100,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     for (int e = threadIdx.x; e < pbf * wslots; e += blockDim.x) win[e] = make_float2(0.f, 0.f);
-    for (int e = threadIdx.x; e < npb; e += blockDim.x) wst[e] = a.strip_start[(size_t)strip * a.S + s0 + e];
+    for (int e = threadIdx.x; e < npb; e += blockDim.x) wst[e] = a.strip_start[(size_t)strip * a.strip_stride + s0 + e];
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], kWsProducers);
         mbar_init(&bars[1], kWsProducers);

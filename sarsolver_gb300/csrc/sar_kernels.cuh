@@ -64,7 +64,8 @@ struct FpGridArgs {
     const PulseGeom* pulses;   // [S]
     const float2* x;           // [P]
     float2* acc;               // [S][Lg] profile accumulator (pre-zeroed)
-    const int* strip_start;    // [n_strips][S] first bin of each strip window
+    const int* strip_start;    // first bin of each strip window: strip_start[strip * strip_stride + s]
+    int strip_stride;          // pulses per strip row of that table (the plan's S; S is a block's count)
     unsigned* flags;
     int S, Lg, bg0;
     int seg_tiles;             // tiles per strip segment (along y; along x when transposed)

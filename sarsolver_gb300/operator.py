@@ -17,7 +17,7 @@ import numpy as np
 import torch
 from scipy.sparse.linalg import LinearOperator
 
-from .plan import SarPlan
+from .plan import SarPlan, block_pulses_for
 
 
 def _to_device(x, device) -> torch.Tensor:
@@ -34,8 +34,9 @@ class NumpySimpleSarOperator(LinearOperator):
     """Scalar Born SAR operator A on the GPU with the reference's scipy interface.
 
     Signature of the reference (numpy/operator.py:12-13) plus ``interp`` and ``device``.
-    ``num_threads``, ``verbose`` and ``num_calculation_blocks`` are accepted for compatibility;
-    the GPU plan replaces process fan-out and pulse blocking.
+    ``num_threads`` and ``verbose`` are accepted for compatibility (the GPU plan replaces process
+    fan-out); ``num_calculation_blocks`` > 1 builds a streamed plan whose device memory is bounded by
+    two blocks of ceil(S / num_calculation_blocks) pulses, as the reference's blocking bounds its RAM.
     """
 
     def __init__(self, scene, aperture, num_threads: Optional[int] = None, upsample_ratio: float = 128.0,
@@ -50,7 +51,8 @@ class NumpySimpleSarOperator(LinearOperator):
         self._verbose = verbose
         self._num_calculation_blocks = num_calculation_blocks
         self._interp = interp
-        self.plan = SarPlan(scene, aperture, upsample_ratio=upsample_ratio, interp=interp, device=device)
+        self.plan = SarPlan(scene, aperture, upsample_ratio=upsample_ratio, interp=interp, device=device,
+                            block_pulses=block_pulses_for(scene, aperture.num_slow_times, num_calculation_blocks))
 
     # tensor-level API -----------------------------------------------------
     def forward(self, x) -> torch.Tensor:

@@ -28,6 +28,16 @@ def _interleave(z) -> np.ndarray:
     return np.ascontiguousarray(np.asarray(z, dtype=np.complex128).reshape(-1)).view(np.float64)
 
 
+def block_pulses_for(scene, num_slow_times: int, num_calculation_blocks) -> Optional[int]:
+    """Pulses per block of a streamed plan for the reference's ``num_calculation_blocks`` (slow-time
+    blocks, whose purpose in the reference is bounding memory, cxx_binding/forward.py:66-96): None
+    (a resident plan) for one block or an unstructured scene (streamed plans need a regular grid)."""
+    blocks = int(num_calculation_blocks or 1)
+    if blocks <= 1 or grid_axes(scene) is None:
+        return None
+    return -(-int(num_slow_times) // blocks)
+
+
 class SarPlan:
     """Operator plan on one CUDA device.
 
@@ -35,11 +45,13 @@ class SarPlan:
     ``upsample_ratio`` (default 128, as the reference) and the added ``interp``
     ("nearest_ref": the reference's bins and conventions; "linear": exact transpose pair) and
     ``path`` ("auto": grid fast path for linear, per-pixel double-float path for nearest_ref;
-    "grid" / "points" force one).
+    "grid" / "points" force one), and ``block_pulses``: a streamed plan whose device memory is
+    bounded by two blocks of that many pulses instead of the whole aperture (regular grids;
+    sar_plan_create_streamed), the replacement of the reference's ``num_calculation_blocks``.
     """
 
     def __init__(self, scene, aperture, upsample_ratio: float = 128.0, interp: str = "nearest_ref",
-                 device: Optional[torch.device] = None, path: str = "auto"):
+                 device: Optional[torch.device] = None, path: str = "auto", block_pulses: Optional[int] = None):
         if interp not in _lib.INTERP:
             raise ValueError(f"interp must be one of {sorted(_lib.INTERP)}")
         if path not in _lib.PATH:
@@ -95,7 +107,12 @@ class SarPlan:
         handle = ctypes.c_void_p()
         with torch.cuda.device(self.device):
             torch.cuda.current_stream(self.device)   # make sure the context exists
-            _lib.check(lib.sar_plan_create(ctypes.byref(g), self.device.index, ctypes.byref(handle)), "sar_plan_create")
+            if block_pulses:
+                _lib.check(lib.sar_plan_create_streamed(ctypes.byref(g), self.device.index, int(block_pulses),
+                                                        ctypes.byref(handle)), "sar_plan_create_streamed")
+            else:
+                _lib.check(lib.sar_plan_create(ctypes.byref(g), self.device.index, ctypes.byref(handle)),
+                           "sar_plan_create")
         self._handle = handle
         self._lib = lib
         info = _lib.SarPlanInfo()
@@ -112,6 +129,7 @@ class SarPlan:
         self.fused_upsampling = bool(info.fused_upsampling)
         self.fused_downsampling = bool(info.fused_downsampling)
         self.scatter_lanes_y = bool(info.scatter_lanes_y)
+        self.block_pulses = int(info.block_pulses)
         # The aperture's own weighting; phase corrections multiply it (autodiff.phase_weights).
         self.base_weights = torch.as_tensor(
             np.asarray(aperture.slow_time_weighting, dtype=np.complex64).reshape(-1)).to(self.device)
@@ -189,6 +207,8 @@ class SarPlan:
         if not self.is_grid:
             raise ValueError("streamed backprojection needs a regular-grid scene")
         S, N = self.num_slow_times, self.num_freqs
+        if self.block_pulses:
+            block = min(int(block), self.block_pulses)
         yh = torch.as_tensor(y_host).reshape(S, N)
         if yh.dtype != torch.complex64:
             yh = yh.to(torch.complex64)
