@@ -98,5 +98,12 @@ def test_pdhg_meets_reference_artifact(cil):
                            g=fake_cil.ZeroFunction())
     solver.run(3)
     soln = np.load(os.path.join(GOLDEN, "little_pdhg.npz"))["soln"].reshape(solver.x.array.shape)
-    assert solver.x.array == pytest.approx(soln, rel=1.0e-3)
+    got = solver.x.array
+    assert rel_l2(got, soln) < 1e-5
+    # the reference's elementwise rel 1e-3, with an absolute floor at complex64 accuracy relative
+    # to the image's scale: pixels ~1e4 below the image's RMS carry FP32 rounding of the full-scale
+    # sums (one such pixel: |x| = 2.8e-7 against RMS 2.8e-3, |error| = 3.4e-10)
+    assert got == pytest.approx(soln, rel=1.0e-3, abs=1.0e-6 * np.abs(soln).max())
+    strict = np.abs(got - soln) <= 1.0e-3 * np.abs(soln)
+    assert strict.mean() > 0.9999
 
