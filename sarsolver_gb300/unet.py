@@ -175,52 +175,3 @@ class UNetFunction(torch.autograd.Function):
     def backward(ctx, grad_out: torch.Tensor):
         ctx.net.backward(grad_out)
         return None, None, None
-
-
-def _main(argv=None) -> None:
-    """Time the network's forward and backward passes (CUDA events) on a random image:
-    ``python -m sarsolver_gb300.unet --size 512 --batch 1 --iters 10``."""
-    import argparse
-    import json
-
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--size", type=int, default=512)
-    ap.add_argument("--batch", type=int, default=1)
-    ap.add_argument("--iters", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--base-channels", type=int, default=32)
-    args = ap.parse_args(argv)
-    torch.cuda.set_device(0)
-    net = UNet(args.base_channels, seed=0)
-    g = torch.Generator(device="cuda")
-    g.manual_seed(0)
-    shape = (args.batch, args.size, args.size)
-    x = torch.complex(torch.randn(shape, device="cuda", generator=g), torch.randn(shape, device="cuda", generator=g))
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-    fwd = bwd = 0.0
-    for i in range(args.warmup + args.iters):
-        ev[0].record()
-        y = net.forward(x)
-        ev[1].record()
-        net.zero_grad()
-        net.backward(y)
-        ev[2].record()
-        torch.cuda.synchronize()
-        if i >= args.warmup:
-            fwd += ev[0].elapsed_time(ev[1])
-            bwd += ev[1].elapsed_time(ev[2])
-    c = args.base_channels
-    # multiply-adds per pixel of the 15 convolutions at their levels (3x3 taps; 1x1 output layer)
-    macs = 0.0
-    for l in net.layers:
-        macs += l["taps"] * (l["cin0"] + l["cin1"]) * l["cout"] / 4 ** l["level"]
-    flops_fwd = 2.0 * macs * args.batch * args.size ** 2
-    out = {"size": args.size, "batch": args.batch, "base_channels": c,
-           "forward_ms": fwd / args.iters, "backward_ms": bwd / args.iters,
-           "forward_tflops": flops_fwd / (fwd / args.iters * 1e-3) / 1e12,
-           "backward_tflops": 2 * flops_fwd / (bwd / args.iters * 1e-3) / 1e12, "flags": net.flags()}
-    print(json.dumps(out))
-
-
-if __name__ == "__main__":
-    _main()
