@@ -301,7 +301,7 @@ def learned_vs_plain(scenes: int) -> dict:
     warm, cfg = load_warm_start(DEFAULT_WEIGHTS)
     src = SceneSource(cfg, seed=424242, continuous=True)
     compare(warm, src, 1)                       # warm-up: plans, cuFFT plans, module loads
-    recs = compare(warm, src, scenes, repeats=2)
+    recs = compare(warm, src, scenes, repeats=2, truth=True)
     # component times on the last scene's plan: one operator pair and one U-Net inference
     plan, y, _, _, _ = src.sample()
     b = plan.adjoint(y)

@@ -439,9 +439,10 @@ size_t bp_grid_ws_smem_bytes(int wwin, int pb) {
 //   four only read with split bins: nearest-bin modes and windows wider than 256 bins)
 // so that each half of a 16-byte shared-memory load is one operand pair.  Per pixel the
 // polynomials are evaluated in Horner form in the row offset dj (the only per-row constant a
-// thread keeps), the phase is reduced to [-0.5, 0.5] cycles with the 1.5 * 2^23 shifter
-// instead of rint (keeping the special-function pipe for sin and cos), and the complex
-// multiply-accumulate runs on (pulse p, pulse p + 1) accumulator pairs.  A stage with an odd
+// thread keeps); the thread's phase constant is reduced mod 1 once per pulse pair, so every pixel's
+// phase stays below ~5 cycles and goes to __sincosf without a per-pixel reduction (the special-
+// function pipe then carries only sine and cosine: two of its operations per pixel-pulse), and
+// the complex multiply-accumulate runs on (pulse p, pulse p + 1) accumulator pairs.  A stage with an odd
 // number of pulses gets a padding pulse with zero coefficients and a zeroed window.
 __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
@@ -658,13 +659,15 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
                     bv2 = f2(H.z, H.w);
                 }
             }
+            // the thread's phase constant mod 1 (once per pulse pair): its pixels' phases then stay
+            // below ~5 cycles, which __sincosf's own argument reduction takes as is
+            cph = fma2(f2(rintf(cph.x), rintf(cph.y)), M1, cph);
             const float4* wa = win + (size_t)(2 * pp) * ww;
             const float4* wb = wa + ww;
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
                 const float2 d = DU[r];
                 const float2 ph = fma2(fma2(fma2(c9, d, b2), d, b1), d, cph);
-                const float2 f = fma2(f2(rintf(ph.x), rintf(ph.y)), M1, ph);   // ph - rint(ph), exact
                 const float2 v = PRECISE ? fma2(fma2(fma2(vtop, d, bv2), d, bv1), d, cv) : fma2(fma2(bv2, d, bv1), d, cv);
                 float2 r1 = add2(v, SH);
                 const float2 s = fma2(add2(r1, NSH), M1, v);               // v - rint(v), exact
@@ -689,7 +692,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
                 const float4 pa = wa[ia], pq = wb[ib];
                 const float2 re = f2(fmaf(s.x, pa.z, pa.x), fmaf(s.y, pq.z, pq.x));
                 const float2 im = f2(fmaf(s.x, pa.w, pa.y), fmaf(s.y, pq.w, pq.y));
-                const float2 x = mul2(f, TWO_PI2);
+                const float2 x = mul2(ph, TWO_PI2);   // |ph| < ~5 cycles: no per-pixel reduction
                 float2 sn, cn;
                 __sincosf(x.x, &sn.x, &cn.x);
                 __sincosf(x.y, &sn.y, &cn.y);
@@ -979,7 +982,10 @@ template <bool TWO, int G>
 __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float c9p, const ColumnTerms& ctq, float c9q,
                                                   const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
                                                   int ws, int lane) {
-    const float2 cph = f2(ctp.cph, ctq.cph), b1 = f2(ctp.b1, ctq.b1), b2 = f2(ctp.b2, ctq.b2), c9 = f2(c9p, c9q);
+    // the lane's phase constant and its rate along the walked rows mod 1 (rows are integer offsets),
+    // so that each row's phase stays below ~5 cycles and goes to __sincosf without reduction
+    const float2 cph = f2(ctp.cph - rintf(ctp.cph), ctq.cph - rintf(ctq.cph));
+    const float2 b1 = f2(ctp.b1 - rintf(ctp.b1), ctq.b1 - rintf(ctq.b1)), b2 = f2(ctp.b2, ctq.b2), c9 = f2(c9p, c9q);
     const float2 cv = f2(ctp.cv, ctq.cv), bv1 = f2(ctp.bv1, ctq.bv1), bv2 = f2(ctp.bv2, ctq.bv2);
     const float2 SH = f2(SAR_SHIFTER, SAR_SHIFTER);
     const float2 M1 = f2(-1.f, -1.f), TWO_PI2 = f2(SAR_TWO_PI, SAR_TWO_PI);
@@ -1004,11 +1010,10 @@ __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float 
         const float2 d = f2(dj, dj);
         const float2 xv = xrow[rr * kXtStride + lane];
         const float2 ph = fma2(fma2(fma2(c9, d, b2), d, b1), d, cph);
-        const float2 f = fma2(f2(rintf(ph.x), rintf(ph.y)), M1, ph);   // ph - rint(ph), exact
         const float2 v = fma2(fma2(bv2, d, bv1), d, cv);
         const float2 av = add2(v, nc);
         const float2 aa = f2(fabsf(av.x), fabsf(av.y));
-        const float2 x = mul2(f, TWO_PI2);
+        const float2 x = mul2(ph, TWO_PI2);
         float2 sn, cn;
         __sincosf(x.x, &sn.x, &cn.x);
         __sincosf(x.y, &sn.y, &cn.y);

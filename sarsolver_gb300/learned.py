@@ -307,6 +307,11 @@ class SolveRecord:
     start_residual: float       # ||A^H (y - A x0)|| / ||A^H y|| of the warm start
     plain_converged: bool
     learned_converged: bool
+    # ceiling of any scene-predicting warm start: CGLS started at the true scene (a perfect
+    # prior over scenes; the least-squares solution it must still reach also fits the noise)
+    truth_iterations: int = 0
+    truth_ms: float = float("nan")
+    truth_start_residual: float = float("nan")
 
 
 def _timed(fn):
@@ -318,15 +323,21 @@ def _timed(fn):
 
 
 def compare(warm: WarmStart, source: SceneSource, count: int, tol: float = 1e-3, max_iterations: int = 1000,
-            repeats: int = 1) -> List[SolveRecord]:
+            repeats: int = 1, truth: bool = False) -> List[SolveRecord]:
     """Plain CGLS from zero vs CGLS from the learned warm start, both to ``tol`` in the
     normal-equations residual; times are wall clock around the whole solve (the warm start's
-    backprojection, network and the CGLS iterations), best of ``repeats``."""
+    backprojection, network and the CGLS iterations), best of ``repeats``.  With ``truth`` also
+    CGLS started at the true scene (given start, no network), the ceiling of any warm start that
+    predicts the scene."""
     out = []
     for _ in range(count):
-        plan, y, _, extent, snr = source.sample()
-        best_plain = best_learned = float("inf")
+        plan, y, x_true, extent, snr = source.sample()
+        best_plain = best_learned = best_truth = float("inf")
+        it = None
         for _ in range(repeats):
+            if truth:
+                (xt, it), tt = _timed(lambda: cgls(plan, y, x0=x_true, tol=tol, max_iterations=max_iterations))
+                best_truth = min(best_truth, tt)
             (xp, ip), tp = _timed(lambda: cgls(plan, y, tol=tol, max_iterations=max_iterations))
             best_plain = min(best_plain, tp)
 
@@ -335,6 +346,10 @@ def compare(warm: WarmStart, source: SceneSource, count: int, tol: float = 1e-3,
 
             (xl, il), tl = _timed(learned)
             best_learned = min(best_learned, tl)
-        out.append(SolveRecord(extent, snr, ip.iterations, best_plain, il.iterations, best_learned,
-                               il.history[0] if il.history else float("nan"), ip.converged, il.converged))
+        rec = SolveRecord(extent, snr, ip.iterations, best_plain, il.iterations, best_learned,
+                          il.history[0] if il.history else float("nan"), ip.converged, il.converged)
+        if it is not None:
+            rec.truth_iterations, rec.truth_ms = it.iterations, best_truth
+            rec.truth_start_residual = it.history[0] if it.history else float("nan")
+        out.append(rec)
     return out

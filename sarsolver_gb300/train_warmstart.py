@@ -45,6 +45,11 @@ def summary(records) -> dict:
         "learned_iterations": float(np.mean([r.learned_iterations for r in records])),
         "warm_start_residual": float(np.mean([r.start_residual for r in records])),
         "all_converged": bool(all(r.plain_converged and r.learned_converged for r in records)),
+        **({"truth_start_iterations": float(np.mean([r.truth_iterations for r in records])),
+            "truth_start_ms": float(np.mean([r.truth_ms for r in records])),
+            "truth_start_residual": float(np.mean([r.truth_start_residual for r in records])),
+            "warm_start_ceiling_speedup": plain_ms / float(np.mean([r.truth_ms for r in records]))}
+           if records and np.isfinite(records[0].truth_ms) else {}),
     }
 
 
