@@ -125,8 +125,29 @@ class WarmStart:
         b = plan.adjoint(y)
         return cgls(plan, y, x0=self.direction(b), tol=tol, max_iterations=max_iterations, start="scaled", ahy=b)
 
-    def loss(self, plan: SarPlan, y: torch.Tensor) -> torch.Tensor:
-        """Normal-equations residual of the warm start, squared and relative; differentiable in U."""
+    def loss(self, plan: SarPlan, y: torch.Tensor, x_true: Optional[torch.Tensor] = None,
+             kind: str = "normal") -> torch.Tensor:
+        """Training loss of the warm start, differentiable in U.
+
+        ``normal``: the normal-equations residual ||A^H (y - A x0)||^2 / ||A^H y||^2 of x0 = c z,
+        z = b + s U(b / s) (weights the error by the squared singular values, so it favours the
+        components CGLS settles in its first iterations anyway).  ``data``: 1 - cos^2 of the angle
+        between A z and y (real scale), i.e. the data residual ||y - c A z||^2 / ||y||^2 at the
+        solver's best real c -- the starting error CGLS minimises, in the A-norm.  ``truth``: the
+        same against the noise-free data A x_true (needs ``x_true``): z should predict the scene."""
+        if kind in ("data", "truth"):
+            with torch.no_grad():
+                b = plan.adjoint(y)
+                s = torch.sqrt((b.real.square() + b.imag.square()).mean()).clamp_min(1e-30)
+                t = y if kind == "data" else plan.forward(x_true)
+            u = _UNetApply.apply(b.view(1, self.n, self.n), self.net, float(1.0 / s), self.anchor).reshape(-1)
+            az = sar_forward(plan, b + s * u)
+            re = (az.real.double() * t.real.double() + az.imag.double() * t.imag.double()).sum()
+            aa = (az.real.double() ** 2 + az.imag.double() ** 2).sum()
+            tt = (t.real.double() ** 2 + t.imag.double() ** 2).sum()
+            return 1.0 - re * re / (aa * tt).clamp_min(1e-300)
+        if kind != "normal":
+            raise ValueError(f"unknown loss {kind!r}")
         with torch.no_grad():
             b, bb, c, s = self._terms(plan, y)
         u = _UNetApply.apply(b.view(1, self.n, self.n), self.net, float(1.0 / s), self.anchor).reshape(-1)
@@ -266,9 +287,9 @@ class TrainLog:
 
 
 def train(net: UNet, source: SceneSource, scenes: int, batch: int = 8, lr: float = 1e-3, log_every: int = 50,
-          warm: Optional[WarmStart] = None, printer=None) -> TrainLog:
-    """Adam on the mean warm-start loss over mini-batches of generated scenes; cosine learning
-    rate decay to lr / 20."""
+          warm: Optional[WarmStart] = None, printer=None, loss: str = "normal") -> TrainLog:
+    """Adam on the mean warm-start loss (``WarmStart.loss`` of kind ``loss``) over mini-batches of
+    generated scenes; cosine learning rate decay to lr / 20."""
     warm = warm or WarmStart(net, source.cfg.n)
     steps = max(1, scenes // batch)
     log = TrainLog()
@@ -277,8 +298,8 @@ def train(net: UNet, source: SceneSource, scenes: int, batch: int = 8, lr: float
     for step in range(steps):
         net.zero_grad()
         for _ in range(batch):
-            plan, y, _, _, _ = source.sample()
-            L = warm.loss(plan, y)
+            plan, y, x_true, _, _ = source.sample()
+            L = warm.loss(plan, y, x_true, kind=loss)
             (L / batch).backward()
             running.append(float(L.detach()))
         rate = lr * (0.05 + 0.95 * 0.5 * (1.0 + math.cos(math.pi * step / steps)))

@@ -64,6 +64,9 @@ def main(argv=None):
     ap.add_argument("--out", default=DEFAULT_WEIGHTS)
     ap.add_argument("--init", default=None, help="start from this checkpoint")
     ap.add_argument("--tol", type=float, default=1e-3)
+    ap.add_argument("--loss", choices=["normal", "data", "truth"], default="normal",
+                    help="training loss (WarmStart.loss): normal-equations residual, data residual, or "
+                         "data-domain error against the noise-free scene")
     args = ap.parse_args(argv)
 
     torch.cuda.set_device(0)
@@ -74,7 +77,7 @@ def main(argv=None):
         net.set_params(state["params"])
     warm = WarmStart(net, cfg.n)
     src = SceneSource(cfg, seed=1000 + args.seed)
-    log = train(net, src, args.scenes, batch=args.batch, lr=args.lr, warm=warm,
+    log = train(net, src, args.scenes, batch=args.batch, lr=args.lr, warm=warm, loss=args.loss,
                 printer=lambda s: print(s, flush=True)) if args.scenes > 0 else None
     src.close()
     if net.flags():
@@ -83,7 +86,7 @@ def main(argv=None):
         os.makedirs(os.path.dirname(os.path.abspath(args.out)), exist_ok=True)
         # bf16 is what the kernels use for the filters; biases lose nothing that matters.
         torch.save({"base_channels": args.base_channels, "params": net.params().cpu().to(torch.bfloat16),
-                    "config": dataclasses.asdict(cfg),
+                    "config": dataclasses.asdict(cfg), "loss": args.loss,
                     "log": {"steps": log.steps, "loss": log.loss, "scenes": log.scenes, "seconds": log.seconds}},
                    args.out)
         print(json.dumps({"trained_scenes": log.scenes, "seconds": round(log.seconds, 1),
@@ -91,7 +94,7 @@ def main(argv=None):
     if args.eval:
         test = SceneSource(cfg, seed=99991, continuous=True)
         compare(warm, test, 1, tol=args.tol)    # warm-up (plans, cuFFT, module loads)
-        recs = compare(warm, test, args.eval, tol=args.tol, repeats=2)
+        recs = compare(warm, test, args.eval, tol=args.tol, repeats=2, truth=True)
         for r in recs:
             print(json.dumps(dataclasses.asdict(r)), flush=True)
         print(json.dumps({"summary": summary(recs)}), flush=True)
