@@ -448,6 +448,12 @@ __device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+// 16-byte shared-memory load at a 32-bit shared address.
+__device__ __forceinline__ float4 lds_f4(uint32_t addr) {
+    float4 v;
+    asm("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
+    return v;
+}
 
 __device__ __forceinline__ void producer_coeffs_pair(const GridConst& g, const PulseGeom* __restrict__ pulses, int s0,
                                                      int npb, int pass, const df3* anchors, float4* coef, int* base,
@@ -472,11 +478,16 @@ __device__ __forceinline__ void producer_coeffs_pair(const GridConst& g, const P
     if (valid) {
         bin_coeffs(ae, vb, b, g, co);
         // every pixel's bin must fall inside the tile's staged window: index rint(v) + ww / 2 in
-        // [0, ww - 1] (the consumers clamp, so an undersized window would otherwise pass silently)
+        // [0, ww - 1] (an undersized window would otherwise be clamped silently, or read out of it)
         float lo, hi;
         bin_extent(co, &lo, &hi);
         const float half = 0.5f * (float)ww;
-        if (!(lo >= -half - 0.49f && hi <= half - 0.51f)) raise_flag(flags, FLAG_GATHER_WINDOW);
+        if (!(lo >= -half - 0.49f && hi <= half - 0.51f)) {
+            // the result is invalid (flagged); a zero set keeps every consumer index at ww / 2,
+            // inside the window, so the lanes-along-x consumers may address without clamping
+            raise_flag(flags, FLAG_GATHER_WINDOW);
+            co = Coeffs{};
+        }
     }
     if (valid || pad) {   // the padding pulse stores zeros (co = {})
         float* dst = reinterpret_cast<float*>(coef + ((pi >> 1) * 4 + q) * kPairSetF4) + (pi & 1);
@@ -664,6 +675,12 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
             cph = fma2(f2(rintf(cph.x), rintf(cph.y)), M1, cph);
             const float4* wa = win + (size_t)(2 * pp) * ww;
             const float4* wb = wa + ww;
+            // lanes along x: window addresses straight from the shifter's bits (index rint(v) +
+            // ww / 2 = bits + idx_bias; 32-bit shared addresses, mod 2^32) with no clamp -- the
+            // producers' bound on every set keeps the index in [0, ww - 1] (measured 4 % faster
+            // there; lanes along y keep the clamped form, which is faster for them)
+            const uint32_t wa_s = smem_addr(wa), wb_s = wa_s + 16u * (uint32_t)ww;
+            const uint32_t wa_b = wa_s + 16u * (uint32_t)idx_bias, wb_b = wb_s + 16u * (uint32_t)idx_bias;
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
                 const float2 d = DU[r];
@@ -672,8 +689,15 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
                 float2 r1 = add2(v, SH);
                 const float2 s = fma2(add2(r1, NSH), M1, v);               // v - rint(v), exact
                 if (PRECISE) r1 = add2(r1, fma2(cid, d, ci));              // + the exact integer part
-                unsigned ia = min((unsigned)(__float_as_int(r1.x) + idx_bias), idx_max);
-                unsigned ib = min((unsigned)(__float_as_int(r1.y) + idx_bias), idx_max);
+                unsigned ia = 0, ib = 0;
+                uint32_t aa = 0, ab = 0;
+                if (LANES_Y) {
+                    ia = min((unsigned)(__float_as_int(r1.x) + idx_bias), idx_max);
+                    ib = min((unsigned)(__float_as_int(r1.y) + idx_bias), idx_max);
+                } else {
+                    aa = wa_b + ((uint32_t)__float_as_int(r1.x) << 4);
+                    ab = wb_b + ((uint32_t)__float_as_int(r1.y) << 4);
+                }
                 if (NEAREST && (fabsf(s.x) > kNearEdge || fabsf(s.y) > kNearEdge)) {
                     // near a rounding boundary: the exact bin, as a window index of the pulse
                     const int px = ti * kTile + (LANES_Y ? 4 * warp + r : lane);
@@ -686,10 +710,14 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
                         const int gi = exact_grid_bin(a.steps, a.pulses, a.alpha2, g.s_r.hi, g.s_r.lo, a.bg0,
                                                       BIN_ADJ_NEAREST, px, py, k, sp + h);
                         const unsigned w = min((unsigned)(gi - g0), idx_max);
-                        if (h) ib = w; else ia = w;
+                        if (LANES_Y) {
+                            if (h) ib = w; else ia = w;
+                        } else {
+                            if (h) ab = wb_s + 16u * w; else aa = wa_s + 16u * w;
+                        }
                     }
                 }
-                const float4 pa = wa[ia], pq = wb[ib];
+                const float4 pa = LANES_Y ? wa[ia] : lds_f4(aa), pq = LANES_Y ? wb[ib] : lds_f4(ab);
                 const float2 re = f2(fmaf(s.x, pa.z, pa.x), fmaf(s.y, pq.z, pq.x));
                 const float2 im = f2(fmaf(s.x, pa.w, pa.y), fmaf(s.y, pq.w, pq.y));
                 const float2 x = mul2(ph, TWO_PI2);   // |ph| < ~5 cycles: no per-pixel reduction
@@ -844,7 +872,7 @@ __device__ __forceinline__ RowEval<PRECISE> scatter_eval(const ColumnTerms& ct, 
     const float v = pixel_bin<PRECISE>(ct, w9, dj, dj2, dj3);
     e.bp = bin_position<PRECISE>(v, PRECISE ? fmaf(ib, dj, ct.ci) : 0.f);
     float sn, cn;
-    __sincosf(SAR_TWO_PI * (ph - rintf(ph)), &sn, &cn);
+    __sincosf(SAR_TWO_PI * ph, &sn, &cn);   // |ph| < ~5 cycles: the caller reduced the constants
     e.cr = xv.x * cn - xv.y * sn;   // x * exp(+2 pi i f)
     e.ci = fmaf(xv.x, sn, xv.y * cn);
     return e;
@@ -879,16 +907,22 @@ __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, 
                                              const ColumnTerms& ctq, float c9q, float w9q, float ibq,
                                              const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
                                              int ws, int lane, const NearCtx& nc) {
+    // the lane's phase constant and its rate along the rows mod 1 (rows are integer offsets)
+    ColumnTerms cp = ctp, cq = ctq;
+    cp.cph -= rintf(cp.cph);
+    cp.b1 -= rintf(cp.b1);
+    cq.cph -= rintf(cq.cph);
+    cq.b1 -= rintf(cq.b1);
 #pragma unroll 2
     for (int rr = 0; rr < 16; ++rr) {
         const float dj = (float)(rr - 8);
         const float2 xv = xrow[rr * kXtStride + lane];
-        const RowEval<PRECISE> ep = scatter_eval<PRECISE>(ctp, c9p, w9p, ibp, dj, xv);
+        const RowEval<PRECISE> ep = scatter_eval<PRECISE>(cp, c9p, w9p, ibp, dj, xv);
         const int ip = (int)min((unsigned)(ep.bp.n + off_p), (unsigned)(ws - 2));
         RowEval<PRECISE> eq;
         int iq = 0;
         if (TWO) {
-            eq = scatter_eval<PRECISE>(ctq, c9q, w9q, ibq, dj, xv);
+            eq = scatter_eval<PRECISE>(cq, c9q, w9q, ibq, dj, xv);
             iq = (int)min((unsigned)(eq.bp.n + off_q), (unsigned)(ws - 2));
         }
         if (LINEAR) {
