@@ -220,6 +220,10 @@ class SarPlan:
         bufs = [torch.empty((block, N), dtype=torch.complex64, device=self.device) for _ in range(2)]
         copied = [torch.cuda.Event() for _ in range(2)]
         consumed = [torch.cuda.Event() for _ in range(2)]
+        # The buffers come from the compute stream's pool: memory freed there may still be read by
+        # kernels already queued on it (e.g. the previous call's gathers), so the side stream's
+        # copies start only after everything queued on the compute stream so far.
+        side.wait_stream(compute)
         nblk = (S + block - 1) // block
         with torch.cuda.device(self.device):
             for k in range(nblk):

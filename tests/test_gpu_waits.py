@@ -51,11 +51,14 @@ def test_streamed_backprojection_is_bitwise_reproducible():
     plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp="linear")
     y = torch.from_numpy(crandn(rng, 512, 512)).to(torch.complex64)
     yh = y.pin_memory()
+    # back to back, no synchronisation in between: the second call's host-to-device copies must not
+    # overwrite staging memory the first call's gathers are still reading
     a = plan.adjoint_streamed(yh, block=128).clone()
     b = plan.adjoint_streamed(yh, block=128).clone()
+    c = plan.adjoint_streamed(yh, block=128).clone()
     full = plan.adjoint(y.cuda())
     torch.cuda.synchronize()
-    assert torch.equal(a, b)
+    assert torch.equal(a, b) and torch.equal(b, c)
     assert float(torch.linalg.vector_norm(a - full) / torch.linalg.vector_norm(full)) < 5e-6
     assert plan.device_flags() == 0
 
