@@ -105,6 +105,7 @@ struct sar_plan {
     int wwin = 0, pb = 32;
     int lanes_y = 0;
     bool staged = true;
+    bool values = false;   // stored profiles are plain values (kProfValues), not pairs
     int seg_tiles = 0, segs_per_column = 0, ws = 0, pbf = 16;
     size_t n_strips = 0;
     int chunk = 0;
@@ -479,14 +480,19 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
         p->bg0 = (long)std::floor(vmin) - span_ww / 2 - 4;
         const double span = std::ceil(vmax) + span_ww / 2 + 5 - (double)p->bg0;
         if (span > 2.0e9) return fail(SAR_ERR_NOT_SUPPORTED, "range span too large");
-        p->Lg = (int)span;
+        p->Lg = (int)span + ((int)span & 1);   // even: rows of plain values stay 16-byte aligned
         // Backprojection staging: pulses per stage so that the double-buffered windows of the
         // pipelined kernel fit shared memory with two CTAs per SM; otherwise read windows
         // from global memory directly.
         p->staged = false;
         p->pb = 32;
-        for (int pb = 32; pb >= 2; pb /= 2)   // stages the two producer warps split evenly
-            if (bp_grid_ws_smem_bytes(p->wwin, pb) <= kBpSmemBudget) {
+        // stages the two producer warps split evenly.  Nearest-bin sampling with windows wider than
+        // 256 bins (large upsampling factors) stores and stages plain values, half the bytes of
+        // pairs: at upsample 128 that measured a third faster, at upsample 8 slower (wider
+        // addressing in the gather), so narrower windows keep pairs.
+        p->values = p->interp == SAR_INTERP_NEAREST_REF && p->wwin > 256;
+        for (int pb = 32; pb >= 2; pb /= 2)
+            if (bp_grid_ws_smem_bytes(p->wwin, pb, p->values) <= kBpSmemBudget) {
                 p->pb = pb;
                 p->staged = true;
                 break;
@@ -597,7 +603,7 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
         p->bg0 = (long)std::floor(vmin) - 4;
         const double span = std::ceil(vmax) + 6 - (double)p->bg0;
         if (span > 2.0e9) return fail(SAR_ERR_NOT_SUPPORTED, "range span too large");
-        p->Lg = (int)span;
+        p->Lg = (int)span + ((int)span & 1);
         p->wwin = 0;
     }
     // nearest bins on the grid paths: antenna norms for the exact decisions near a boundary
@@ -824,6 +830,11 @@ int sar_plan_get_info(const sar_plan* p, sar_plan_info* info) {
     return SAR_OK;
 }
 
+// Stored profile format of a plan (the upsampling writers' `linear` argument).
+static int prof_format(const sar_plan* p) {
+    return p->values ? kProfValues : p->interp == SAR_INTERP_LINEAR ? kProfLinearPairs : kProfNearestPairs;
+}
+
 // Upsampled profiles of pulses [begin, end): y row s is read at y + s * N; with pairs_out the
 // (value, difference) pairs of pulse s go to pairs_rows + s * Lg (the plan's buffer for a resident
 // plan; a ring slot, addressed from the block's first pulse, for a streamed one).
@@ -835,8 +846,7 @@ static int upsample_rows(sar_plan* p, const float2* y, size_t begin, size_t end,
         const int dbl = p->fft_double;
         if (pairs_out && p->fused_up) {
             SAR_CUDA(launch_upsample_pairs_fused(y, p->d_wave, p->d_wadj, p->d_tw_n, p->d_tw_m, pairs_rows, (int)p->N,
-                                                 (long)p->M, p->Lg, p->bg0, rows, (int)first,
-                                                 p->interp == SAR_INTERP_LINEAR, st),
+                                                 (long)p->M, p->Lg, p->bg0, rows, (int)first, prof_format(p), st),
                      "fused upsampling");
             continue;
         }
@@ -851,7 +861,7 @@ static int upsample_rows(sar_plan* p, const float2* y, size_t begin, size_t end,
                       "cufftExecC2C (callbacks)");
             SAR_CUDA(launch_unpack_compact(p->d_compact, p->Lc, p->d_wadj, pairs_out ? p->d_prof : nullptr,
                                            pairs_out ? nullptr : prof, (long)p->M, p->Lg, rows, (int)first,
-                                           p->interp == SAR_INTERP_LINEAR, st),
+                                           prof_format(p), st),
                      "unpack");
             continue;
         }
@@ -860,7 +870,7 @@ static int upsample_rows(sar_plan* p, const float2* y, size_t begin, size_t end,
         if (rc) return rc;
         if (pairs_out)
             SAR_CUDA(launch_unpack_pairs(p->d_spec, dbl, p->d_wadj, pairs_rows, (long)p->M, p->Lg, p->bg0, rows,
-                                         (int)first, p->interp == SAR_INTERP_LINEAR, st),
+                                         (int)first, prof_format(p), st),
                      "unpack");
         else
             SAR_CUDA(launch_unpack_profiles(p->d_spec, dbl, prof, (long)p->M, p->Lg, p->bg0, rows, (int)first, st),
@@ -887,6 +897,7 @@ static PointArgs point_args(sar_plan* p, int bin_rule) {
     a.bg0 = (int)p->bg0;
     a.linear = p->interp == SAR_INTERP_LINEAR;
     a.flags = p->d_flags;
+    a.values = p->values ? 1 : 0;
     return a;
 }
 
@@ -908,6 +919,7 @@ static int gather_pulses(sar_plan* p, const float4* pairs, size_t first, size_t 
     a.accumulate = accumulate ? 1 : 0;
     a.lanes_y = p->lanes_y;
     a.nearest = p->interp == SAR_INTERP_NEAREST_REF;
+    a.values = p->values ? 1 : 0;
     a.steps = p->d_steps;
     a.alpha2 = p->d_alpha2 ? p->d_alpha2 + first : nullptr;   // indexed by block-relative pulse
     a.wait_budget = p->wait_budget;
@@ -917,8 +929,16 @@ static int gather_pulses(sar_plan* p, const float4* pairs, size_t first, size_t 
 }
 
 // Ring slot of a streamed plan for the block starting at pulse `first`.
+// `rows` profile rows after `base`: rows of Lg 16-byte pairs, or of Lg plain 8-byte values for
+// plans that store values (may point before the buffer when the callee only touches rows from
+// the block's first pulse on).
+static float4* prof_rows(const sar_plan* p, float4* base, long rows) {
+    const long bytes = rows * (long)p->Lg * (p->values ? 8 : 16);
+    return reinterpret_cast<float4*>(reinterpret_cast<char*>(base) + bytes);
+}
+
 static float4* ring_slot(sar_plan* p, size_t first) {
-    return p->d_prof + ((first / p->block) & 1) * p->block * (size_t)p->Lg;
+    return prof_rows(p, p->d_prof, (long)(((first / p->block) & 1) * p->block));
 }
 
 int sar_adjoint(sar_plan* p, const void* y_dev, void* x_dev, void* stream) {
@@ -938,7 +958,7 @@ int sar_adjoint(sar_plan* p, const void* y_dev, void* x_dev, void* stream) {
             const size_t count = std::min(p->block, p->S - first);
             float4* slot = ring_slot(p, first);
             int rc = upsample_rows(p, (const float2*)y_dev, first, first + count, st, true, nullptr,
-                                   slot - first * (size_t)p->Lg);
+                                   prof_rows(p, slot, -(long)first));
             if (rc) return rc;
             if ((rc = gather_pulses(p, slot, first, count, (float2*)x_dev, first > 0, st))) return rc;
         }
@@ -1084,9 +1104,9 @@ int sar_adjoint_pulse_block(sar_plan* p, const void* y_block_dev, size_t first_p
     // at y + s * N, so the base is moved back by first_pulse rows (only rows of the block are read).
     const float2* y = reinterpret_cast<const float2*>(y_block_dev) - first_pulse * p->N;
     // profile pairs: the resident buffer's rows of these pulses, or the streamed plan's ring slot
-    float4* pairs = p->block ? ring_slot(p, first_pulse) : p->d_prof + first_pulse * (size_t)p->Lg;
+    float4* pairs = p->block ? ring_slot(p, first_pulse) : prof_rows(p, p->d_prof, (long)first_pulse);
     int rc = upsample_rows(p, y, first_pulse, first_pulse + count, st, true, nullptr,
-                           pairs - first_pulse * (size_t)p->Lg);
+                           prof_rows(p, pairs, -(long)first_pulse));
     if (rc) return rc;
     return gather_pulses(p, pairs, first_pulse, count, (float2*)x_dev, accumulate, st);
 }

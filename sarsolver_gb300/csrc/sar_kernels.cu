@@ -268,9 +268,16 @@ __global__ void __launch_bounds__(kThreads, 2) bp_grid_kernel(const BpGridArgs a
             for (int r = 0; r < 4; ++r) {
                 const PixelEval e = e4[r];
                 const int gi = gi4[r];
-                const float4 pv = __ldg(gp + gi);
-                const float re = fmaf(e.sf, pv.z, pv.x);
-                const float im = fmaf(e.sf, pv.w, pv.y);
+                float re, im;
+                if (NEAREST && a.values) {   // nearest-bin profiles stored as plain values (float2 rows)
+                    const float2 pv = __ldg(reinterpret_cast<const float2*>(a.pairs) + (size_t)(s0 + pi) * a.Lg + gi);
+                    re = pv.x;
+                    im = pv.y;
+                } else {
+                    const float4 pv = __ldg(gp + gi);
+                    re = fmaf(e.sf, pv.z, pv.x);
+                    im = fmaf(e.sf, pv.w, pv.y);
+                }
                 float sn, cn;
                 __sincosf(SAR_TWO_PI * e.f, &sn, &cn);
                 // x += value * exp(-2 pi i f)
@@ -422,10 +429,26 @@ __device__ __forceinline__ void producer_coeffs(const GridConst& g, const PulseG
 constexpr int kPairSetF4 = 2 * kSetF4 + 1;
 __host__ __device__ inline size_t pair_coef_f4(int pb) { return (size_t)((pb + 1) / 2) * 4 * kPairSetF4; }
 
-size_t bp_grid_ws_smem_bytes(int wwin, int pb) {
-    // windows [2][pb][wwin] + coefficient sets [2][pb/2][4] + base bins [2][pb] + 4 mbarriers + 4 anchors
-    return sizeof(float4) * ((size_t)2 * pb * wwin + 2 * pair_coef_f4(pb)) + sizeof(int) * 2 * pb +
-           4 * sizeof(uint64_t) + 4 * sizeof(df3);
+// Staged window per pulse: linear, wwin (value, difference) pairs of 16 bytes; nearest-bin, wwin + 2
+// plain 8-byte values starting at an even bin, so that every bulk copy starts on a 16-byte
+// boundary (the bin the window is centred on sits one value later when its start is odd).
+__host__ __device__ inline int win_elems(int wwin, int values) { return values ? wwin + 2 : wwin; }
+__host__ __device__ inline int win_elem_bytes(int values) { return values ? 8 : 16; }
+
+size_t bp_grid_ws_smem_bytes(int wwin, int pb, int values) {
+    // windows [2][pb][elems] + coefficient sets [2][pb/2][4] + base bins [2][pb] + 4 mbarriers + 4 anchors
+    return (size_t)2 * pb * win_elems(wwin, values) * win_elem_bytes(values) + sizeof(float4) * 2 * pair_coef_f4(pb) +
+           sizeof(int) * 2 * pb + 4 * sizeof(uint64_t) + 4 * sizeof(df3);
+}
+
+// First stored-span element a nearest-bin window copies for a pulse whose window is centred on
+// bin `base`: the window's first bin rounded down to even, kept inside [0, Lg - (wwin + 2)]
+// (*clamped when that moved it; Lg is even).
+__device__ __forceinline__ long value_window_start(int base, int wwin, int bg0, int Lg, bool* clamped) {
+    long g0 = ((long)base - wwin / 2 - bg0) & ~1L;
+    const long last = ((long)Lg - (wwin + 2)) & ~1L;
+    *clamped = g0 < 0 || g0 > last;
+    return g0 < 0 ? 0 : (g0 > last ? last : g0);
 }
 
 // ------------------------------------------- K2: two pulses per packed instruction
@@ -505,12 +528,16 @@ __device__ __forceinline__ void producer_coeffs_pair(const GridConst& g, const P
 // terms in di).  A quarter-warp's eight 16-byte window loads are conflict-free when they fall
 // in distinct 16-byte bank groups or on the same bin; lanes along the axis where bins change
 // slowly (cross-range) make them land on one or two bins.
-template <bool LANES_Y, bool PRECISE, bool NEAREST>
+template <bool LANES_Y, bool PRECISE, bool NEAREST, bool VALUES = false>
 __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const BpGridArgs a) {
     extern __shared__ __align__(16) float4 smem[];
     const int pb = a.pb, ww = a.wwin;
+    // VALUES (nearest-bin sampling with wide windows): windows of plain values, half the bytes of
+    // pairs, whose difference half nearest-bin sampling never reads.  A window's size in float4
+    // units: ww pairs, or (ww + 2) / 2 for ww + 2 values
+    const int wst = VALUES ? win_elems(ww, 1) / 2 : ww;
     float4* win0 = smem;
-    float4* coef0 = win0 + 2 * pb * ww;
+    float4* coef0 = win0 + 2 * pb * wst;
     int* base0 = reinterpret_cast<int*>(coef0 + 2 * pair_coef_f4(pb));
     uint64_t* bars = reinterpret_cast<uint64_t*>(base0 + 2 * pb);   // full[0..1], empty[2..3]
     df3* anchors = reinterpret_cast<df3*>(bars + 4);
@@ -554,29 +581,37 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
             const int s0 = (st0 + st) * pb, npb = min(pb, a.S - s0);
             float4* coef = coef0 + b * pair_coef_f4(pb);
             int* base = base0 + b * pb;
-            float4* win = win0 + (size_t)b * pb * ww;
+            float4* win = win0 + (size_t)b * pb * wst;
             int mine = 0;   // pulses of this stage staged by this warp
             for (int pass = 8 * pw; pass < npb; pass += 8 * kWsProducers) {
                 producer_coeffs_pair(g, a.pulses, s0, npb, pass, anchors, coef, base, lane, ww, a.flags);
                 mine += min(8, npb - pass);
                 if ((npb & 1) && npb - pass < 8) {   // this pass holds the padding pulse: zero its window
-                    float4* pw_ = win + (size_t)npb * ww;
-                    for (int e = lane; e < ww; e += 32) pw_[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+                    float4* pw_ = win + (size_t)npb * wst;
+                    for (int e = lane; e < wst; e += 32) pw_[e] = make_float4(0.f, 0.f, 0.f, 0.f);
                 }
             }
             __syncwarp();
-            if (lane == 0) mbar_arrive_expect_tx(&bars[b], (uint32_t)(mine * ww * sizeof(float4)));
+            if (lane == 0) mbar_arrive_expect_tx(&bars[b], (uint32_t)(mine * wst * sizeof(float4)));
             for (int pass = 8 * pw; pass < npb; pass += 8 * kWsProducers) {
                 const int pi = pass + lane;
                 if (lane < 8 && pi < npb) {
-                    long gi = (long)base[pi] - ww / 2 - a.bg0;
-                    if (gi < 0 || gi > (long)a.Lg - ww) {
-                        raise_flag(a.flags, FLAG_TILE_WINDOW);
-                        gi = gi < 0 ? 0 : (long)a.Lg - ww;
+                    const void* src;
+                    if (VALUES) {
+                        bool clamped;
+                        const long g0 = value_window_start(base[pi], ww, a.bg0, a.Lg, &clamped);
+                        if (clamped) raise_flag(a.flags, FLAG_TILE_WINDOW);
+                        src = reinterpret_cast<const float2*>(a.pairs) + (size_t)(s0 + pi) * a.Lg + g0;
+                    } else {
+                        long gi = (long)base[pi] - ww / 2 - a.bg0;
+                        if (gi < 0 || gi > (long)a.Lg - ww) {
+                            raise_flag(a.flags, FLAG_TILE_WINDOW);
+                            gi = gi < 0 ? 0 : (long)a.Lg - ww;
+                        }
+                        src = a.pairs + (size_t)(s0 + pi) * a.Lg + gi;
                     }
                     fence_proxy_async_smem();
-                    bulk_g2s(win + (size_t)pi * ww, a.pairs + (size_t)(s0 + pi) * a.Lg + gi,
-                             (uint32_t)(ww * sizeof(float4)), &bars[b]);
+                    bulk_g2s(win + (size_t)pi * wst, src, (uint32_t)(wst * sizeof(float4)), &bars[b]);
                 }
             }
             issued = st + 1;
@@ -617,7 +652,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
         }
         const int npp = (min(pb, a.S - (st0 + st) * pb) + 1) >> 1;
         const float4* coef = coef0 + b * pair_coef_f4(pb) + q * kPairSetF4;
-        const float4* win = win0 + (size_t)b * pb * ww;
+        const float4* win = win0 + (size_t)b * pb * wst;
         float2* st_re = acc2_re;
         float2* st_im = acc2_im;
 #pragma unroll 1
@@ -673,8 +708,16 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
             // the thread's phase constant mod 1 (once per pulse pair): its pixels' phases then stay
             // below ~5 cycles, which __sincosf's own argument reduction takes as is
             cph = fma2(f2(rintf(cph.x), rintf(cph.y)), M1, cph);
-            const float4* wa = win + (size_t)(2 * pp) * ww;
-            const float4* wb = wa + ww;
+            const float4* wa = win + (size_t)(2 * pp) * wst;
+            const float4* wb = wa + wst;
+            // nearest-bin value windows: the pulse's window start within its copy (0 or 1 value; a
+            // window clamped at the span's end is flagged, and the offset stays 0 or 1 regardless)
+            const float2 *va = nullptr, *vb = nullptr;
+            if (VALUES) {   // the copy starts at the window's first bin rounded down to even
+                const int* bp = base0 + b * pb + 2 * pp;
+                va = reinterpret_cast<const float2*>(wa) + ((bp[0] - ww / 2 - a.bg0) & 1);
+                vb = reinterpret_cast<const float2*>(wa + wst) + ((bp[1] - ww / 2 - a.bg0) & 1);
+            }
             // lanes along x: window addresses straight from the shifter's bits (index rint(v) +
             // ww / 2 = bits + idx_bias; 32-bit shared addresses, mod 2^32) with no clamp -- the
             // producers' bound on every set keeps the index in [0, ww - 1] (measured 4 % faster
@@ -691,7 +734,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
                 if (PRECISE) r1 = add2(r1, fma2(cid, d, ci));              // + the exact integer part
                 unsigned ia = 0, ib = 0;
                 uint32_t aa = 0, ab = 0;
-                if (LANES_Y) {
+                if (LANES_Y || VALUES) {
                     ia = min((unsigned)(__float_as_int(r1.x) + idx_bias), idx_max);
                     ib = min((unsigned)(__float_as_int(r1.y) + idx_bias), idx_max);
                 } else {
@@ -706,20 +749,31 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
                         if (fabsf(h ? s.y : s.x) <= kNearEdge || sp + h >= a.S) continue;
-                        const int g0 = min(max(base0[b * pb + 2 * pp + h] - ww / 2 - a.bg0, 0), a.Lg - ww);
+                        // the window's first bin: for value windows (index 0 of va / vb) unclamped -- a
+                        // clamped window is flagged, and the index below is clamped into the window
+                        // either way; for pair windows where the producer placed it
+                        const int g0 = VALUES ? base0[b * pb + 2 * pp + h] - ww / 2 - a.bg0
+                                              : min(max(base0[b * pb + 2 * pp + h] - ww / 2 - a.bg0, 0), a.Lg - ww);
                         const int gi = exact_grid_bin(a.steps, a.pulses, a.alpha2, g.s_r.hi, g.s_r.lo, a.bg0,
                                                       BIN_ADJ_NEAREST, px, py, k, sp + h);
                         const unsigned w = min((unsigned)(gi - g0), idx_max);
-                        if (LANES_Y) {
+                        if (LANES_Y || VALUES) {
                             if (h) ib = w; else ia = w;
                         } else {
                             if (h) ab = wb_s + 16u * w; else aa = wa_s + 16u * w;
                         }
                     }
                 }
-                const float4 pa = LANES_Y ? wa[ia] : lds_f4(aa), pq = LANES_Y ? wb[ib] : lds_f4(ab);
-                const float2 re = f2(fmaf(s.x, pa.z, pa.x), fmaf(s.y, pq.z, pq.x));
-                const float2 im = f2(fmaf(s.x, pa.w, pa.y), fmaf(s.y, pq.w, pq.y));
+                float2 re, im;
+                if (VALUES) {   // the bin's value, no interpolation
+                    const float2 pa = va[ia], pq = vb[ib];
+                    re = f2(pa.x, pq.x);
+                    im = f2(pa.y, pq.y);
+                } else {
+                    const float4 pa = LANES_Y ? wa[ia] : lds_f4(aa), pq = LANES_Y ? wb[ib] : lds_f4(ab);
+                    re = f2(fmaf(s.x, pa.z, pa.x), fmaf(s.y, pq.z, pq.x));
+                    im = f2(fmaf(s.x, pa.w, pa.y), fmaf(s.y, pq.w, pq.y));
+                }
                 const float2 x = mul2(ph, TWO_PI2);   // |ph| < ~5 cycles: no per-pixel reduction
                 float2 sn, cn;
                 __sincosf(x.x, &sn.x, &cn.x);
@@ -787,7 +841,9 @@ cudaError_t launch_bp_grid_ws(const BpGridArgs& a_in, cudaStream_t st) {
             cudaMemsetAsync(a.x, 0, sizeof(float2) * (size_t)a.g.nx * a.g.ny * a.g.nz, st);
         if (z != cudaSuccess) return z;
     }
-    const size_t smem = bp_grid_ws_smem_bytes(a.wwin, a.pb);
+    // value windows copy from even bins of rows of an even length (16-byte aligned)
+    if (a.values && (!a.nearest || (a.Lg & 1) || a.Lg < a.wwin + 2)) return cudaErrorInvalidValue;
+    const size_t smem = bp_grid_ws_smem_bytes(a.wwin, a.pb, a.values);
     const unsigned blocks = (unsigned)(tiles * a.parts);
     cudaError_t e;
     auto go = [&](auto kernel) -> cudaError_t {
@@ -798,7 +854,11 @@ cudaError_t launch_bp_grid_ws(const BpGridArgs& a_in, cudaStream_t st) {
     };
     if (a.nearest) {
         if (!a.g.precise_bins || !a.steps || !a.alpha2) return cudaErrorInvalidValue;
-        e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, true, true>) : go(bp_grid_ws_pair_kernel<false, true, true>);
+        if (a.values)
+            e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, true, true, true>)
+                          : go(bp_grid_ws_pair_kernel<false, true, true, true>);
+        else
+            e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, true, true>) : go(bp_grid_ws_pair_kernel<false, true, true>);
     } else if (a.g.precise_bins) {
         e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, true, false>) : go(bp_grid_ws_pair_kernel<false, true, false>);
     } else {
@@ -1399,8 +1459,16 @@ __global__ void __launch_bounds__(kPointThreads) bp_points_kernel(const PointArg
         float sr = 0.f, si = 0.f;
         for (int j = 0; j < n; ++j) {
             const PointEval e = eval_point(a, sp[j], sa2[j], pt);
-            const float4 pv = __ldg(pairs + (size_t)(s0 + j) * a.Lg + e.gi);
-            const float re = fmaf(e.sf, pv.z, pv.x), im = fmaf(e.sf, pv.w, pv.y);
+            float re, im;
+            if (a.values) {   // nearest-bin profiles stored as plain values (float2 rows)
+                const float2 pv = __ldg(reinterpret_cast<const float2*>(pairs) + (size_t)(s0 + j) * a.Lg + e.gi);
+                re = pv.x;
+                im = pv.y;
+            } else {
+                const float4 pv = __ldg(pairs + (size_t)(s0 + j) * a.Lg + e.gi);
+                re = fmaf(e.sf, pv.z, pv.x);
+                im = fmaf(e.sf, pv.w, pv.y);
+            }
             float sn, cn;
             __sincosf(SAR_TWO_PI * e.f, &sn, &cn);
             sr = fmaf(re, cn, fmaf(im, sn, sr));
@@ -1512,9 +1580,9 @@ __global__ void pack_adjoint_kernel(const float2* __restrict__ y, const float2* 
     spec[row * M + m] = make_spec<T>(v.x, v.y);
 }
 
-// pairs[s][w] for bin b = bg0 + w: (p(b) + 0.5 d, d) with d = p(b+1) - p(b), both scaled by
-// the pulse factor (linear); (p(b), 0) for nearest-bin sampling.  Bins wrap modulo M
-// (sarsolver_cxx.cpp:22-24).
+// pairs[s][w] for bin b = bg0 + w by `format` (kProfPairs...): linear, (p(b) + 0.5 d, d) with
+// d = p(b+1) - p(b), both scaled by the pulse factor; nearest, (p(b), 0); values, the scaled p(b)
+// alone in float2 rows of the same length.  Bins wrap modulo M (sarsolver_cxx.cpp:22-24).
 template <class T>
 __global__ void unpack_pairs_kernel(const T* __restrict__ spec, const float2* __restrict__ wfac,
                                     float4* __restrict__ pairs, long M, int Lg, long bg0, int first,
@@ -1527,16 +1595,18 @@ __global__ void unpack_pairs_kernel(const T* __restrict__ spec, const float2* __
     const float2 f = __ldg(wfac + first + row);
     const float2 a = to_f2(spec[row * M + m0]);
     const float2 p0 = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
-    float4 out;
-    if (linear) {
-        const float2 b = to_f2(spec[row * M + m1]);
-        const float2 p1 = make_float2(b.x * f.x - b.y * f.y, b.x * f.y + b.y * f.x);
-        const float dx = p1.x - p0.x, dy = p1.y - p0.y;
-        out = make_float4(fmaf(0.5f, dx, p0.x), fmaf(0.5f, dy, p0.y), dx, dy);
-    } else {
-        out = make_float4(p0.x, p0.y, 0.f, 0.f);
+    if (linear == kProfValues) {
+        reinterpret_cast<float2*>(pairs)[(size_t)(first + row) * Lg + w] = p0;
+        return;
     }
-    pairs[(size_t)(first + row) * Lg + w] = out;
+    if (linear == kProfNearestPairs) {
+        pairs[(size_t)(first + row) * Lg + w] = make_float4(p0.x, p0.y, 0.f, 0.f);
+        return;
+    }
+    const float2 b = to_f2(spec[row * M + m1]);
+    const float2 p1 = make_float2(b.x * f.x - b.y * f.y, b.x * f.y + b.y * f.x);
+    const float dx = p1.x - p0.x, dy = p1.y - p0.y;
+    pairs[(size_t)(first + row) * Lg + w] = make_float4(fmaf(0.5f, dx, p0.x), fmaf(0.5f, dy, p0.y), dx, dy);
 }
 
 // Stored span from the callback transform's compact output compact[row][w] (w = bin - bg0;
@@ -1558,16 +1628,18 @@ __global__ void unpack_compact_kernel(const float2* __restrict__ compact, int Lc
     const float2 f = __ldg(wfac + first + row);
     const float2 a = c[w0];
     const float2 p0 = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
-    float4 out;
-    if (linear) {
-        const float2 b = c[w1];
-        const float2 p1 = make_float2(b.x * f.x - b.y * f.y, b.x * f.y + b.y * f.x);
-        const float dx = p1.x - p0.x, dy = p1.y - p0.y;
-        out = make_float4(fmaf(0.5f, dx, p0.x), fmaf(0.5f, dy, p0.y), dx, dy);
-    } else {
-        out = make_float4(p0.x, p0.y, 0.f, 0.f);
+    if (linear == kProfValues) {   // float2 rows of values
+        reinterpret_cast<float2*>(pairs)[(size_t)(first + row) * Lg + w] = p0;
+        return;
     }
-    pairs[(size_t)(first + row) * Lg + w] = out;
+    if (linear == kProfNearestPairs) {
+        pairs[(size_t)(first + row) * Lg + w] = make_float4(p0.x, p0.y, 0.f, 0.f);
+        return;
+    }
+    const float2 b = c[w1];
+    const float2 p1 = make_float2(b.x * f.x - b.y * f.y, b.x * f.y + b.y * f.x);
+    const float dx = p1.x - p0.x, dy = p1.y - p0.y;
+    pairs[(size_t)(first + row) * Lg + w] = make_float4(fmaf(0.5f, dx, p0.x), fmaf(0.5f, dy, p0.y), dx, dy);
 }
 
 cudaError_t launch_unpack_compact(const float2* compact, int Lc, const float2* wfac, float4* pairs, float2* prof,
@@ -1925,21 +1997,24 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) upsample_pairs_kernel(
         __syncthreads();
     }
     const float2 f = __ldg(wfac + s);
-    float4* dst = pairs + s * Lg;
+    float4* dst = pairs + s * Lg;                                   // (value, difference) pairs
+    float2* vdst = reinterpret_cast<float2*>(pairs) + s * Lg;       // plain values
     for (int w = t; w < Lg; w += T) {
         const int r0 = (bmod + w) % U, r1 = (bmod + w + 1) % U;
         const float2 a = stage[r0 * C + w / U];
         const float2 p0 = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
-        float4 o;
-        if (linear) {
-            const float2 c = stage[r1 * C + (w + 1) / U];
-            const float2 p1 = make_float2(c.x * f.x - c.y * f.y, c.x * f.y + c.y * f.x);
-            const float dx = p1.x - p0.x, dy = p1.y - p0.y;
-            o = make_float4(fmaf(0.5f, dx, p0.x), fmaf(0.5f, dy, p0.y), dx, dy);
-        } else {
-            o = make_float4(p0.x, p0.y, 0.f, 0.f);
+        if (linear == kProfValues) {
+            vdst[w] = p0;
+            continue;
         }
-        dst[w] = o;
+        if (linear == kProfNearestPairs) {
+            dst[w] = make_float4(p0.x, p0.y, 0.f, 0.f);
+            continue;
+        }
+        const float2 c = stage[r1 * C + (w + 1) / U];
+        const float2 p1 = make_float2(c.x * f.x - c.y * f.y, c.x * f.y + c.y * f.x);
+        const float dx = p1.x - p0.x, dy = p1.y - p0.y;
+        dst[w] = make_float4(fmaf(0.5f, dx, p0.x), fmaf(0.5f, dy, p0.y), dx, dy);
     }
 }
 

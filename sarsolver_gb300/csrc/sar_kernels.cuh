@@ -20,6 +20,11 @@ enum : unsigned {
 // Clock budget of a bounded in-kernel wait (about 2 s at 2 GHz) unless a launch sets its own.
 constexpr long long kDefaultWaitBudgetCycles = 4000000000ll;
 
+// Stored profile formats (the `linear` argument of the upsampling writers): nearest-bin pairs
+// (value, 0) and linear pairs (value at mid-bin, difference), float4 rows; or plain values, float2
+// rows of even length, which nearest-bin plans with wide staged windows use (half the bytes).
+constexpr int kProfNearestPairs = 0, kProfLinearPairs = 1, kProfValues = 2;
+
 constexpr int kTile = 32;          // pixels per tile side
 constexpr int kThreads = 256;      // threads per tile CTA: 32 columns x 8 warps, 4 rows each
 constexpr int kMaxStagePulses = 32;
@@ -29,7 +34,8 @@ constexpr int kSetF4 = 6;          // float4 per (pulse, sub-tile) coefficient s
 struct BpGridArgs {
     GridConst g;
     const PulseGeom* pulses;   // [S]
-    const float4* pairs;       // [S][Lg]: (value at mid-bin, difference) per bin
+    const float4* pairs;       // [S][Lg]: (value at mid-bin, difference) per bin; with `values`, the
+                               //    plain values as float2 rows of even length Lg
     float2* x;                 // [P] image, (k*ny + j)*nx + i
     unsigned* flags;
     int S, Lg, bg0;            // stored profile span: bins [bg0, bg0 + Lg)
@@ -40,6 +46,7 @@ struct BpGridArgs {
     int accumulate;            // 1: x += result
     int lanes_y;               // 1: lanes of a warp run along y (chosen when bins change more slowly
                                //    along y than along x: fewer shared-memory bank conflicts)
+    int values = 0;            // 1 (with nearest): the profiles are plain values (kProfValues)
     int nearest;               // 1: nearest-bin pairs; bins near a rounding boundary are decided again
                                //    with the per-pixel double-float range (needs steps, alpha2)
     const double* steps;       // [9] grid steps ex, ey, ez (FP64), for those exact decisions
@@ -55,7 +62,7 @@ size_t bp_grid_smem_bytes(int wwin, int pb, int staged);
 cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st);
 // Warp-specialised variant: one producer warp computes coefficients and stages windows with
 // bulk copies into a double buffer while eight consumer warps gather (pb <= 32).
-size_t bp_grid_ws_smem_bytes(int wwin, int pb);
+size_t bp_grid_ws_smem_bytes(int wwin, int pb, int values);
 cudaError_t launch_bp_grid_ws(const BpGridArgs& a, cudaStream_t st);
 
 // Forward projection over a regular grid (K3): scatter into strip windows, merge globally.
@@ -93,6 +100,7 @@ struct PointArgs {
     int S, P, Lg, bg0;
     int linear;                // forward scatter weights: 1 linear, 0 nearest bin
     unsigned* flags;
+    int values = 0;            // 1: the backprojection's profiles are plain values (kProfValues)
 };
 cudaError_t launch_bp_points(const PointArgs& a, const float4* pairs, float2* x, int accumulate,
                              cudaStream_t st);

@@ -14,7 +14,10 @@
 //   pulse factors       S x 8 bytes (slow-time weight, conjugated for linear interpolation)
 //   grid steps          9 doubles, and antenna norms S x 16 bytes (nearest-bin decisions near a
 //                       rounding boundary are taken again exactly from these)
-//   profile pairs       S x span x 16 bytes (value at mid-bin, difference), fully rewritten
+//   profile pairs       S x span x 16 bytes (value at mid-bin, difference), fully rewritten; for
+//                       nearest-bin sampling with staged windows wider than 256 bins, as a plan
+//                       stores them, S x span' x 8 bytes of plain values (span' = span rounded
+//                       up to even, so that the staged copies stay 16-byte aligned)
 // Sizes beyond the array are rejected with SAR_ERR_INVALID_ARGUMENT and a message.
 //
 // All calls share the one array and it keeps the previous call's contents: calls that overlap
@@ -195,15 +198,21 @@ extern "C" int sar_adjoint_from_profiles_noalloc(const sar_geometry* g, const vo
     double* d_steps = reinterpret_cast<double*>(scratch + off_steps);
     float4* d_a2 = reinterpret_cast<float4*>(scratch + off_a2);
 
+    const bool values = !linear && wwin > 256;
+    const int lg_rows = values ? (int)(span + (span & 1)) : (int)span;
     cudaError_t e = cudaMemsetAsync(flags, 0, sizeof(unsigned), st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_table, table.data(), S * sizeof(PulseGeom), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_w, wfac.data(), S * sizeof(float2), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_steps, steps, sizeof steps, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_a2, a2.data(), S * sizeof(float4), cudaMemcpyHostToDevice, st);
+    // Pair rows of lg_rows entries (values: an even row length; a padding column when span is odd
+    // reads column 0 and lies outside every window, which the span check keeps in
+    // [first_bin, first_bin + span)).
     // Pairs over the caller's span: with M = span and first bin 0 the unpack kernel reads column
     // w and w + 1 of each row (the last column's difference wraps; it lies in the margin).
     if (e == cudaSuccess)
-        e = launch_unpack_pairs(prof_dev, 0, d_w, d_pairs, (long)span, (int)span, 0, (int)S, 0, linear ? 1 : 0, st);
+        e = launch_unpack_pairs(prof_dev, 0, d_w, d_pairs, (long)span, lg_rows, 0, (int)S, 0,
+                                values ? kProfValues : linear ? kProfLinearPairs : kProfNearestPairs, st);
     if (e == cudaSuccess) {
         BpGridArgs a;
         a.g = gc;
@@ -212,19 +221,20 @@ extern "C" int sar_adjoint_from_profiles_noalloc(const sar_geometry* g, const vo
         a.x = (float2*)x_dev;
         a.flags = flags;
         a.S = (int)S;
-        a.Lg = (int)span;
+        a.Lg = lg_rows;
         a.bg0 = (int)first_bin;
         a.wwin = wwin;
         a.accumulate = 0;
         a.nearest = linear ? 0 : 1;
+        a.values = values ? 1 : 0;
         a.steps = d_steps;
         a.alpha2 = d_a2;
         a.lanes_y = choose_lanes_y(g->transmit_posns, g->receive_posns, S, g->grid_origin, g->grid_step_x,
                                    g->grid_step_y, g->grid_step_z, nx, ny, nz);
         a.pb = 32;
         a.staged = 0;
-        for (int pb = 32; pb >= 2; pb /= 2)
-            if (bp_grid_ws_smem_bytes(wwin, pb) <= 110 * 1024) {
+        for (int pb = 32; pb >= 2; pb /= 2)   // as a plan chooses its stages
+            if (bp_grid_ws_smem_bytes(wwin, pb, a.values) <= 110 * 1024) {
                 a.pb = pb;
                 a.staged = 1;
                 break;

@@ -194,6 +194,31 @@ def test_gather_lane_layouts_match_oracle(turn, mode):
     assert plan.device_flags() == 0
 
 
+@pytest.mark.parametrize("turn", [0, 1])
+def test_value_windows_match_oracle(turn):
+    """nearest_ref at the reference's default upsample 128: staged windows wider than 256 bins,
+    which store and stage plain values (half the bytes of pairs), in both lane layouts, with an
+    odd pulse count and partial tiles, against the FP64 oracle (bins near a rounding boundary are
+    decided exactly, so the linear-mode tolerance holds)."""
+    rng = np.random.default_rng(41 + turn)
+    case = spotlight_case(37, 96, 70, 0.1, 4.0, upsample=128.0, weights=np.exp(1j * rng.uniform(-3, 3, 37)))
+    if turn:
+        ap = case.aperture
+        rot = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+        case.aperture = NumpySimpleSarAperture(ap.transmitter_positions @ rot.T, ap.receiver_positions @ rot.T,
+                                               ap.stab_ref_posns, ap.centre_frequency, ap.sample_bandwidth,
+                                               num_freqs=ap.num_freqs, slow_time_weighting=ap.slow_time_weighting)
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=128.0, interp="nearest_ref", path="grid")
+    assert plan.is_grid and plan.tile_window > 256 and plan.gather_lanes_y == (turn == 0)
+    y = crandn(rng, 37, 96)
+    e_a = rel_l2(gpu_adjoint(plan, y), oracle.adjoint(case.problem(), y, "nearest_ref", threads=8))
+    assert e_a < LINEAR_TOL, e_a
+    x = crandn(rng, case.scene.num_scatterers)
+    e_f = rel_l2(gpu_forward(plan, x), oracle.forward(case.problem(), x, "nearest_ref", threads=8))
+    assert e_f < LINEAR_TOL, e_f
+    assert plan.device_flags() == 0
+
+
 @pytest.mark.parametrize("mode,srp_shift,nf", [("linear", 0.0, 4096), ("nearest_ref", 0.0, 4096), ("linear", 1.0, 4096),
                                                ("linear", 0.0, 2048), ("linear", 0.0, 1024), ("nearest_ref", 1.0, 1024)])
 def test_fused_upsampling_matches_oracle(mode, srp_shift, nf):

@@ -54,13 +54,15 @@ def _noalloc(lib, g, prof, first, span, x):
     return fn(ctypes.byref(g), ctypes.c_void_p(prof.data_ptr()), first, span, ctypes.c_void_p(x.data_ptr()), stream)
 
 
-@pytest.mark.parametrize("interp", ["linear", "nearest_ref"])
-def test_noalloc_backprojection_matches_plan_twice(interp):
+@pytest.mark.parametrize("interp,upsample", [("linear", 8.0), ("nearest_ref", 8.0), ("nearest_ref", 128.0)])
+def test_noalloc_backprojection_matches_plan_twice(interp, upsample):
+    """Upsample 128 with nearest bins: staged windows wider than 256 bins, of plain values."""
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     lib = _lib.load()
     rng = np.random.default_rng(17)
-    case = spotlight_case(96, 256, 100, 0.5, 4.0, weights=np.exp(1j * rng.uniform(-1, 1, 96)))
+    case = spotlight_case(96, 256, 100, 0.5 if upsample == 8.0 else 0.1, 4.0, upsample=upsample,
+                          weights=np.exp(1j * rng.uniform(-1, 1, 96)))
     plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp=interp, path="grid")
     y = torch.from_numpy(crandn(rng, 96, 256)).to(torch.complex64).cuda()
     ref = plan.adjoint(y).cpu().numpy()
