@@ -1372,8 +1372,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                 continue;
             }
             float2* dst = a.acc + (size_t)(s0 + p) * a.Lg + gi;
-            atomicAdd(&dst->x, v.x);
-            atomicAdd(&dst->y, v.y);
+            atomicAdd(dst, v);   // one vector reduction for both components
         }
     }
 }
@@ -1802,14 +1801,24 @@ cudaError_t launch_unpack_pairs(const void* spec, int dbl, const float2* wfac, f
 // For N = 1024, 2048 or 4096 and M = U N (integer U): bin b = U j + r of the inverse length-M transform of the
 // zero-padded spectrum (frequencies k in [-N/2, N/2), X_k = conj(W) y at k mod N) is
 //   p(U j + r) = sum_k X_k e^{2 pi i k r / M} e^{2 pi i k j / N},
-// an N-point inverse DFT of the spectrum twiddled by e^{2 pi i k r / M}.  One CTA of N / 16
-// threads per pulse row computes the U such transforms in shared memory (Stockham: a radix-N/256
-// first pass on the 16 values each thread holds, then two radix-16 passes with one 16-point
-// butterfly per thread), keeps the bins of the stored span
-// [bg0, bg0 + Lg] (taken modulo M) and writes the (value, difference) pairs of
-// unpack_pairs_kernel directly: the row is read once (N values) and only the span is written,
-// where the unfused path writes and reads the M-point rows three times.  Twiddles come from
-// FP64-computed tables e^{2 pi i q / N} and e^{2 pi i q / M}.
+// an N-point inverse DFT of the spectrum twiddled by e^{2 pi i k r / M} (the same holds for any
+// integer r, r >= U giving the bins U (j + 1) + r - U).  One CTA of N / 16 threads per pulse row
+// computes the U such transforms in shared memory (Stockham: a radix-N/256 first pass on the 16
+// values each thread holds, then two radix-16 passes with one 16-point butterfly per thread),
+// keeps the bins of the stored span [bg0, bg0 + Lg] (taken modulo M) and writes the (value,
+// difference) pairs of unpack_pairs_kernel directly: the row is read once (N values) and only the
+// span is written, where the unfused path writes and reads the M-point rows three times.
+// Twiddles come from FP64-computed tables e^{2 pi i q / N} and e^{2 pi i q / M}, each transform's
+// e^{2 pi i k r / M} read from the table at k r mod M (no chained products, so any U keeps FP32
+// accuracy).
+//
+// Staged form (spans whose U residues fit shared memory): the span is gathered residue-major in
+// shared memory and written row-contiguously at the end.  Direct form (longer spans, i.e. large
+// U): transform q in [0, U) takes r = (bg0 mod U) + q, whose bins are exactly the span's bins
+// w = q + U i, and writes them straight to global memory at stride U; linear pairs of the bins of
+// transform q - 1 are written once transform q (their right neighbours) is known, from a
+// shared-memory copy of the previous transform's span values, and those of the last transform
+// from a copy of the first's.
 template <int N>
 struct UpShape {
     static constexpr int T = N / 16;     // threads per row: one radix-16 butterfly each
@@ -1931,6 +1940,14 @@ __device__ __forceinline__ void apply_powers(float2 (&v)[16], float2 w) {
     v[15] = cmulf(v[15], cmulf(w8, w7));
 }
 
+// Table index of e^{2 pi i k r / M} for the FFT-order index kp (signed frequency k = kp or kp - N)
+// and 0 <= r < 2U: |k r| < M < 2^30 (checked by the launchers), so one wrap suffices.
+template <int N>
+__device__ __forceinline__ int tw_index(int kp, int r, int M) {
+    const int kr = (kp < N / 2 ? kp : kp - N) * r;
+    return kr < 0 ? kr + M : kr;
+}
+
 // Radix-16 Stockham pass over N points (sub-transform length ns = N / 256 or N / 16 before it).
 template <int N>
 __device__ __forceinline__ void up_pass(const float2* in, float2* out, int ns, const float2* __restrict__ tw_n) {
@@ -1946,7 +1963,7 @@ __device__ __forceinline__ void up_pass(const float2* in, float2* out, int ns, c
     for (int r = 0; r < 16; ++r) out[up_pad(base + r * ns)] = v[r];
 }
 
-template <int N>
+template <int N, bool DIRECT>
 __global__ void __launch_bounds__(N / 16, 8192 / N) upsample_pairs_kernel(
     const float2* __restrict__ y, const float2* __restrict__ wave, const float2* __restrict__ wfac,
     const float2* __restrict__ tw_n, const float2* __restrict__ tw_m, float4* __restrict__ pairs, int U, long M,
@@ -1955,11 +1972,18 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) upsample_pairs_kernel(
     extern __shared__ __align__(16) float2 upsm[];
     float2* A = upsm;
     float2* B = upsm + up_pad(N);
-    // span bins bg0 .. bg0 + Lg (mod M), residue-major: bin w of residue r = (bg0 + w) mod U at
-    // stage[r C + w / U], C = 2 (mod 16) so that both the scatter and the pair reads avoid bank conflicts
+    // staged: span bins bg0 .. bg0 + Lg (mod M), residue-major: bin w of residue r = (bg0 + w) mod U
+    // at stage[r C + w / U], C = 2 (mod 16) so that both the scatter and the pair reads avoid bank
+    // conflicts.  Direct (linear pairs): the previous transform's and the first transform's span
+    // values, C each.
     float2* stage = upsm + 2 * up_pad(N);
+    float2* prev = stage;
+    float2* res0 = stage + C;
     const int t = threadIdx.x;
     const long s = (long)first + blockIdx.x;
+    const float2 f = __ldg(wfac + s);
+    float4* dst = pairs + s * Lg;                                   // (value, difference) pairs
+    float2* vdst = reinterpret_cast<float2*>(pairs) + s * Lg;       // plain values
     // this thread's spectrum values, k' = t + T e (FFT order index = k mod N)
     float2 X[16];
 #pragma unroll
@@ -1970,35 +1994,61 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) upsample_pairs_kernel(
         X[e] = make_float2(w.x * yv.x + w.y * yv.y, w.x * yv.y - w.y * yv.x);
     }
     const int bmod = (int)(((bg0 % U) + U) % U);
-    for (int r = 0; r < U; ++r) {
-        // pass 1 straight from registers: X holds the spectrum times e^{2 pi i k r / M} (advanced by
-        // one factor e^{2 pi i k / M} per r, read contiguously)
+    // direct: bin bg0 + q + U i = U (j0 + i) + bmod + q
+    const long j0 = (bg0 - bmod) / U;
+    for (int q = 0; q < U; ++q) {
+        const int r = DIRECT ? bmod + q : q;
+        // pass 1 straight from registers: the spectrum times e^{2 pi i k r / M}
         float2 v[16];
 #pragma unroll
-        for (int e = 0; e < 16; ++e) {
-            v[e] = X[e];
-            const int kp = t + T * e;
-            X[e] = cmulf(X[e], __ldg(tw_m + (kp < N / 2 ? kp : M - (N - kp))));
-        }
+        for (int e = 0; e < 16; ++e) v[e] = cmulf(X[e], __ldg(tw_m + tw_index<N>(t + T * e, r, (int)M)));
         up_first_pass<N>(v, A, t);
         __syncthreads();
         up_pass<N>(A, B, R0, tw_n);
         __syncthreads();
         up_pass<N>(B, A, 16 * R0, tw_n);
         __syncthreads();
-        // A holds p(U j + r) at j; keep the span's bins with this residue
-        int w0 = r - bmod;
-        if (w0 < 0) w0 += U;
-        for (int i = t; w0 + U * i <= Lg; i += T) {
-            long b = (bg0 + w0 + U * i) % M;
-            if (b < 0) b += M;
-            stage[r * C + i] = A[up_pad((int)(b / U))];
+        if (DIRECT) {
+            // A holds p(U j + r) at j: the span's bins w = q + U i, at j = j0 + i (mod N)
+            for (int i = t; q + U * i <= Lg; i += T) {
+                const int w = q + U * i;
+                const float2 a = A[up_pad((int)((j0 + i) & (N - 1)))];   // j mod N (N a power of two)
+                const float2 p1 = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
+                if (linear == kProfValues) {
+                    if (w < Lg) vdst[w] = p1;
+                } else if (linear == kProfNearestPairs) {
+                    if (w < Lg) dst[w] = make_float4(p1.x, p1.y, 0.f, 0.f);
+                } else {
+                    if (q == 0) {
+                        res0[i] = p1;
+                    } else if (w - 1 < Lg) {   // the pair of bin w - 1 (transform q - 1, same i)
+                        const float2 p0 = prev[i];
+                        const float dx = p1.x - p0.x, dy = p1.y - p0.y;
+                        dst[w - 1] = make_float4(fmaf(0.5f, dx, p0.x), fmaf(0.5f, dy, p0.y), dx, dy);
+                    }
+                    prev[i] = p1;
+                }
+            }
+        } else {
+            // A holds p(U j + r) at j; keep the span's bins with this residue
+            int w0 = r - bmod;
+            if (w0 < 0) w0 += U;
+            const long jb = (bg0 + w0 - r) / U;   // bin bg0 + w0 + U i = U (jb + i) + r
+            for (int i = t; w0 + U * i <= Lg; i += T) stage[r * C + i] = A[up_pad((int)((jb + i) & (N - 1)))];
         }
         __syncthreads();
     }
-    const float2 f = __ldg(wfac + s);
-    float4* dst = pairs + s * Lg;                                   // (value, difference) pairs
-    float2* vdst = reinterpret_cast<float2*>(pairs) + s * Lg;       // plain values
+    if (DIRECT) {
+        // linear pairs of the last transform's bins w = U - 1 + U i: right neighbour U (i + 1), the
+        // first transform's value i + 1
+        if (linear == kProfLinearPairs)
+            for (int i = t; U - 1 + U * i < Lg; i += T) {
+                const float2 p0 = prev[i], p1 = res0[i + 1];
+                const float dx = p1.x - p0.x, dy = p1.y - p0.y;
+                dst[U - 1 + U * i] = make_float4(fmaf(0.5f, dx, p0.x), fmaf(0.5f, dy, p0.y), dx, dy);
+            }
+        return;
+    }
     for (int w = t; w < Lg; w += T) {
         const int r0 = (bmod + w) % U, r1 = (bmod + w + 1) % U;
         const float2 a = stage[r0 * C + w / U];
@@ -2029,8 +2079,8 @@ static int up_stage_row(int Lg, int U) {
 // [-N/2, N/2) is  K(k) = sum_r e^{-2 pi i k r / M} DFT_N(a_r)[k mod N],  a_r[j] = a[U j + r]; each
 // forward DFT is computed as conj(inverse DFT(conj a_r)) with the Stockham passes above, and
 // y[(i + N/2) mod N] = W[i] f K(k_i) is written directly (replaces pack_forward + FFT + extract).
-// The twiddle e^{2 pi i k r / M} advances by one factor per r in registers; the accumulation
-// runs on the conjugate and is conjugated once at the end.
+// The twiddle e^{2 pi i k r / M} is read from the table at k r mod M; the accumulation runs on
+// the conjugate and is conjugated once at the end.
 template <int N>
 __global__ void __launch_bounds__(N / 16, 8192 / N) downsample_forward_kernel(
     const float2* __restrict__ acc, const float2* __restrict__ wave, const float2* __restrict__ wfac,
@@ -2044,12 +2094,9 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) downsample_forward_kernel(
     const long s = (long)first + blockIdx.x;
     const float2* arow = acc + s * Lg;
     const int bmod = (int)(((bg0 % U) + U) % U);
-    float2 Y[16], Z[16];   // conj of the output at k = t + T e, and e^{2 pi i k r / M}
+    float2 Y[16];   // conj of the output at k = t + T e
 #pragma unroll
-    for (int e = 0; e < 16; ++e) {
-        Y[e] = make_float2(0.f, 0.f);
-        Z[e] = make_float2(1.f, 0.f);
-    }
+    for (int e = 0; e < 16; ++e) Y[e] = make_float2(0.f, 0.f);
     for (int r = 0; r < U; ++r) {
         // conj(a_r) into A
         for (int e = t; e < up_pad(N); e += T) A[e] = make_float2(0.f, 0.f);
@@ -2072,14 +2119,13 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) downsample_forward_kernel(
         __syncthreads();
         up_pass<N>(A, B, 16 * R0, tw_n);
         __syncthreads();
-        // Y += e^{2 pi i k r / M} B[k]  (conjugate domain), then advance the twiddles
+        // Y += e^{2 pi i k r / M} B[k]  (conjugate domain)
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
             const int kp = t + T * e;
-            const float2 c = cmulf(Z[e], B[up_pad(kp)]);
+            const float2 c = cmulf(__ldg(tw_m + tw_index<N>(kp, r, (int)M)), B[up_pad(kp)]);
             Y[e].x += c.x;
             Y[e].y += c.y;
-            Z[e] = cmulf(Z[e], __ldg(tw_m + (kp < N / 2 ? kp : M - (N - kp))));
         }
         __syncthreads();
     }
@@ -2097,7 +2143,7 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) downsample_forward_kernel(
 static bool fused_fft_length(int N) { return N == 1024 || N == 2048 || N == 4096; }
 
 bool downsample_fused_supported(int N, long M, int Lg) {
-    return fused_fft_length(N) && M % N == 0 && M / N <= 64 && Lg >= 1 && Lg <= M;
+    return fused_fft_length(N) && M % N == 0 && M < (1L << 30) && Lg >= 1 && Lg <= M;
 }
 
 template <int N>
@@ -2121,13 +2167,19 @@ cudaError_t launch_downsample_forward_fused(const float2* acc, const float2* wav
     return launch_down_t<4096>(acc, wave, wfac, tw_n, tw_m, y, M, Lg, bg0, rows, first, st);
 }
 
+// Shared memory of the staged form (transform buffers and the residue-major span), and of the
+// direct form (transform buffers and two rows of span values for linear pairs).
 size_t upsample_fused_smem_bytes(int N, int Lg, int U) {
     return sizeof(float2) * ((size_t)2 * (N + N / 16) + (size_t)U * up_stage_row(Lg, U));
 }
+static size_t upsample_direct_smem_bytes(int N, int Lg, int U) {
+    return sizeof(float2) * ((size_t)2 * (N + N / 16) + (size_t)2 * up_stage_row(Lg, U));
+}
+constexpr size_t kUpSmemBudget = 112 * 1024;
 
 bool upsample_fused_supported(int N, long M, int Lg) {
-    return fused_fft_length(N) && M % N == 0 && M / N <= 64 && Lg >= 1 &&
-           upsample_fused_smem_bytes(N, Lg, (int)(M / N)) <= 112 * 1024;
+    return fused_fft_length(N) && M % N == 0 && M < (1L << 30) && Lg >= 1 && Lg <= M &&
+           upsample_direct_smem_bytes(N, Lg, (int)(M / N)) <= kUpSmemBudget;
 }
 
 template <int N>
@@ -2135,12 +2187,16 @@ static cudaError_t launch_up_t(const float2* y, const float2* wave, const float2
                                const float2* tw_m, float4* pairs, long M, int Lg, long bg0, int rows, int first,
                                int linear, cudaStream_t st) {
     const int U = (int)(M / N);
-    const size_t smem = upsample_fused_smem_bytes(N, Lg, U);
-    cudaError_t e = cudaFuncSetAttribute(upsample_pairs_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    upsample_pairs_kernel<N><<<rows, N / 16, smem, st>>>(y, wave, wfac, tw_n, tw_m, pairs, U, M, Lg, bg0, first,
-                                                         linear, up_stage_row(Lg, U));
-    return cudaGetLastError();
+    const bool staged = upsample_fused_smem_bytes(N, Lg, U) <= kUpSmemBudget;
+    const size_t smem = staged ? upsample_fused_smem_bytes(N, Lg, U) : upsample_direct_smem_bytes(N, Lg, U);
+    auto go = [&](auto kern) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        kern<<<rows, N / 16, smem, st>>>(y, wave, wfac, tw_n, tw_m, pairs, U, M, Lg, bg0, first, linear,
+                                         up_stage_row(Lg, U));
+        return cudaGetLastError();
+    };
+    return staged ? go(upsample_pairs_kernel<N, false>) : go(upsample_pairs_kernel<N, true>);
 }
 
 cudaError_t launch_upsample_pairs_fused(const float2* y, const float2* wave, const float2* wfac, const float2* tw_n,

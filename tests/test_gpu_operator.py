@@ -219,25 +219,35 @@ def test_value_windows_match_oracle(turn):
     assert plan.device_flags() == 0
 
 
-@pytest.mark.parametrize("mode,srp_shift,nf", [("linear", 0.0, 4096), ("nearest_ref", 0.0, 4096), ("linear", 1.0, 4096),
-                                               ("linear", 0.0, 2048), ("linear", 0.0, 1024), ("nearest_ref", 1.0, 1024)])
-def test_fused_upsampling_matches_oracle(mode, srp_shift, nf):
-    """N = 1024, 2048 or 4096 samples with U = 8: the range profiles come from the fused upsampling
-    kernel (eight N-point transforms per pulse, stored span only), and the forward projection
-    ends in the fused downsampling kernel (its transpose).  Against the FP64 oracle in both modes;
-    the stored span starts below bin 0 (taken modulo M), also with the SRP moved off the scene
-    centre."""
+@pytest.mark.parametrize("mode,srp_shift,nf,U", [("linear", 0.0, 4096, 8), ("nearest_ref", 0.0, 4096, 8),
+                                                 ("linear", 1.0, 4096, 8), ("linear", 0.0, 2048, 8),
+                                                 ("linear", 0.0, 1024, 8), ("nearest_ref", 1.0, 1024, 8),
+                                                 ("linear", 0.0, 1024, 128), ("nearest_ref", 1.0, 1024, 128),
+                                                 ("linear", 1.0, 2048, 128)])
+def test_fused_upsampling_matches_oracle(mode, srp_shift, nf, U):
+    """N = 1024, 2048 or 4096 samples: the range profiles come from the fused upsampling kernel
+    (U N-point transforms per pulse, stored span only), and the forward projection ends in the
+    fused downsampling kernel (its transpose).  Against the FP64 oracle in both modes; the stored
+    span starts below bin 0 (taken modulo M), also with the SRP moved off the scene centre.  At
+    U = 128 and N = 1024 the scene is wide enough that the span's U residues do not fit shared
+    memory: the upsampling writes each transform's bins straight to its row (direct form), nearest
+    bins as plain values; at N = 2048 (a narrower scene) they are staged."""
     rng = np.random.default_rng(31)
-    case = spotlight_case(48, nf, 48, 0.5, 3.0, weights=np.exp(1j * rng.uniform(-3, 3, 48)))
+    wide = U > 8 and nf == 1024
+    case = spotlight_case(48, nf, 48, 1.5 if wide else 0.25 if U > 8 else 0.5, 3.0, upsample=float(U),
+                          weights=np.exp(1j * rng.uniform(-3, 3, 48)))
     if srp_shift:
         ap = case.aperture
         srp = np.tile(np.array([12.0, -3.0, 0.0]), (48, 1))
         case.aperture = NumpySimpleSarAperture(ap.transmitter_positions, ap.receiver_positions, srp,
                                                ap.centre_frequency, ap.sample_bandwidth, num_freqs=nf,
                                                slow_time_weighting=ap.slow_time_weighting)
-    plan = SarPlan(case.scene, case.aperture, upsample_ratio=8.0, interp=mode)
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=float(U), interp=mode)
     assert plan.fused_upsampling and plan.fused_downsampling
     assert plan.profile_first_bin < 0
+    # direct form exactly when the residue-major staging would need more than the kernel's 112 KB
+    row = ((plan.profile_length + U) // U + 13) // 16 * 16 + 2
+    assert (8 * (2 * (nf + nf // 16) + U * row) > 112 * 1024) == wide
     y = crandn(rng, 48, nf)
     got = gpu_adjoint(plan, y)
     ref = oracle.adjoint(case.problem(), y, mode, threads=8)
