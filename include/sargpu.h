@@ -129,6 +129,9 @@ typedef struct sar_plan_info {
     int scatter_lanes_y;        /* 1: the grid forward scatter runs warp lanes along y and walks the
                                    tile along x (bins change more slowly along x), 0: lanes along x */
     size_t block_pulses;        /* streamed plan: pulses per block (0: resident plan) */
+    int scatter_shear;          /* m != 0: the grid forward scatter walks the rows of a sheared
+                                   lattice (steps ex, ey + m ex) that follow the iso-range lines,
+                                   for linear sampling of collections looking across the grid axes */
 } sar_plan_info;
 
 /* Create a plan on `device` (-1: the current device).  Copies all host inputs. */

@@ -95,7 +95,7 @@ class SarPlanInfo(ctypes.Structure):
         ("tile_window", c_size_t), ("strip_window", c_size_t), ("device_bytes", c_size_t), ("grid", c_int),
         ("interp", c_int), ("num_fast_times", c_size_t), ("num_slow_times", c_size_t), ("num_scatterers", c_size_t),
         ("device", c_int), ("fft_callbacks", c_int), ("gather_lanes_y", c_int), ("fused_upsampling", c_int), ("fused_downsampling", c_int),
-        ("scatter_lanes_y", c_int), ("block_pulses", c_size_t),
+        ("scatter_lanes_y", c_int), ("block_pulses", c_size_t), ("scatter_shear", c_int),
     ]
 
 
@@ -251,5 +251,11 @@ def load_host() -> ctypes.CDLL:
         lib.sar_bin_extent_host.argtypes = [P, P, P, P, c_int, c_int, c_int, P, P, P, c_double, c_double,
                                             ctypes.c_float, c_int, c_int, c_int, c_int, c_int, P]
         lib.sar_bin_extent_host.restype = c_int
+        lib.sar_geom_host_eval_sheared.argtypes = [P, P, P, P, c_int, c_int, c_int, c_size_t, P, P, P, c_double,
+                                                   c_double, ctypes.c_float, c_int, c_int, P, P]
+        lib.sar_choose_shear_host.argtypes = [P, P, c_size_t, P, P, P, P, c_int, c_int, c_int, c_double]
+        lib.sar_choose_shear_host.restype = c_int
+        lib.sar_parallelogram_distance_host.argtypes = [P, P, P, P, P, P]
+        lib.sar_parallelogram_distance_host.restype = None
         _HOST = lib
     return _HOST

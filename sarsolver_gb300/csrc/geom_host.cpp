@@ -17,13 +17,16 @@ using namespace sar;
 // transposed: the forward scatter's other layout, where a thread holds dj and walks di
 // (row_terms); otherwise a thread holds di and walks dj (column_terms), as the backprojection
 // and the default scatter layout do.
+// shear != 0: the forward scatter's sheared lattice (make_lattice_const); every lattice pixel that
+// is an image pixel writes that image pixel's entry.
 static int geom_host_eval(const double* origin, const double* ex, const double* ey, const double* ez, int nx,
                           int ny, int nz, size_t num_pulses, const double* tx, const double* rx,
                           const double* srp, double kappa, double s_r, float bin_offset, int precise_bins,
-                          bool transposed, float* phase_out, double* bin_out) {
+                          bool transposed, float* phase_out, double* bin_out, int shear = 0) {
     if (nx <= 0 || ny <= 0 || nz <= 0) return 1;
-    GridConst g = make_grid_const(ex, ey, ez, kappa, s_r, bin_offset, nx, ny, nz);
+    GridConst g = make_lattice_const(ex, ey, ez, kappa, s_r, bin_offset, nx, ny, nz, shear);
     g.precise_bins = precise_bins;
+    const int lnx = g.nx;   // lattice width
     const size_t P = (size_t)nx * ny * nz;
     for (size_t s = 0; s < num_pulses; ++s) {
         PulseGeom pg = make_pulse_geom(tx + 3 * s, rx + 3 * s, srp + 3 * s, origin);
@@ -35,7 +38,7 @@ static int geom_host_eval(const double* origin, const double* ex, const double* 
                     df vb[4];
                     df vsum = df_make(0.0f, 0.0f);
                     for (int q = 0; q < 4; ++q) {
-                        int ai = ti * 32 + 8 + 16 * (q & 1);
+                        int ai = ti * 32 + 8 + 16 * (q & 1) + g.a_off;
                         int aj = tj * 32 + 8 + 16 * (q >> 1);
                         df3 anchor = pixel_position(ai, aj, k, g);
                         ae[q] = expand_anchor(anchor, pg, g);
@@ -48,7 +51,9 @@ static int geom_host_eval(const double* origin, const double* ex, const double* 
                     for (int lj = 0; lj < 32; ++lj)
                         for (int li = 0; li < 32; ++li) {
                             int i = ti * 32 + li, j = tj * 32 + lj;
-                            if (i >= nx || j >= ny) continue;
+                            if (i >= lnx || j >= ny) continue;
+                            i += g.a_off + g.shear * j;   // the image pixel
+                            if (i < 0 || i >= nx) continue;
                             int q = (li >= 16) + 2 * (lj >= 16);
                             float di = (float)(li - 8 - 16 * (q & 1));
                             float dj = (float)(lj - 8 - 16 * (q >> 1));
@@ -99,6 +104,29 @@ extern "C" int sar_geom_host_eval_transposed(const double* origin, const double*
 }
 
 // Unstructured-position scheme: phase (cycles, [-0.5, 0.5]) and bin position per point.
+extern "C" int sar_geom_host_eval_sheared(const double* origin, const double* ex, const double* ey,
+                                         const double* ez, int nx, int ny, int nz, size_t num_pulses,
+                                         const double* tx, const double* rx, const double* srp, double kappa,
+                                         double s_r, float bin_offset, int precise_bins, int shear,
+                                         float* phase_out, double* bin_out) {
+    return geom_host_eval(origin, ex, ey, ez, nx, ny, nz, num_pulses, tx, rx, srp, kappa, s_r, bin_offset,
+                          precise_bins, false, phase_out, bin_out, shear);
+}
+
+// The forward scatter's shear choice (choose_shear) and the parallelogram distance bound of its
+// lattice strips, for tests.
+extern "C" int sar_choose_shear_host(const double* tx, const double* rx, size_t num_pulses, const double* origin,
+                                     const double* ex, const double* ey, const double* ez, int nx, int ny, int nz,
+                                     double s_r) {
+    return choose_shear(tx, rx, num_pulses, origin, ex, ey, ez, nx, ny, nz, s_r,
+                        choose_lanes_y(tx, rx, num_pulses, origin, ex, ey, ez, nx, ny, nz));
+}
+
+extern "C" void sar_parallelogram_distance_host(const double* a, const double* o, const double* e1, const double* e2,
+                                                double* dmin, double* dmax) {
+    parallelogram_distance_bounds(a, o, e1, e2, dmin, dmax);
+}
+
 extern "C" int sar_geom_host_eval_points(const double* origin, size_t num_points, const double* pos,
                                          size_t num_pulses, const double* tx, const double* rx,
                                          const double* srp, double kappa, double s_r,

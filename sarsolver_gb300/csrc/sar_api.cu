@@ -104,6 +104,7 @@ struct sar_plan {
     int Lg = 0;
     int wwin = 0, pb = 32;
     int lanes_y = 0;
+    bool fwd_transposed = false;   // forward scatter: lanes along y, rows walked along x
     bool staged = true;
     bool values = false;   // stored profiles are plain values (kProfValues), not pairs
     int seg_tiles = 0, segs_per_column = 0, ws = 0, pbf = 16;
@@ -497,11 +498,33 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
                 p->staged = true;
                 break;
             }
+        // Forward scatter layout: it walks the gather's lane axis (the transpose of its lane
+        // choice), or, for linear sampling across the grid axes, a sheared lattice whose rows
+        // follow the iso-range lines (choose_shear), walked with lanes along x.
+        p->fwd_transposed = !p->lanes_y;
+        const int shear = (p->interp == SAR_INTERP_LINEAR && !p->gc_fwd.precise_bins)
+                              ? choose_shear(tx, rx, S, origin, ex, ey, ez, nx, ny, nz, s_r, p->lanes_y)
+                              : 0;
+        double ey_f[3];
+        for (int c = 0; c < 3; ++c) ey_f[c] = ey[c] + shear * ex[c];
+        if (shear) {
+            const int precise = p->gc_fwd.precise_bins;
+            p->gc_fwd = make_lattice_const(ex, ey, ez, kappa, s_r, forward_bin_offset(p->interp), nx, ny, nz, shear);
+            p->gc_fwd.precise_bins = precise;
+            p->fwd_transposed = false;
+        }
         // Forward strips: lines of tiles along the axis the scatter walks (columns along y; rows
-        // along x for the transposed scatter, the gather's lanes along x), split into segments
-        // whose window fits shared memory.
-        const bool strips_x = !p->lanes_y;
-        const int lines = strips_x ? ty_tiles : tx_tiles, along = strips_x ? tx_tiles : ty_tiles;
+        // along x for the transposed scatter; lattice columns for a sheared lattice, only their
+        // tiles that hold image pixels), split into segments whose window fits shared memory.
+        const bool strips_x = p->fwd_transposed;
+        const int ftx = p->gc_fwd.tiles_x, fty = p->gc_fwd.tiles_y;
+        const int lines = strips_x ? fty : ftx;
+        std::vector<int> line_lo(lines, 0), line_hi(lines, (strips_x ? ftx : fty) - 1);
+        int along = 0;
+        for (int ln = 0; ln < lines; ++ln) {
+            if (!strips_x) lattice_tile_range(p->gc_fwd, ln, &line_lo[ln], &line_hi[ln]);
+            along = std::max(along, line_hi[ln] - line_lo[ln] + 1);
+        }
         p->forward_points = true;
         for (int pbf : {16, 8}) {
             int seg = along;
@@ -513,17 +536,32 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
                 for (int k = 0; k < nz; ++k)
                     for (int ln = 0; ln < lines; ++ln)
                         for (int sg = 0; sg < segs; ++sg) {
-                            const int t0 = sg * seg, t1 = std::min(t0 + seg, along);
+                            const int t0 = line_lo[ln] + sg * seg, t1 = std::min(t0 + seg, line_hi[ln] + 1);
+                            const size_t strip = ((size_t)k * lines + ln) * segs + sg;
+                            if (t0 >= t1) continue;   // no tile: the kernel's CTA leaves at once
                             const int ti0 = strips_x ? t0 : ln, tj0 = strips_x ? ln : t0;
                             const double nu = strips_x ? (t1 - t0) * kTile - 1.0 : kTile - 1.0;
                             const double nv = strips_x ? kTile - 1.0 : (t1 - t0) * kTile - 1.0;
                             double o[3];
                             for (int c = 0; c < 3; ++c)
-                                o[c] = origin[c] + ti0 * kTile * ex[c] + tj0 * kTile * ey[c] + k * ez[c];
-                            const size_t strip = ((size_t)k * lines + ln) * segs + sg;
+                                o[c] = origin[c] + (ti0 * kTile + p->gc_fwd.a_off) * ex[c] + tj0 * kTile * ey_f[c] +
+                                       k * ez[c];
                             for (size_t s = 0; s < S; ++s) {
                                 double lo, hi;
-                                region_range(tx + 3 * s, rx + 3 * s, srp + 3 * s, o, ex, ey, ez, nu, nv, 0.0, &lo, &hi);
+                                if (shear) {   // a parallelogram: the box bound assumes orthogonal edges
+                                    double e1[3], e2[3], a0, a1, b0, b1;
+                                    for (int c = 0; c < 3; ++c) {
+                                        e1[c] = nu * ex[c];
+                                        e2[c] = nv * ey_f[c];
+                                    }
+                                    parallelogram_distance_bounds(tx + 3 * s, o, e1, e2, &a0, &a1);
+                                    parallelogram_distance_bounds(rx + 3 * s, o, e1, e2, &b0, &b1);
+                                    const double ref = dist3(tx + 3 * s, srp + 3 * s) + dist3(rx + 3 * s, srp + 3 * s);
+                                    lo = a0 + b0 - ref;
+                                    hi = a1 + b1 - ref;
+                                } else {
+                                    region_range(tx + 3 * s, rx + 3 * s, srp + 3 * s, o, ex, ey, ez, nu, nv, 0.0, &lo, &hi);
+                                }
                                 const long b0 = (long)std::floor(lo * s_r) - 3;
                                 const long b1 = (long)std::ceil(hi * s_r) + 4;
                                 starts[strip * S + s] = (int)b0;
@@ -825,7 +863,8 @@ int sar_plan_get_info(const sar_plan* p, sar_plan_info* info) {
     info->gather_lanes_y = p->lanes_y;
     info->fused_upsampling = p->fused_up ? 1 : 0;
     info->fused_downsampling = p->fused_down ? 1 : 0;
-    info->scatter_lanes_y = (p->grid && !p->forward_points && !p->lanes_y) ? 1 : 0;
+    info->scatter_lanes_y = (p->grid && !p->forward_points && p->fwd_transposed) ? 1 : 0;
+    info->scatter_shear = (p->grid && !p->forward_points) ? p->gc_fwd.shear : 0;
     info->block_pulses = p->block;
     return SAR_OK;
 }
@@ -1000,8 +1039,8 @@ static int scatter_pulses(sar_plan* p, const float2* x, float2* acc, size_t firs
     a.pbf = p->pbf;
     a.linear = p->interp == SAR_INTERP_LINEAR;
     // the scatter walks the axis along which bins change slowly: the transpose of the gather's
-    // lane choice
-    a.transposed = p->lanes_y ? 0 : 1;
+    // lane choice, or the rows of a sheared lattice
+    a.transposed = p->fwd_transposed ? 1 : 0;
     a.steps = p->d_steps;
     a.alpha2 = p->d_alpha2 ? p->d_alpha2 + first : nullptr;
     SAR_CUDA(launch_fp_grid_ws(a, st), "forward scatter");

@@ -197,10 +197,35 @@ struct GridConst {
     df s_r;                      // bins per metre of bistatic range: fs*M/(N*c_eff)
     float bin_offset;            // -0.5 (linear: n = floor(v)) or +0.5 (adjoint nearest: ceil)
                                  // or 0 (forward nearest: round)
-    int nx, ny, nz;              // grid shape
+    int nx, ny, nz;              // grid shape (of the lattice, for a sheared one)
     int tiles_x, tiles_y;        // 32x32 tiles per plane
     int precise_bins;            // 1: integer/fraction split of the linear bin rates + cubic bin terms
+    // Sheared lattice (forward scatter only): lattice pixel (a, b) is image pixel
+    // (a + a_off + shear b, b), i.e. ey above holds the image's ey + shear ex, nx the lattice
+    // width img_nx + |shear| (ny - 1); 0, 0, nx for the image grid itself.
+    int a_off, shear, img_nx;
 };
+
+// Lattice tiles [lo, hi] of lattice column ta that hold at least one image pixel (all tiles of
+// the column when the lattice is the image grid); lo > hi when none does.
+SAR_HD void lattice_tile_range(const GridConst& g, int ta, int* lo, int* hi) {
+    *lo = 0;
+    *hi = g.tiles_y - 1;
+    if (g.shear == 0) return;
+    int first = g.tiles_y, last = -1;
+    for (int tb = 0; tb < g.tiles_y; ++tb) {
+        // image columns of the tile's pixels: a + a_off + shear b over a in [32 ta, 32 ta + 31],
+        // b in [32 tb, 32 tb + 31]
+        const int c0 = 32 * ta + g.a_off + g.shear * 32 * tb;
+        const int lo_c = c0 + (g.shear < 0 ? 31 * g.shear : 0), hi_c = c0 + 31 + (g.shear > 0 ? 31 * g.shear : 0);
+        if (lo_c <= g.img_nx - 1 && hi_c >= 0) {
+            first = first < tb ? first : tb;
+            last = tb;
+        }
+    }
+    *lo = first;
+    *hi = last;
+}
 
 // Coefficients of one (sub-tile, pulse) pair: 16 floats.
 //  phase (cycles): ph = c0 + c1 di + c2 dj + c3 di^2 + c4 di dj + c5 dj^2

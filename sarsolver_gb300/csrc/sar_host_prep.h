@@ -71,6 +71,24 @@ static inline GridConst make_grid_const(const double* ex, const double* ey, cons
     g.tiles_x = (nx + 31) / 32;
     g.tiles_y = (ny + 31) / 32;
     g.precise_bins = 0;
+    g.a_off = 0;
+    g.shear = 0;
+    g.img_nx = nx;
+    return g;
+}
+
+// Grid constants of the sheared lattice (steps ex, ey + shear ex) over an nx x ny x nz image:
+// lattice pixel (a, b) is image pixel (a + a_off + shear b, b), a in [0, nx + |shear| (ny - 1)).
+static inline GridConst make_lattice_const(const double* ex, const double* ey, const double* ez, double kappa,
+                                           double s_r, float bin_offset, int nx, int ny, int nz, int shear) {
+    if (shear == 0) return make_grid_const(ex, ey, ez, kappa, s_r, bin_offset, nx, ny, nz);
+    double ey_l[3];
+    for (int c = 0; c < 3; ++c) ey_l[c] = ey[c] + shear * ex[c];
+    GridConst g = make_grid_const(ex, ey_l, ez, kappa, s_r, bin_offset, nx + (shear < 0 ? -shear : shear) * (ny - 1),
+                                  ny, nz);
+    g.a_off = shear > 0 ? -shear * (ny - 1) : 0;
+    g.shear = shear;
+    g.img_nx = nx;
     return g;
 }
 
@@ -105,6 +123,95 @@ static inline void box_distance_bounds(const double* a, const double* o, const d
         if (d > best) best = d;
     }
     *dmax = best;
+}
+
+// Minimum and maximum distance from point a to the parallelogram {o + u e1 + v e2 : u, v in
+// [0, 1]} (e1, e2 the full edge vectors, not necessarily orthogonal): the minimum at the foot of
+// the perpendicular onto the plane when it lies inside, otherwise on one of the four edges; the
+// maximum at a corner (distance is convex).  Bounds the range window of a sheared lattice strip.
+static inline void parallelogram_distance_bounds(const double* a, const double* o, const double* e1,
+                                                 const double* e2, double* dmin, double* dmax) {
+    auto dot = [](const double* x, const double* y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
+    const double w[3] = {a[0] - o[0], a[1] - o[1], a[2] - o[2]};
+    const double g11 = dot(e1, e1), g12 = dot(e1, e2), g22 = dot(e2, e2);
+    const double det = g11 * g22 - g12 * g12;
+    double best = INFINITY;
+    if (det > 1e-12 * (g11 * g22 + 1e-300)) {
+        const double r1 = dot(e1, w), r2 = dot(e2, w);
+        const double u = (r1 * g22 - r2 * g12) / det, v = (r2 * g11 - r1 * g12) / det;
+        if (u >= 0.0 && u <= 1.0 && v >= 0.0 && v <= 1.0) {
+            double q[3];
+            for (int c = 0; c < 3; ++c) q[c] = o[c] + u * e1[c] + v * e2[c];
+            best = dist3(a, q);
+        }
+    }
+    if (!(best < INFINITY)) {
+        // edges p0 + t d, t in [0, 1]: (o, e1), (o + e1, e2), (o, e2), (o + e2, e1)
+        for (int edge = 0; edge < 4; ++edge) {
+            const double* from = edge == 1 ? e1 : edge == 3 ? e2 : nullptr;
+            const double* dir = (edge == 0 || edge == 3) ? e1 : e2;
+            double p0[3], d[3];
+            for (int c = 0; c < 3; ++c) {
+                p0[c] = o[c] + (from ? from[c] : 0.0);
+                d[c] = dir[c];
+            }
+            const double dd = dot(d, d);
+            const double pw[3] = {a[0] - p0[0], a[1] - p0[1], a[2] - p0[2]};
+            double t = dd > 0.0 ? dot(pw, d) / dd : 0.0;
+            t = t < 0.0 ? 0.0 : (t > 1.0 ? 1.0 : t);
+            double q[3];
+            for (int c = 0; c < 3; ++c) q[c] = p0[c] + t * d[c];
+            const double dist = dist3(a, q);
+            if (dist < best) best = dist;
+        }
+    }
+    *dmin = best;
+    double far = 0.0;
+    for (int corner = 0; corner < 4; ++corner) {
+        double q[3];
+        for (int c = 0; c < 3; ++c) q[c] = o[c] + ((corner & 1) ? e1[c] : 0.0) + ((corner & 2) ? e2[c] : 0.0);
+        const double dist = dist3(a, q);
+        if (dist > far) far = dist;
+    }
+    *dmax = far;
+}
+
+// Shear of the forward scatter's lattice (sar_geom.cuh GridConst): for linear sampling, where
+// the scatter's register run windows need a lane's bin to change by less than ~0.3 bins per
+// walked row, and collections that look across the grid axes (bins change alike along x and y,
+// e.g. along the diagonal).  The walk along lattice rows (steps ey + m ex) follows the iso-range
+// lines when m ex cancels the bin rate of ey.  Returns m in {-1, +1} when the walk rate of that
+// lattice over all pulses (at the scene centre) stays below kShearWalk bins per row while the
+// unsheared layout's does not and the lanes (along x) keep distinct bins; 0 otherwise.
+constexpr double kShearWalk = 0.25;
+static inline int choose_shear(const double* tx, const double* rx, size_t S, const double* origin,
+                               const double* ex, const double* ey, const double* ez, int nx, int ny, int nz,
+                               double s_r, int lanes_y) {
+    double c[3];
+    for (int d = 0; d < 3; ++d)
+        c[d] = origin[d] + 0.5 * ((nx - 1) * ex[d] + (ny - 1) * ey[d] + (nz - 1) * ez[d]);
+    double walk0 = 0.0, walk[2] = {0.0, 0.0}, lane_min = INFINITY;
+    for (size_t s = 0; s < S; ++s) {
+        double gx = 0.0, gy = 0.0;
+        for (int ant = 0; ant < 2; ++ant) {
+            const double* a = (ant ? rx : tx) + 3 * s;
+            const double w[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+            const double n = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+            if (!(n > 0.0)) return 0;
+            gx += (w[0] * ex[0] + w[1] * ex[1] + w[2] * ex[2]) / n;
+            gy += (w[0] * ey[0] + w[1] * ey[1] + w[2] * ey[2]) / n;
+        }
+        gx *= s_r;
+        gy *= s_r;
+        if (!isfinite(gx) || !isfinite(gy)) return 0;
+        walk0 = fmax(walk0, fabs(lanes_y ? gy : gx));   // the unsheared scatter walks the gather's lane axis
+        walk[0] = fmax(walk[0], fabs(gy - gx));
+        walk[1] = fmax(walk[1], fabs(gy + gx));
+        lane_min = fmin(lane_min, fabs(gx));
+    }
+    if (walk0 < kShearWalk || lane_min < 1.5) return 0;
+    const int m = walk[0] <= walk[1] ? -1 : 1;
+    return walk[m > 0] < kShearWalk ? m : 0;
 }
 
 // 1 when range bins change more slowly along the grid's y axis than along x, at the grid centre

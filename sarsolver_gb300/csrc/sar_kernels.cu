@@ -66,7 +66,7 @@ __device__ __forceinline__ TileThread tile_thread() {
 }
 
 __device__ __forceinline__ df3 subtile_anchor(int ti, int tj, int k, int q, const GridConst& g) {
-    return pixel_position(ti * kTile + 8 + 16 * (q & 1), tj * kTile + 8 + 16 * (q >> 1), k, g);
+    return pixel_position(ti * kTile + 8 + 16 * (q & 1) + g.a_off, tj * kTile + 8 + 16 * (q >> 1), k, g);
 }
 
 // One (pulse, sub-tile) coefficient set per thread of the first ceil(4 pb / 32) warps.
@@ -956,6 +956,7 @@ struct NearCtx {
     int bg0, i0, j0, k, transposed;
     int sp, sq;     // pulse indices
     int wsp, wsq;   // first bin (absolute) of each pulse's window
+    int a_off, shear;   // lattice pixel (i, j) is image pixel (i + a_off + shear j, j)
 };
 
 // 16 rows of one half tile for the pulse pair (p, q).  MODE 2: bins n, n+1 of different lanes
@@ -1022,7 +1023,8 @@ __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, 
                 fp = fabsf(ep.bp.s) > kNearEdge;
                 fq = TWO && fabsf(eq.bp.s) > kNearEdge;
                 if (fp || fq) {
-                    const int pi = nc.i0 + (nc.transposed ? rr : lane), pj = nc.j0 + (nc.transposed ? lane : rr);
+                    const int pj = nc.j0 + (nc.transposed ? lane : rr);
+                    const int pi = nc.i0 + (nc.transposed ? rr : lane) + nc.a_off + nc.shear * pj;
                     if (fp)
                         xp = min(max(exact_grid_bin(nc.steps, nc.pulses, nc.alpha2, nc.sr_hi, nc.sr_lo, nc.bg0,
                                                     BIN_FWD_NEAREST, pi, pj, nc.k, nc.sp) + nc.bg0 - nc.wsp, 0), ws - 1);
@@ -1194,8 +1196,12 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
     const int strip = (k * lines + line) * a.segs_per_column + seg;
     const int s0 = blockIdx.y * pbf;
     const int npb = min(pbf, a.S - s0);
-    const int t0 = seg * a.seg_tiles;
-    const int ntile = min(a.seg_tiles, along - t0);
+    // the line's tiles (on a sheared lattice only those holding image pixels) and this segment's
+    int t_lo = 0, t_hi = along - 1;
+    if (!TRANSPOSED) lattice_tile_range(g, line, &t_lo, &t_hi);
+    const int t0 = t_lo + seg * a.seg_tiles;
+    const int ntile = min(a.seg_tiles, t_hi + 1 - t0);
+    if (ntile <= 0) return;   // no tile: the whole CTA leaves before any barrier exists
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     for (int e = threadIdx.x; e < pbf * wslots; e += blockDim.x) win[e] = make_float2(0.f, 0.f);
@@ -1221,13 +1227,15 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
             }
             const int ti = TRANSPOSED ? t0 + t : line, tj = TRANSPOSED ? line : t0 + t;
             if (lane < 4) anchors[lane] = subtile_anchor(ti, tj, k, lane, g);
-            // this warp's half of the tile's image values (rows 16 pw .. 16 pw + 15)
+            // this warp's half of the tile's image values (rows 16 pw .. 16 pw + 15); lattice pixel
+            // (i, j) is image pixel (i + a_off + shear j, j), zero outside the image
             float2* xt = xt0 + b * kTile * kXtStride;
             const int i = ti * kTile + lane;
             for (int r = 16 * pw; r < 16 * pw + 16; ++r) {
                 const int j = tj * kTile + r;
-                const float2 xv =
-                    (i < g.nx && j < g.ny) ? a.x[((size_t)k * g.ny + j) * g.nx + i] : make_float2(0.f, 0.f);
+                const int ic = i + g.a_off + g.shear * j;
+                const float2 xv = (ic >= 0 && ic < g.img_nx && j < g.ny) ? a.x[((size_t)k * g.ny + j) * g.img_nx + ic]
+                                                                        : make_float2(0.f, 0.f);
                 xt[TRANSPOSED ? lane * kXtStride + r : r * kXtStride + lane] = xv;   // line = walked offset
             }
             __syncwarp();
@@ -1342,6 +1350,8 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                         nc.sq = s0 + pq;
                         nc.wsp = wst[p];
                         nc.wsq = wst[pq];
+                        nc.a_off = g.a_off;
+                        nc.shear = g.shear;
                     }
                     if (two)
                         scatter_half<LINEAR, PRECISE, true>(mode, ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq,

@@ -130,6 +130,7 @@ class SarPlan:
         self.fused_downsampling = bool(info.fused_downsampling)
         self.scatter_lanes_y = bool(info.scatter_lanes_y)
         self.block_pulses = int(info.block_pulses)
+        self.scatter_shear = int(info.scatter_shear)
         # The aperture's own weighting; phase corrections multiply it (autodiff.phase_weights).
         self.base_weights = torch.as_tensor(
             np.asarray(aperture.slow_time_weighting, dtype=np.complex64).reshape(-1)).to(self.device)

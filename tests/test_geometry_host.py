@@ -5,6 +5,8 @@ GPU, that their phase (cycles, mod 1) and range-bin position agree with FP64 ran
 the reference does (sarsolver_cxx.cpp:10-20, :283, :287) to well inside the 1e-5 relative-error
 budget, on the benchmark geometry at full size.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -352,3 +354,93 @@ def test_bin_extent_bounds_every_pixel_bin(precise):
                     lo, hi, vmin, vmax = out
                     assert lo - 1e-3 <= vmin and vmax <= hi + 1e-3, (s, ti, tj, q, out)
                     assert hi - lo < 1.2 * (vmax - vmin) + 4.0   # tight: the linear terms dominate
+
+
+def host_eval_sheared(scene, tx, rx, srp, kappa, s_r, shear, bin_offset=-0.5):
+    """The forward scatter's sheared-lattice evaluation, written at the image pixels (NaN where
+    no lattice pixel landed)."""
+    lib = _lib.load_host()
+    shape, origin, ex, ey, ez = grid_axes(scene)
+    nz, ny, nx = shape
+    S = tx.shape[0]
+    ph = np.full((S, nz * ny * nx), np.nan, np.float32)
+    bn = np.full((S, nz * ny * nx), np.nan)
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (origin, ex, ey, ez, tx, rx, srp)]
+    assert lib.sar_geom_host_eval_sheared(*[a.ctypes.data for a in arrs[:4]], nx, ny, nz, S,
+                                          *[a.ctypes.data for a in arrs[4:]], kappa, s_r, bin_offset, 0, shear,
+                                          ph.ctypes.data, bn.ctypes.data) == 0
+    return ph, bn
+
+
+def choose_shear(scene, tx, rx, s_r):
+    lib = _lib.load_host()
+    shape, origin, ex, ey, ez = grid_axes(scene)
+    nz, ny, nx = shape
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (tx, rx, origin, ex, ey, ez)]
+    return lib.sar_choose_shear_host(arrs[0].ctypes.data, arrs[1].ctypes.data, tx.shape[0],
+                                     *[a.ctypes.data for a in arrs[2:]], nx, ny, nz, s_r)
+
+
+@pytest.mark.parametrize("az,expect", [(0.0, 0), (90.0, 0), (45.0, -1), (135.0, 1), (-45.0, 1), (20.0, 0)])
+def test_scatter_shear_choice(az, expect):
+    """Linear sampling at upsample 8 on the benchmark image: collections along the grid axes keep
+    the plain layouts, those along a diagonal walk a lattice sheared by one pixel per row the
+    way that cancels the bin rate (-1 when range falls along +x and +y alike), and one at 20
+    degrees, whose iso-range slope is near neither, is left alone."""
+    tx = spotlight(4096, 5.0, centre_az_deg=az)
+    n, spacing = 2048, 0.25
+    scene = GridSarScene([1, n, n], [0.0, spacing * (n - 1), spacing * (n - 1)])
+    assert choose_shear(scene, tx, tx, 200.0e6 * 8 / C) == expect
+
+
+@pytest.mark.parametrize("az", [45.0, 135.0])
+def test_sheared_lattice_precision_and_walk(az):
+    """The benchmark image seen along a diagonal, on the sheared lattice the forward scatter
+    walks: every image pixel is evaluated exactly once, to the precision bounds of the plain
+    layouts against FP64, and a lattice row step (one row along y, `shear` pixels along x)
+    changes a pixel's bin by less than 0.32 anywhere (below 0.25 at the scene centre, where the
+    shear is chosen), the slow walk that lets the scatter's register run windows of 4 rows work
+    (3 steps below 0.98 bins; against 1.9 bins per pixel along either grid axis)."""
+    all_tx = spotlight(4096, 5.0, centre_az_deg=az)
+    tx = all_tx[[0, 2047, 4095]]
+    srp = np.zeros_like(tx)
+    n, spacing = 2048, 0.25
+    scene = GridSarScene([1, n, n], [0.0, spacing * (n - 1), spacing * (n - 1)])
+    kappa, s_r = 10.0e9 / C, 200.0e6 * 8 / C
+    m = choose_shear(scene, all_tx, all_tx, s_r)
+    assert m != 0
+    ph, bn = host_eval_sheared(scene, tx, tx, srp, kappa, s_r, m)
+    assert not np.isnan(bn).any() and not np.isnan(ph).any()
+    pos = scene.positions
+    for s in range(tx.shape[0]):
+        tp, tb = fp64_truth(tx[s], tx[s], srp[s], pos, kappa, s_r)
+        pmax, prms, bmax = errors(ph[s], bn[s] + 0.5, tp, tb)   # bin offset -1/2 of linear sampling
+        assert pmax < 1.0e-5 and prms < 1.5e-6 and bmax < 5.0e-5, (pmax, prms, bmax)
+        b = bn[s].reshape(n, n)   # [j, i]
+        walk = b[1:, max(m, 0):n + min(m, 0)] - b[:-1, max(-m, 0):n - max(m, 0)]
+        assert np.abs(walk).max() < 0.32, np.abs(walk).max()
+
+
+def test_parallelogram_distance_bounds():
+    """Exact minimum and maximum distance from a point to a (sheared) parallelogram, against dense
+    sampling: the minimum is never above the sampled one and within the sampling step of it, the
+    maximum is the farthest corner."""
+    lib = _lib.load_host()
+    rng = np.random.default_rng(3)
+    t = np.linspace(0.0, 1.0, 401)
+    uu, vv = np.meshgrid(t, t)
+    for trial in range(40):
+        o = rng.normal(size=3) * 10
+        e1 = rng.normal(size=3) * 5
+        e2 = e1 * rng.uniform(-1, 1) + rng.normal(size=3) * 5   # far from orthogonal
+        a = o + rng.normal(size=3) * (3 if trial % 2 else 30)
+        if trial % 3 == 0:   # a point right above the inside
+            a = o + 0.3 * e1 + 0.6 * e2 + np.cross(e1, e2) / np.linalg.norm(np.cross(e1, e2)) * 2.0
+        dmin, dmax = ctypes.c_double(), ctypes.c_double()
+        arrs = [np.ascontiguousarray(x, dtype=np.float64) for x in (a, o, e1, e2)]
+        lib.sar_parallelogram_distance_host(*[x.ctypes.data for x in arrs], ctypes.byref(dmin), ctypes.byref(dmax))
+        pts = o + uu[..., None] * e1 + vv[..., None] * e2
+        d = np.linalg.norm(pts - a, axis=-1)
+        step = (np.linalg.norm(e1) + np.linalg.norm(e2)) / 400
+        assert dmin.value <= d.min() + 1e-9 and dmin.value >= d.min() - step, (dmin.value, d.min())
+        assert abs(dmax.value - d.max()) < 1e-9

@@ -161,7 +161,7 @@ def test_linear_matches_fp64_oracle(kind):
 
 
 @pytest.mark.parametrize("mode", ["linear", "nearest_ref"])
-@pytest.mark.parametrize("turn", [0, 1, 0.5])
+@pytest.mark.parametrize("turn", [0, 1, 0.5, -0.5])
 def test_gather_lane_layouts_match_oracle(turn, mode):
     """The grid backprojection runs its lanes along the axis where range bins change slowly:
     along y for a collection looking along x, along x once the collection is turned by 90
@@ -170,8 +170,10 @@ def test_gather_lane_layouts_match_oracle(turn, mode):
     the grid path.  The forward projection of the same plans runs its lanes the other way (along
     the axis where bins change fast, walking the slow one): lanes along x, then lanes along y on
     a transposed tile once turned, with register run windows (linear) and single-bin
-    read-modify-writes (nearest) in both layouts.  turn = 0.5: looking along the grid diagonal,
-    where bins change alike along both axes (no run windows; two-phase read-modify-writes)."""
+    read-modify-writes (nearest) in both layouts.  turn = +-0.5: looking along a grid diagonal,
+    where bins change alike along both axes: linear sampling walks a lattice sheared by -+1 pixel
+    per row along the iso-range lines (register run windows again, partial lattice tiles at every
+    image edge), nearest sampling keeps the plain layout (two-phase read-modify-writes)."""
     rng = np.random.default_rng(21 + int(2 * turn))
     case = spotlight_case(37, 96, 70, 0.3, 4.0, weights=np.exp(1j * rng.uniform(-3, 3, 37)))
     if turn:
@@ -182,8 +184,9 @@ def test_gather_lane_layouts_match_oracle(turn, mode):
                                                ap.stab_ref_posns, ap.centre_frequency, ap.sample_bandwidth,
                                                num_freqs=ap.num_freqs, slow_time_weighting=ap.slow_time_weighting)
     plan = SarPlan(case.scene, case.aperture, upsample_ratio=case.upsample_ratio, interp=mode, path="grid")
-    if turn != 0.5:
+    if abs(turn) != 0.5:
         assert plan.gather_lanes_y == (turn == 0) and plan.scatter_lanes_y == (turn == 1)
+    assert plan.scatter_shear == ((-1 if turn > 0 else 1) if abs(turn) == 0.5 and mode == "linear" else 0)
     y = crandn(rng, 37, 96)
     tol = LINEAR_TOL   # nearest bins too: those near a rounding boundary are decided exactly
     e_a = rel_l2(gpu_adjoint(plan, y), oracle.adjoint(case.problem(), y, mode, threads=8))
