@@ -569,7 +569,8 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
                             }
                         }
                 const int ws = (need + 31) & ~31;
-                if (fp_grid_ws_smem_bytes(ws, pbf) <= kFpSmemBudget) {
+                if (fp_grid_ws_smem_bytes(ws, pbf, p->interp == SAR_INTERP_LINEAR && !p->gc_fwd.precise_bins) <=
+                    kFpSmemBudget) {
                     p->seg_tiles = seg;
                     p->segs_per_column = segs;
                     p->ws = ws;

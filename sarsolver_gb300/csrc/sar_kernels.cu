@@ -19,6 +19,8 @@
 // load gives a linearly interpolated sample.
 #include "sar_kernels.cuh"
 
+#include <type_traits>
+
 namespace sar {
 
 #define SAR_TWO_PI 6.28318530717958647692f
@@ -896,13 +898,14 @@ struct FpWsLayout {
     size_t win, coef, xt, base, fast, wst, bars, anchors, total;
 };
 
-__host__ __device__ inline FpWsLayout fp_ws_layout(int ws, int pbf) {
+// wide_x: image values staged as (re, re, im, im) (the linear run-window kernels), else (re, im).
+__host__ __device__ inline FpWsLayout fp_ws_layout(int ws, int pbf, int wide_x) {
     FpWsLayout L;
     L.win = 0;
     L.coef = L.win + (size_t)pbf * window_slots(ws) * sizeof(float2);
     L.coef = (L.coef + 15) & ~(size_t)15;
     L.xt = L.coef + (size_t)2 * pbf * 4 * kSetF4 * sizeof(float4);
-    L.base = L.xt + (size_t)2 * kTile * kXtStride * sizeof(float2);
+    L.base = L.xt + (size_t)2 * kTile * kXtStride * (wide_x ? sizeof(float4) : sizeof(float2));
     L.fast = L.base + (size_t)2 * pbf * sizeof(int);
     L.wst = L.fast + (size_t)2 * pbf * sizeof(int);
     L.bars = (L.wst + (size_t)pbf * sizeof(int) + 7) & ~(size_t)7;
@@ -911,7 +914,7 @@ __host__ __device__ inline FpWsLayout fp_ws_layout(int ws, int pbf) {
     return L;
 }
 
-size_t fp_grid_ws_smem_bytes(int ws, int pbf) { return fp_ws_layout(ws, pbf).total; }
+size_t fp_grid_ws_smem_bytes(int ws, int pbf, int wide_x) { return fp_ws_layout(ws, pbf, wide_x).total; }
 
 // Window slot of bin w: one padding slot every 16 bins, so lanes whose bins differ by a
 // multiple of 16 do not share a shared-memory bank pair.
@@ -946,6 +949,10 @@ __device__ __forceinline__ void rmw_add(float2* wp, int idx, float w, float cr, 
     *q = u;
 }
 
+// A staged image value: (re, im), or (re, re, im, im) for the linear run-window kernels.
+__device__ __forceinline__ float2 staged_value(const float2 v) { return v; }
+__device__ __forceinline__ float2 staged_value(const float4 v) { return make_float2(v.x, v.z); }
+
 // What the nearest-bin scatter needs to decide a bin again exactly (exact_grid_bin): the pixel of
 // row 0 / lane 0 of the half tile, the walk direction, both pulses and their window starts.
 struct NearCtx {
@@ -963,10 +970,10 @@ struct NearCtx {
 // disjoint (one phase per row); MODE 1: bins n distinct (two phases); MODE 0: atomics.  Nearest
 // bins within 5e-5 of a rounding boundary are decided again exactly; such a bin may equal a
 // neighbouring lane's, so those contributions go in with atomics in a phase of their own.
-template <bool LINEAR, bool PRECISE, int MODE, bool TWO>
+template <bool LINEAR, bool PRECISE, int MODE, bool TWO, typename XT>
 __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, float w9p, float ibp,
                                              const ColumnTerms& ctq, float c9q, float w9q, float ibq,
-                                             const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
+                                             const XT* xrow, float2* wp, float2* wq, int off_p, int off_q,
                                              int ws, int lane, const NearCtx& nc) {
     // the lane's phase constant and its rate along the rows mod 1 (rows are integer offsets)
     ColumnTerms cp = ctp, cq = ctq;
@@ -977,7 +984,7 @@ __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, 
 #pragma unroll 2
     for (int rr = 0; rr < 16; ++rr) {
         const float dj = (float)(rr - 8);
-        const float2 xv = xrow[rr * kXtStride + lane];
+        const float2 xv = staged_value(xrow[rr * kXtStride + lane]);
         const RowEval<PRECISE> ep = scatter_eval<PRECISE>(cp, c9p, w9p, ibp, dj, xv);
         const int ip = (int)min((unsigned)(ep.bp.n + off_p), (unsigned)(ws - 2));
         RowEval<PRECISE> eq;
@@ -1076,15 +1083,18 @@ constexpr float kRunSpan = 0.98f;
 
 template <bool TWO, int G>
 __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float c9p, const ColumnTerms& ctq, float c9q,
-                                                  const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
+                                                  const float4* xrow, float2* wp, float2* wq, int off_p, int off_q,
                                                   int ws, int lane) {
     // the lane's phase constant and its rate along the walked rows mod 1 (rows are integer offsets),
-    // so that each row's phase stays below ~5 cycles and goes to __sincosf without reduction
-    const float2 cph = f2(ctp.cph - rintf(ctp.cph), ctq.cph - rintf(ctq.cph));
-    const float2 b1 = f2(ctp.b1 - rintf(ctp.b1), ctq.b1 - rintf(ctq.b1)), b2 = f2(ctp.b2, ctq.b2), c9 = f2(c9p, c9q);
+    // so that each row's phase stays below ~5 cycles and goes to __sincosf without reduction; the
+    // phase polynomial then in radians (scaled once here, not per row)
+    const float2 TWO_PI2 = f2(SAR_TWO_PI, SAR_TWO_PI);
+    const float2 cph = mul2(f2(ctp.cph - rintf(ctp.cph), ctq.cph - rintf(ctq.cph)), TWO_PI2);
+    const float2 b1 = mul2(f2(ctp.b1 - rintf(ctp.b1), ctq.b1 - rintf(ctq.b1)), TWO_PI2);
+    const float2 b2 = mul2(f2(ctp.b2, ctq.b2), TWO_PI2), c9 = mul2(f2(c9p, c9q), TWO_PI2);
     const float2 cv = f2(ctp.cv, ctq.cv), bv1 = f2(ctp.bv1, ctq.bv1), bv2 = f2(ctp.bv2, ctq.bv2);
     const float2 SH = f2(SAR_SHIFTER, SAR_SHIFTER);
-    const float2 M1 = f2(-1.f, -1.f), TWO_PI2 = f2(SAR_TWO_PI, SAR_TWO_PI);
+    const float2 M1 = f2(-1.f, -1.f);
 #pragma unroll
   for (int g0 = 0; g0 < 16; g0 += G) {
     // window slot n0 of each pulse: the smaller bin of the group's first and last rows
@@ -1096,26 +1106,27 @@ __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float 
         n0p = min(max(min(__float_as_int(ra.x), __float_as_int(rb.x)) - SAR_SHIFTER_BITS + off_p, 0), ws - 3);
         n0q = min(max(min(__float_as_int(ra.y), __float_as_int(rb.y)) - SAR_SHIFTER_BITS + off_q, 0), ws - 3);
     }
-    // -(n0 + 1/2) in the frame of v (exact for |n0| < 2^22), so that a = v - (n0 + 1/2)
-    const float2 nc = f2(-((float)(n0p - off_p) + 0.5f), -((float)(n0q - off_q) + 0.5f));
+    // a = v - (n0 + 1/2): the bin polynomial's constant moved by -(n0 + 1/2) (exact for |n0| < 2^22)
+    const float2 cva = add2(cv, f2(-((float)(n0p - off_p) + 0.5f), -((float)(n0q - off_q) + 0.5f)));
     float2 Cr = f2(0.f, 0.f), Ci = f2(0.f, 0.f), Dr = f2(0.f, 0.f), Di = f2(0.f, 0.f);
     float2 Er = f2(0.f, 0.f), Ei = f2(0.f, 0.f);
 #pragma unroll 4
     for (int rr = g0; rr < g0 + G; ++rr) {
         const float dj = (float)(rr - 8);
         const float2 d = f2(dj, dj);
-        const float2 xv = xrow[rr * kXtStride + lane];
-        const float2 ph = fma2(fma2(fma2(c9, d, b2), d, b1), d, cph);
-        const float2 v = fma2(fma2(bv2, d, bv1), d, cv);
-        const float2 av = add2(v, nc);
+        // the pixel value staged as (re, re, im, im): both pulses' products packed
+        const float4 X = xrow[rr * kXtStride + lane];
+        const float2 XR = f2(X.x, X.y), XI = f2(X.z, X.w);
+        const float2 x = fma2(fma2(fma2(c9, d, b2), d, b1), d, cph);
+        const float2 av = fma2(fma2(bv2, d, bv1), d, cva);
         const float2 aa = f2(fabsf(av.x), fabsf(av.y));
-        const float2 x = mul2(ph, TWO_PI2);
         float2 sn, cn;
         __sincosf(x.x, &sn.x, &cn.x);
         __sincosf(x.y, &sn.y, &cn.y);
-        // c = x exp(+2 pi i f) for both pulses
-        const float2 cr = f2(fmaf(xv.x, cn.x, -xv.y * sn.x), fmaf(xv.x, cn.y, -xv.y * sn.y));
-        const float2 ci = f2(fmaf(xv.x, sn.x, xv.y * cn.x), fmaf(xv.x, sn.y, xv.y * cn.y));
+        // c = x exp(+i phase) for both pulses
+        const float2 xs = mul2(XI, sn);
+        const float2 cr = fma2(XR, cn, f2(-xs.x, -xs.y));
+        const float2 ci = fma2(XR, sn, mul2(XI, cn));
         Cr = add2(Cr, cr);
         Ci = add2(Ci, ci);
         Dr = fma2(av, cr, Dr);
@@ -1140,10 +1151,10 @@ __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float 
   }
 }
 
-template <bool LINEAR, bool PRECISE, bool TWO>
+template <bool LINEAR, bool PRECISE, bool TWO, typename XT>
 __device__ __forceinline__ void scatter_half(int mode, const ColumnTerms& ctp, float c9p, float w9p, float ibp,
                                              const ColumnTerms& ctq, float c9q, float w9q, float ibq,
-                                             const float2* xrow, float2* wp, float2* wq, int off_p, int off_q,
+                                             const XT* xrow, float2* wp, float2* wq, int off_p, int off_q,
                                              int ws, int lane, const NearCtx& nc) {
     if constexpr (LINEAR && !PRECISE) {
         if (mode == 5) {
@@ -1160,13 +1171,13 @@ __device__ __forceinline__ void scatter_half(int mode, const ColumnTerms& ctp, f
         }
     }
     if (mode >= 2)
-        scatter_rows<LINEAR, PRECISE, 2, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
+        scatter_rows<LINEAR, PRECISE, 2, TWO, XT>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
                                               nc);
     else if (mode == 1)
-        scatter_rows<LINEAR, PRECISE, 1, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
+        scatter_rows<LINEAR, PRECISE, 1, TWO, XT>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
                                               nc);
     else
-        scatter_rows<LINEAR, PRECISE, 0, TWO>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
+        scatter_rows<LINEAR, PRECISE, 0, TWO, XT>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
                                               nc);
 }
 
@@ -1174,10 +1185,12 @@ template <bool LINEAR, bool PRECISE, bool TRANSPOSED>
 __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridArgs a) {
     extern __shared__ __align__(16) unsigned char fsm[];
     const int pbf = a.pbf, ws = a.ws, wslots = window_slots(ws);
-    const FpWsLayout L = fp_ws_layout(ws, pbf);
+    constexpr bool WIDE_X = LINEAR && !PRECISE;
+    using XT = typename std::conditional<WIDE_X, float4, float2>::type;
+    const FpWsLayout L = fp_ws_layout(ws, pbf, WIDE_X);
     float2* win = reinterpret_cast<float2*>(fsm + L.win);
     float4* coef0 = reinterpret_cast<float4*>(fsm + L.coef);
-    float2* xt0 = reinterpret_cast<float2*>(fsm + L.xt);
+    XT* xt0 = reinterpret_cast<XT*>(fsm + L.xt);
     int* base0 = reinterpret_cast<int*>(fsm + L.base);
     int* fast0 = reinterpret_cast<int*>(fsm + L.fast);
     int* wst = reinterpret_cast<int*>(fsm + L.wst);
@@ -1229,14 +1242,19 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
             if (lane < 4) anchors[lane] = subtile_anchor(ti, tj, k, lane, g);
             // this warp's half of the tile's image values (rows 16 pw .. 16 pw + 15); lattice pixel
             // (i, j) is image pixel (i + a_off + shear j, j), zero outside the image
-            float2* xt = xt0 + b * kTile * kXtStride;
+            XT* xt = xt0 + b * kTile * kXtStride;
             const int i = ti * kTile + lane;
             for (int r = 16 * pw; r < 16 * pw + 16; ++r) {
                 const int j = tj * kTile + r;
                 const int ic = i + g.a_off + g.shear * j;
                 const float2 xv = (ic >= 0 && ic < g.img_nx && j < g.ny) ? a.x[((size_t)k * g.ny + j) * g.img_nx + ic]
                                                                         : make_float2(0.f, 0.f);
-                xt[TRANSPOSED ? lane * kXtStride + r : r * kXtStride + lane] = xv;   // line = walked offset
+                XT sv;   // (re, im), or (re, re, im, im)
+                if constexpr (WIDE_X)
+                    sv = make_float4(xv.x, xv.x, xv.y, xv.y);
+                else
+                    sv = xv;
+                xt[TRANSPOSED ? lane * kXtStride + r : r * kXtStride + lane] = sv;   // line = walked offset
             }
             __syncwarp();
             float4* coef = coef0 + b * pbf * 4 * kSetF4;
@@ -1312,7 +1330,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
         if (ok && !mbar_wait(&bars[b], (t >> 1) & 1, 32, 256)) ok = false;
         if (ok) {
             const float4* coef = coef0 + b * pbf * 4 * kSetF4;
-            const float2* xt = xt0 + b * kTile * kXtStride;
+            const XT* xt = xt0 + b * kTile * kXtStride;
             // Pulses are processed in pairs (p, p + 8): both share each image value and give the
             // warp two independent accumulation chains.
             for (int p = warp; p < npb; p += 2 * (kWsConsumers / 32)) {
@@ -1333,7 +1351,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                         load_column<PRECISE, TRANSPOSED>(coef + (p * 4 + qs) * kSetF4, tt, c9p, w9p, ibp);
                     const ColumnTerms ctq =
                         load_column<PRECISE, TRANSPOSED>(coef + (pq * 4 + qs) * kSetF4, tt, c9q, w9q, ibq);
-                    const float2* xrow = xt + 16 * half * kXtStride;
+                    const XT* xrow = xt + 16 * half * kXtStride;
                     NearCtx nc;
                     if (!LINEAR) {
                         nc.steps = a.steps;
@@ -1389,7 +1407,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
 
 template <bool LINEAR, bool PRECISE, bool TRANSPOSED>
 static cudaError_t launch_fp_grid_ws_t(const FpGridArgs& a, cudaStream_t st) {
-    const size_t smem = fp_grid_ws_smem_bytes(a.ws, a.pbf);
+    const size_t smem = fp_grid_ws_smem_bytes(a.ws, a.pbf, LINEAR && !PRECISE);
     const int lines = TRANSPOSED ? a.g.tiles_y : a.g.tiles_x;
     const dim3 grid((unsigned)(a.segs_per_column * lines * a.g.nz), (unsigned)((a.S + a.pbf - 1) / a.pbf));
     cudaError_t e = cudaFuncSetAttribute(fp_grid_ws_kernel<LINEAR, PRECISE, TRANSPOSED>,

@@ -87,7 +87,7 @@ struct FpGridArgs {
 // Warp-specialised variant: producer warps stage image tiles and coefficient sets; each
 // gathering warp owns whole pulses, so its windows need no atomics when bins along a row of
 // the tile are provably distinct (pbf <= 32, multiple of 8).
-size_t fp_grid_ws_smem_bytes(int ws, int pbf);
+size_t fp_grid_ws_smem_bytes(int ws, int pbf, int wide_x);   // wide_x: linear, not precise bins
 cudaError_t launch_fp_grid_ws(const FpGridArgs& a, cudaStream_t st);
 
 // Unstructured positions (K2/K3 point variants).
