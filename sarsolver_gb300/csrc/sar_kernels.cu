@@ -1849,9 +1849,11 @@ cudaError_t launch_unpack_pairs(const void* spec, int dbl, const float2* wfac, f
 // from a copy of the first's.
 template <int N>
 struct UpShape {
-    static constexpr int T = N / 16;     // threads per row: one radix-16 butterfly each
-    static constexpr int R0 = N / 256;   // radix of the first pass: 4, 8 or 16
-    static constexpr int NB = 16 / R0;   // first-pass butterflies per thread
+    static constexpr int T = N / 16;                // threads per row: one radix-16 butterfly each
+    static constexpr int P = N >= 8192 ? 3 : 2;     // radix-16 passes after the first
+    static constexpr int R0 = N / (P == 3 ? 4096 : 256);   // radix of the first pass: 2, 4, 8 or 16
+    static constexpr int NB = 16 / R0;              // first-pass butterflies per thread
+    static_assert(R0 >= 2 && R0 <= 16 && R0 * (P == 3 ? 4096 : 256) == N, "unsupported transform length");
 };
 
 __device__ __forceinline__ int up_pad(int x) { return x + (x >> 4); }   // one slot per 16: no bank conflicts
@@ -1936,13 +1938,17 @@ __device__ __forceinline__ void up_first_pass(const float2 (&x)[16], float2* out
             dft8_inv(v);
 #pragma unroll
             for (int m = 0; m < 8; ++m) out[up_pad(j * 8 + m)] = v[m];
-        } else {
+        } else if constexpr (R0 == 4) {
             float2 a = x[e1], b = x[e1 + NB], c = x[e1 + 2 * NB], d = x[e1 + 3 * NB];
             dft4_inv(a, b, c, d);
             out[up_pad(j * 4)] = a;
             out[up_pad(j * 4 + 1)] = b;
             out[up_pad(j * 4 + 2)] = c;
             out[up_pad(j * 4 + 3)] = d;
+        } else {
+            const float2 a = x[e1], b = x[e1 + NB];
+            out[up_pad(j * 2)] = make_float2(a.x + b.x, a.y + b.y);
+            out[up_pad(j * 2 + 1)] = make_float2(a.x - b.x, a.y - b.y);
         }
     }
 }
@@ -1991,12 +1997,29 @@ __device__ __forceinline__ void up_pass(const float2* in, float2* out, int ns, c
     for (int r = 0; r < 16; ++r) out[up_pad(base + r * ns)] = v[r];
 }
 
+// The radix-16 passes after the first (from `in`, ping-ponging with `tmp`): returns the buffer that
+// holds the transform.  The caller synchronises before; each pass ends with a barrier.
+template <int N>
+__device__ __forceinline__ float2* up_passes(float2* in, float2* tmp, const float2* __restrict__ tw_n) {
+    constexpr int R0 = UpShape<N>::R0;
+    up_pass<N>(in, tmp, R0, tw_n);
+    __syncthreads();
+    up_pass<N>(tmp, in, 16 * R0, tw_n);
+    __syncthreads();
+    if constexpr (UpShape<N>::P == 3) {
+        up_pass<N>(in, tmp, 256 * R0, tw_n);
+        __syncthreads();
+        return tmp;
+    }
+    return in;
+}
+
 template <int N, bool DIRECT>
 __global__ void __launch_bounds__(N / 16, 8192 / N) upsample_pairs_kernel(
     const float2* __restrict__ y, const float2* __restrict__ wave, const float2* __restrict__ wfac,
     const float2* __restrict__ tw_n, const float2* __restrict__ tw_m, float4* __restrict__ pairs, int U, long M,
     int Lg, long bg0, int first, int linear, int C) {
-    constexpr int T = UpShape<N>::T, R0 = UpShape<N>::R0;
+    constexpr int T = UpShape<N>::T;
     extern __shared__ __align__(16) float2 upsm[];
     float2* A = upsm;
     float2* B = upsm + up_pad(N);
@@ -2032,15 +2055,12 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) upsample_pairs_kernel(
         for (int e = 0; e < 16; ++e) v[e] = cmulf(X[e], __ldg(tw_m + tw_index<N>(t + T * e, r, (int)M)));
         up_first_pass<N>(v, A, t);
         __syncthreads();
-        up_pass<N>(A, B, R0, tw_n);
-        __syncthreads();
-        up_pass<N>(B, A, 16 * R0, tw_n);
-        __syncthreads();
+        const float2* F = up_passes<N>(A, B, tw_n);   // F[j] = p(U j + r)
         if (DIRECT) {
-            // A holds p(U j + r) at j: the span's bins w = q + U i, at j = j0 + i (mod N)
+            // the span's bins w = q + U i, at j = j0 + i (mod N)
             for (int i = t; q + U * i <= Lg; i += T) {
                 const int w = q + U * i;
-                const float2 a = A[up_pad((int)((j0 + i) & (N - 1)))];   // j mod N (N a power of two)
+                const float2 a = F[up_pad((int)((j0 + i) & (N - 1)))];   // j mod N (N a power of two)
                 const float2 p1 = make_float2(a.x * f.x - a.y * f.y, a.x * f.y + a.y * f.x);
                 if (linear == kProfValues) {
                     if (w < Lg) vdst[w] = p1;
@@ -2058,15 +2078,15 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) upsample_pairs_kernel(
                 }
             }
         } else {
-            // A holds p(U j + r) at j; keep the span's bins with this residue
+            // keep the span's bins with this residue
             int w0 = r - bmod;
             if (w0 < 0) w0 += U;
             const long jb = (bg0 + w0 - r) / U;   // bin bg0 + w0 + U i = U (jb + i) + r
-            for (int i = t; w0 + U * i <= Lg; i += T) stage[r * C + i] = A[up_pad((int)((jb + i) & (N - 1)))];
+            for (int i = t; w0 + U * i <= Lg; i += T) stage[r * C + i] = F[up_pad((int)((jb + i) & (N - 1)))];
         }
         __syncthreads();
     }
-    if (DIRECT) {
+    if constexpr (DIRECT) {
         // linear pairs of the last transform's bins w = U - 1 + U i: right neighbour U (i + 1), the
         // first transform's value i + 1
         if (linear == kProfLinearPairs)
@@ -2076,7 +2096,7 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) upsample_pairs_kernel(
                 dst[U - 1 + U * i] = make_float4(fmaf(0.5f, dx, p0.x), fmaf(0.5f, dy, p0.y), dx, dy);
             }
         return;
-    }
+    } else {
     for (int w = t; w < Lg; w += T) {
         const int r0 = (bmod + w) % U, r1 = (bmod + w + 1) % U;
         const float2 a = stage[r0 * C + w / U];
@@ -2093,6 +2113,7 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) upsample_pairs_kernel(
         const float2 p1 = make_float2(c.x * f.x - c.y * f.y, c.x * f.y + c.y * f.x);
         const float dx = p1.x - p0.x, dy = p1.y - p0.y;
         dst[w] = make_float4(fmaf(0.5f, dx, p0.x), fmaf(0.5f, dy, p0.y), dx, dy);
+    }
     }
 }
 
@@ -2114,7 +2135,7 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) downsample_forward_kernel(
     const float2* __restrict__ acc, const float2* __restrict__ wave, const float2* __restrict__ wfac,
     const float2* __restrict__ tw_n, const float2* __restrict__ tw_m, float2* __restrict__ y, int U, long M, int Lg,
     long bg0, int first) {
-    constexpr int T = UpShape<N>::T, R0 = UpShape<N>::R0;
+    constexpr int T = UpShape<N>::T;
     extern __shared__ __align__(16) float2 dnsm[];
     float2* A = dnsm;
     float2* B = dnsm + up_pad(N);
@@ -2143,15 +2164,12 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) downsample_forward_kernel(
         for (int e = 0; e < 16; ++e) v[e] = A[up_pad(t + T * e)];
         up_first_pass<N>(v, B, t);
         __syncthreads();
-        up_pass<N>(B, A, R0, tw_n);
-        __syncthreads();
-        up_pass<N>(A, B, 16 * R0, tw_n);
-        __syncthreads();
-        // Y += e^{2 pi i k r / M} B[k]  (conjugate domain)
+        const float2* F = up_passes<N>(B, A, tw_n);
+        // Y += e^{2 pi i k r / M} F[k]  (conjugate domain)
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
             const int kp = t + T * e;
-            const float2 c = cmulf(__ldg(tw_m + tw_index<N>(kp, r, (int)M)), B[up_pad(kp)]);
+            const float2 c = cmulf(__ldg(tw_m + tw_index<N>(kp, r, (int)M)), F[up_pad(kp)]);
             Y[e].x += c.x;
             Y[e].y += c.y;
         }
@@ -2168,7 +2186,10 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) downsample_forward_kernel(
     }
 }
 
-static bool fused_fft_length(int N) { return N == 1024 || N == 2048 || N == 4096; }
+static bool fused_fft_length(int N) { return N == 512 || N == 1024 || N == 2048 || N == 4096 || N == 8192; }
+
+// Shared memory a fused transform kernel may take: two CTAs per SM up to N = 4096, one for 8192.
+static size_t fused_smem_budget(int N) { return N >= 8192 ? 220 * 1024 : 112 * 1024; }
 
 bool downsample_fused_supported(int N, long M, int Lg) {
     return fused_fft_length(N) && M % N == 0 && M < (1L << 30) && Lg >= 1 && Lg <= M;
@@ -2190,9 +2211,11 @@ cudaError_t launch_downsample_forward_fused(const float2* acc, const float2* wav
                                             const float2* tw_n, const float2* tw_m, float2* y, int N, long M, int Lg,
                                             long bg0, int rows, int first, cudaStream_t st) {
     if (!downsample_fused_supported(N, M, Lg) || rows < 1) return cudaErrorInvalidValue;
+    if (N == 512) return launch_down_t<512>(acc, wave, wfac, tw_n, tw_m, y, M, Lg, bg0, rows, first, st);
     if (N == 1024) return launch_down_t<1024>(acc, wave, wfac, tw_n, tw_m, y, M, Lg, bg0, rows, first, st);
     if (N == 2048) return launch_down_t<2048>(acc, wave, wfac, tw_n, tw_m, y, M, Lg, bg0, rows, first, st);
-    return launch_down_t<4096>(acc, wave, wfac, tw_n, tw_m, y, M, Lg, bg0, rows, first, st);
+    if (N == 4096) return launch_down_t<4096>(acc, wave, wfac, tw_n, tw_m, y, M, Lg, bg0, rows, first, st);
+    return launch_down_t<8192>(acc, wave, wfac, tw_n, tw_m, y, M, Lg, bg0, rows, first, st);
 }
 
 // Shared memory of the staged form (transform buffers and the residue-major span), and of the
@@ -2203,11 +2226,9 @@ size_t upsample_fused_smem_bytes(int N, int Lg, int U) {
 static size_t upsample_direct_smem_bytes(int N, int Lg, int U) {
     return sizeof(float2) * ((size_t)2 * (N + N / 16) + (size_t)2 * up_stage_row(Lg, U));
 }
-constexpr size_t kUpSmemBudget = 112 * 1024;
-
 bool upsample_fused_supported(int N, long M, int Lg) {
     return fused_fft_length(N) && M % N == 0 && M < (1L << 30) && Lg >= 1 && Lg <= M &&
-           upsample_direct_smem_bytes(N, Lg, (int)(M / N)) <= kUpSmemBudget;
+           upsample_direct_smem_bytes(N, Lg, (int)(M / N)) <= fused_smem_budget(N);
 }
 
 template <int N>
@@ -2215,7 +2236,7 @@ static cudaError_t launch_up_t(const float2* y, const float2* wave, const float2
                                const float2* tw_m, float4* pairs, long M, int Lg, long bg0, int rows, int first,
                                int linear, cudaStream_t st) {
     const int U = (int)(M / N);
-    const bool staged = upsample_fused_smem_bytes(N, Lg, U) <= kUpSmemBudget;
+    const bool staged = upsample_fused_smem_bytes(N, Lg, U) <= fused_smem_budget(N);
     const size_t smem = staged ? upsample_fused_smem_bytes(N, Lg, U) : upsample_direct_smem_bytes(N, Lg, U);
     auto go = [&](auto kern) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -2231,9 +2252,11 @@ cudaError_t launch_upsample_pairs_fused(const float2* y, const float2* wave, con
                                         const float2* tw_m, float4* pairs, int N, long M, int Lg, long bg0, int rows,
                                         int first, int linear, cudaStream_t st) {
     if (!upsample_fused_supported(N, M, Lg) || rows < 1) return cudaErrorInvalidValue;
+    if (N == 512) return launch_up_t<512>(y, wave, wfac, tw_n, tw_m, pairs, M, Lg, bg0, rows, first, linear, st);
     if (N == 1024) return launch_up_t<1024>(y, wave, wfac, tw_n, tw_m, pairs, M, Lg, bg0, rows, first, linear, st);
     if (N == 2048) return launch_up_t<2048>(y, wave, wfac, tw_n, tw_m, pairs, M, Lg, bg0, rows, first, linear, st);
-    return launch_up_t<4096>(y, wave, wfac, tw_n, tw_m, pairs, M, Lg, bg0, rows, first, linear, st);
+    if (N == 4096) return launch_up_t<4096>(y, wave, wfac, tw_n, tw_m, pairs, M, Lg, bg0, rows, first, linear, st);
+    return launch_up_t<8192>(y, wave, wfac, tw_n, tw_m, pairs, M, Lg, bg0, rows, first, linear, st);
 }
 
 cudaError_t launch_unpack_profiles(const void* spec, int dbl, float2* prof, long M, int Lg, long bg0, int rows,

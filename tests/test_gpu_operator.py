@@ -222,23 +222,24 @@ def test_value_windows_match_oracle(turn):
     assert plan.device_flags() == 0
 
 
-@pytest.mark.parametrize("mode,srp_shift,nf,U", [("linear", 0.0, 4096, 8), ("nearest_ref", 0.0, 4096, 8),
-                                                 ("linear", 1.0, 4096, 8), ("linear", 0.0, 2048, 8),
-                                                 ("linear", 0.0, 1024, 8), ("nearest_ref", 1.0, 1024, 8),
-                                                 ("linear", 0.0, 1024, 128), ("nearest_ref", 1.0, 1024, 128),
-                                                 ("linear", 1.0, 2048, 128)])
-def test_fused_upsampling_matches_oracle(mode, srp_shift, nf, U):
-    """N = 1024, 2048 or 4096 samples: the range profiles come from the fused upsampling kernel
-    (U N-point transforms per pulse, stored span only), and the forward projection ends in the
-    fused downsampling kernel (its transpose).  Against the FP64 oracle in both modes; the stored
-    span starts below bin 0 (taken modulo M), also with the SRP moved off the scene centre.  At
-    U = 128 and N = 1024 the scene is wide enough that the span's U residues do not fit shared
-    memory: the upsampling writes each transform's bins straight to its row (direct form), nearest
-    bins as plain values; at N = 2048 (a narrower scene) they are staged."""
+@pytest.mark.parametrize("mode,srp_shift,nf,U,spacing,direct", [
+    ("linear", 0.0, 4096, 8, 0.5, False), ("nearest_ref", 0.0, 4096, 8, 0.5, False),
+    ("linear", 1.0, 4096, 8, 0.5, False), ("linear", 0.0, 2048, 8, 0.5, False),
+    ("linear", 0.0, 1024, 8, 0.5, False), ("nearest_ref", 1.0, 1024, 8, 0.5, False),
+    ("linear", 0.0, 512, 8, 0.5, False), ("nearest_ref", 1.0, 512, 8, 0.5, False),
+    ("linear", 0.0, 8192, 8, 0.5, False), ("linear", 1.0, 8192, 64, 1.5, True),
+    ("linear", 0.0, 1024, 128, 1.5, True), ("nearest_ref", 1.0, 1024, 128, 1.5, True),
+    ("linear", 1.0, 2048, 128, 0.25, False)])
+def test_fused_upsampling_matches_oracle(mode, srp_shift, nf, U, spacing, direct):
+    """N = 512 ... 8192 samples: the range profiles come from the fused upsampling kernel (U
+    N-point transforms per pulse: a radix-2, 4, 8 or 16 first pass and two or, at 8192, three
+    radix-16 passes; stored span only), and the forward projection ends in the fused downsampling
+    kernel (its transpose).  Against the FP64 oracle in both modes; the stored span starts below
+    bin 0 (taken modulo M), also with the SRP moved off the scene centre.  Where the scene is wide
+    enough that the span's U residues do not fit shared memory the upsampling writes each
+    transform's bins straight to its row (direct form; nearest bins as plain values at U = 128)."""
     rng = np.random.default_rng(31)
-    wide = U > 8 and nf == 1024
-    case = spotlight_case(48, nf, 48, 1.5 if wide else 0.25 if U > 8 else 0.5, 3.0, upsample=float(U),
-                          weights=np.exp(1j * rng.uniform(-3, 3, 48)))
+    case = spotlight_case(48, nf, 48, spacing, 3.0, upsample=float(U), weights=np.exp(1j * rng.uniform(-3, 3, 48)))
     if srp_shift:
         ap = case.aperture
         srp = np.tile(np.array([12.0, -3.0, 0.0]), (48, 1))
@@ -248,9 +249,11 @@ def test_fused_upsampling_matches_oracle(mode, srp_shift, nf, U):
     plan = SarPlan(case.scene, case.aperture, upsample_ratio=float(U), interp=mode)
     assert plan.fused_upsampling and plan.fused_downsampling
     assert plan.profile_first_bin < 0
-    # direct form exactly when the residue-major staging would need more than the kernel's 112 KB
+    # direct form exactly when the residue-major staging would need more than the kernel's shared
+    # memory (two CTAs per SM up to N = 4096, one at 8192)
     row = ((plan.profile_length + U) // U + 13) // 16 * 16 + 2
-    assert (8 * (2 * (nf + nf // 16) + U * row) > 112 * 1024) == wide
+    budget = (220 if nf >= 8192 else 112) * 1024
+    assert (8 * (2 * (nf + nf // 16) + U * row) > budget) == direct
     y = crandn(rng, 48, nf)
     got = gpu_adjoint(plan, y)
     ref = oracle.adjoint(case.problem(), y, mode, threads=8)
