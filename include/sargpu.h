@@ -132,6 +132,8 @@ typedef struct sar_plan_info {
     int scatter_shear;          /* m != 0: the grid forward scatter walks the rows of a sheared
                                    lattice (steps ex, ey + m ex) that follow the iso-range lines,
                                    for linear sampling of collections looking across the grid axes */
+    int gather_shear;           /* m != 0: the grid backprojection runs on a sheared lattice with warp
+                                   lanes along ey + m ex (collections looking across the grid axes) */
 } sar_plan_info;
 
 /* Create a plan on `device` (-1: the current device).  Copies all host inputs. */

@@ -96,6 +96,7 @@ class SarPlanInfo(ctypes.Structure):
         ("interp", c_int), ("num_fast_times", c_size_t), ("num_slow_times", c_size_t), ("num_scatterers", c_size_t),
         ("device", c_int), ("fft_callbacks", c_int), ("gather_lanes_y", c_int), ("fused_upsampling", c_int), ("fused_downsampling", c_int),
         ("scatter_lanes_y", c_int), ("block_pulses", c_size_t), ("scatter_shear", c_int),
+        ("gather_shear", c_int),
     ]
 
 
@@ -255,6 +256,9 @@ def load_host() -> ctypes.CDLL:
                                                    c_double, ctypes.c_float, c_int, c_int, P, P]
         lib.sar_choose_shear_host.argtypes = [P, P, c_size_t, P, P, P, P, c_int, c_int, c_int, c_double]
         lib.sar_choose_shear_host.restype = c_int
+        lib.sar_geom_host_eval_sheared_lanes.argtypes = lib.sar_geom_host_eval_sheared.argtypes
+        lib.sar_choose_gather_shear_host.argtypes = lib.sar_choose_shear_host.argtypes
+        lib.sar_choose_gather_shear_host.restype = c_int
         lib.sar_parallelogram_distance_host.argtypes = [P, P, P, P, P, P]
         lib.sar_parallelogram_distance_host.restype = None
         _HOST = lib

@@ -113,6 +113,23 @@ extern "C" int sar_geom_host_eval_sheared(const double* origin, const double* ex
                           precise_bins, false, phase_out, bin_out, shear);
 }
 
+// The same lattice in the backprojection's layout there (a thread holds the offset along the
+// lattice's second axis, its lanes' axis, and evaluates along x).
+extern "C" int sar_geom_host_eval_sheared_lanes(const double* origin, const double* ex, const double* ey,
+                                               const double* ez, int nx, int ny, int nz, size_t num_pulses,
+                                               const double* tx, const double* rx, const double* srp, double kappa,
+                                               double s_r, float bin_offset, int precise_bins, int shear,
+                                               float* phase_out, double* bin_out) {
+    return geom_host_eval(origin, ex, ey, ez, nx, ny, nz, num_pulses, tx, rx, srp, kappa, s_r, bin_offset,
+                          precise_bins, true, phase_out, bin_out, shear);
+}
+
+extern "C" int sar_choose_gather_shear_host(const double* tx, const double* rx, size_t num_pulses,
+                                            const double* origin, const double* ex, const double* ey,
+                                            const double* ez, int nx, int ny, int nz, double s_r) {
+    return choose_gather_shear(tx, rx, num_pulses, origin, ex, ey, ez, nx, ny, nz, s_r);
+}
+
 // The forward scatter's shear choice (choose_shear) and the parallelogram distance bound of its
 // lattice strips, for tests.
 extern "C" int sar_choose_shear_host(const double* tx, const double* rx, size_t num_pulses, const double* origin,

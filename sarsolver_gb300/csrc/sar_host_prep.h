@@ -184,6 +184,39 @@ static inline void parallelogram_distance_bounds(const double* a, const double* 
 // lattice over all pulses (at the scene centre) stays below kShearWalk bins per row while the
 // unsheared layout's does not and the lanes (along x) keep distinct bins; 0 otherwise.
 constexpr double kShearWalk = 0.25;
+
+// Shear of the backprojection's lattice: its lanes run along the lattice's second axis (steps
+// ey + m ex), so that a quarter-warp's window loads land on one or two bins and are broadcast.
+// Returns m in {-1, +1} when the better plain lane axis still changes by more than half a bin per
+// pixel over the pulses (bank-conflicted loads: collections looking across the grid axes) and the
+// sheared axis changes by less than half of that; 0 otherwise.
+static inline int choose_gather_shear(const double* tx, const double* rx, size_t S, const double* origin,
+                                      const double* ex, const double* ey, const double* ez, int nx, int ny, int nz,
+                                      double s_r) {
+    double c[3];
+    for (int d = 0; d < 3; ++d)
+        c[d] = origin[d] + 0.5 * ((nx - 1) * ex[d] + (ny - 1) * ey[d] + (nz - 1) * ez[d]);
+    double ax = 0.0, ay = 0.0, am[2] = {0.0, 0.0};
+    for (size_t s = 0; s < S; ++s) {
+        double gx = 0.0, gy = 0.0;
+        for (int ant = 0; ant < 2; ++ant) {
+            const double* a = (ant ? rx : tx) + 3 * s;
+            const double w[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+            const double n = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+            if (!(n > 0.0)) return 0;
+            gx += (w[0] * ex[0] + w[1] * ex[1] + w[2] * ex[2]) / n;
+            gy += (w[0] * ey[0] + w[1] * ey[1] + w[2] * ey[2]) / n;
+        }
+        if (!isfinite(gx) || !isfinite(gy)) return 0;
+        ax = fmax(ax, fabs(gx) * s_r);
+        ay = fmax(ay, fabs(gy) * s_r);
+        am[0] = fmax(am[0], fabs(gy - gx) * s_r);
+        am[1] = fmax(am[1], fabs(gy + gx) * s_r);
+    }
+    const double plain = fmin(ax, ay);
+    const int m = am[0] <= am[1] ? -1 : 1;
+    return (plain > 0.5 && am[m > 0] < 0.5 * plain) ? m : 0;
+}
 static inline int choose_shear(const double* tx, const double* rx, size_t S, const double* origin,
                                const double* ex, const double* ey, const double* ez, int nx, int ny, int nz,
                                double s_r, int lanes_y) {

@@ -322,6 +322,7 @@ static cudaError_t launch_bp_grid_t(const BpGridArgs& a, cudaStream_t st) {
 }
 
 cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st) {
+    if (a.g.shear) return cudaErrorInvalidValue;   // sheared lattices run on the staged gather only
     if (a.nearest) {
         if (!a.g.precise_bins || !a.steps || !a.alpha2) return cudaErrorInvalidValue;
         return launch_bp_grid_t<true, true>(a, st);
@@ -530,7 +531,9 @@ __device__ __forceinline__ void producer_coeffs_pair(const GridConst& g, const P
 // terms in di).  A quarter-warp's eight 16-byte window loads are conflict-free when they fall
 // in distinct 16-byte bank groups or on the same bin; lanes along the axis where bins change
 // slowly (cross-range) make them land on one or two bins.
-template <bool LANES_Y, bool PRECISE, bool NEAREST, bool VALUES = false>
+// SHEARED: the tiles are those of a sheared lattice (GridConst.shear; linear sampling, lanes
+// along its second axis), written through the shear to the image.
+template <bool LANES_Y, bool PRECISE, bool NEAREST, bool VALUES = false, bool SHEARED = false>
 __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const BpGridArgs a) {
     extern __shared__ __align__(16) float4 smem[];
     const int pb = a.pb, ww = a.wwin;
@@ -551,6 +554,11 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
     tile /= g.tiles_y;
     const int ti = tile % g.tiles_x;
     const int k = tile / g.tiles_x;
+    if constexpr (SHEARED) {   // a lattice tile without image pixels leaves before any barrier exists
+        int lo, hi;
+        lattice_tile_range(g, ti, &lo, &hi);
+        if (tj < lo || tj > hi) return;
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x < 4) anchors[threadIdx.x] = subtile_anchor(ti, tj, k, threadIdx.x, g);
     if (threadIdx.x == 0) {
@@ -744,9 +752,10 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
                     ab = wb_b + ((uint32_t)__float_as_int(r1.y) << 4);
                 }
                 if (NEAREST && (fabsf(s.x) > kNearEdge || fabsf(s.y) > kNearEdge)) {
-                    // near a rounding boundary: the exact bin, as a window index of the pulse
-                    const int px = ti * kTile + (LANES_Y ? 4 * warp + r : lane);
+                    // near a rounding boundary: the exact bin, as a window index of the pulse (of the
+                    // image pixel, on a sheared lattice)
                     const int py = tj * kTile + (LANES_Y ? lane : 4 * warp + r);
+                    const int px = ti * kTile + (LANES_Y ? 4 * warp + r : lane) + (SHEARED ? g.a_off + g.shear * py : 0);
                     const int sp = (st0 + st) * pb + 2 * pp;
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
@@ -798,10 +807,11 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
     }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-        const int i = ti * kTile + (LANES_Y ? 4 * warp + r : lane);
+        // lattice pixel (a, j) is image pixel (a + a_off + shear j, j)
         const int j = tj * kTile + (LANES_Y ? lane : 4 * warp + r);
-        if (i < g.nx && j < g.ny) {
-            const size_t p = ((size_t)k * g.ny + j) * g.nx + i;
+        const int i = ti * kTile + (LANES_Y ? 4 * warp + r : lane) + (SHEARED ? g.a_off + g.shear * j : 0);
+        if ((SHEARED ? (i >= 0 && i < g.img_nx) : i < g.nx) && j < g.ny) {
+            const size_t p = ((size_t)k * g.ny + j) * (SHEARED ? g.img_nx : g.nx) + i;
             if (a.parts > 1) {   // the image was zeroed by the launcher (parts > 1 never accumulates)
                 atomicAdd(&a.x[p].x, acc_re[r]);
                 atomicAdd(&a.x[p].y, acc_im[r]);
@@ -837,10 +847,10 @@ cudaError_t launch_bp_grid_ws(const BpGridArgs& a_in, cudaStream_t st) {
     if (a_in.pb < 1 || a_in.pb > 32 || a_in.wwin < 4 || (a_in.wwin & 3)) return cudaErrorInvalidValue;
     BpGridArgs a = a_in;
     const long tiles = (long)a.g.tiles_x * a.g.tiles_y * a.g.nz;
-    a.parts = ws_parts(tiles, (a.S + a.pb - 1) / a.pb, a.accumulate);
+    a.parts = ws_parts(a.tiles_valid > 0 ? a.tiles_valid : tiles, (a.S + a.pb - 1) / a.pb, a.accumulate);
     if (a.parts > 1) {
         const cudaError_t z =
-            cudaMemsetAsync(a.x, 0, sizeof(float2) * (size_t)a.g.nx * a.g.ny * a.g.nz, st);
+            cudaMemsetAsync(a.x, 0, sizeof(float2) * (size_t)a.g.img_nx * a.g.ny * a.g.nz, st);
         if (z != cudaSuccess) return z;
     }
     // value windows copy from even bins of rows of an even length (16-byte aligned)
@@ -854,7 +864,11 @@ cudaError_t launch_bp_grid_ws(const BpGridArgs& a_in, cudaStream_t st) {
         kernel<<<blocks, kWsThreads, smem, st>>>(a);
         return cudaSuccess;
     };
-    if (a.nearest) {
+    if (a.g.shear) {   // sheared lattices: linear sampling, lanes along the lattice's second axis
+        if (a.nearest || a.values || !a.lanes_y) return cudaErrorInvalidValue;
+        e = a.g.precise_bins ? go(bp_grid_ws_pair_kernel<true, true, false, false, true>)
+                             : go(bp_grid_ws_pair_kernel<true, false, false, false, true>);
+    } else if (a.nearest) {
         if (!a.g.precise_bins || !a.steps || !a.alpha2) return cudaErrorInvalidValue;
         if (a.values)
             e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, true, true, true>)

@@ -57,6 +57,7 @@ struct BpGridArgs {
                                //    other warp role may take before it gives up (FLAG_WAIT_TIMEOUT)
     int hold_first_stage = 0;  // test aid: the producers never publish the first pulse stage, so the
                                //    consumers' first wait can only run out (nothing is copied for it)
+    long tiles_valid = 0;      // tiles holding image pixels (a sheared lattice's); 0: all tiles
 };
 size_t bp_grid_smem_bytes(int wwin, int pb, int staged);
 cudaError_t launch_bp_grid(const BpGridArgs& a, cudaStream_t st);

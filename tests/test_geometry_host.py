@@ -356,29 +356,30 @@ def test_bin_extent_bounds_every_pixel_bin(precise):
                     assert hi - lo < 1.2 * (vmax - vmin) + 4.0   # tight: the linear terms dominate
 
 
-def host_eval_sheared(scene, tx, rx, srp, kappa, s_r, shear, bin_offset=-0.5):
-    """The forward scatter's sheared-lattice evaluation, written at the image pixels (NaN where
-    no lattice pixel landed)."""
+def host_eval_sheared(scene, tx, rx, srp, kappa, s_r, shear, bin_offset=-0.5, lanes=False):
+    """The sheared-lattice evaluation, written at the image pixels (NaN where no lattice pixel
+    landed): the forward scatter's layout, or with `lanes` the backprojection's."""
     lib = _lib.load_host()
+    fn = lib.sar_geom_host_eval_sheared_lanes if lanes else lib.sar_geom_host_eval_sheared
     shape, origin, ex, ey, ez = grid_axes(scene)
     nz, ny, nx = shape
     S = tx.shape[0]
     ph = np.full((S, nz * ny * nx), np.nan, np.float32)
     bn = np.full((S, nz * ny * nx), np.nan)
     arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (origin, ex, ey, ez, tx, rx, srp)]
-    assert lib.sar_geom_host_eval_sheared(*[a.ctypes.data for a in arrs[:4]], nx, ny, nz, S,
-                                          *[a.ctypes.data for a in arrs[4:]], kappa, s_r, bin_offset, 0, shear,
-                                          ph.ctypes.data, bn.ctypes.data) == 0
+    assert fn(*[a.ctypes.data for a in arrs[:4]], nx, ny, nz, S, *[a.ctypes.data for a in arrs[4:]], kappa, s_r,
+              bin_offset, 0, shear, ph.ctypes.data, bn.ctypes.data) == 0
     return ph, bn
 
 
-def choose_shear(scene, tx, rx, s_r):
+def choose_shear(scene, tx, rx, s_r, gather=False):
     lib = _lib.load_host()
+    fn = lib.sar_choose_gather_shear_host if gather else lib.sar_choose_shear_host
     shape, origin, ex, ey, ez = grid_axes(scene)
     nz, ny, nx = shape
     arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (tx, rx, origin, ex, ey, ez)]
-    return lib.sar_choose_shear_host(arrs[0].ctypes.data, arrs[1].ctypes.data, tx.shape[0],
-                                     *[a.ctypes.data for a in arrs[2:]], nx, ny, nz, s_r)
+    return fn(arrs[0].ctypes.data, arrs[1].ctypes.data, tx.shape[0], *[a.ctypes.data for a in arrs[2:]], nx, ny, nz,
+              s_r)
 
 
 @pytest.mark.parametrize("az,expect", [(0.0, 0), (90.0, 0), (45.0, -1), (135.0, 1), (-45.0, 1), (20.0, 0)])
@@ -386,15 +387,18 @@ def test_scatter_shear_choice(az, expect):
     """Linear sampling at upsample 8 on the benchmark image: collections along the grid axes keep
     the plain layouts, those along a diagonal walk a lattice sheared by one pixel per row the
     way that cancels the bin rate (-1 when range falls along +x and +y alike), and one at 20
-    degrees, whose iso-range slope is near neither, is left alone."""
+    degrees, whose iso-range slope is near neither, is left alone.  The backprojection makes the
+    same choice for its lanes (at upsample 8 and 128)."""
     tx = spotlight(4096, 5.0, centre_az_deg=az)
     n, spacing = 2048, 0.25
     scene = GridSarScene([1, n, n], [0.0, spacing * (n - 1), spacing * (n - 1)])
     assert choose_shear(scene, tx, tx, 200.0e6 * 8 / C) == expect
+    for U in (8, 128):
+        assert choose_shear(scene, tx, tx, 200.0e6 * U / C, gather=True) == expect
 
 
-@pytest.mark.parametrize("az", [45.0, 135.0])
-def test_sheared_lattice_precision_and_walk(az):
+@pytest.mark.parametrize("az,lanes", [(45.0, False), (135.0, False), (45.0, True)])
+def test_sheared_lattice_precision_and_walk(az, lanes):
     """The benchmark image seen along a diagonal, on the sheared lattice the forward scatter
     walks: every image pixel is evaluated exactly once, to the precision bounds of the plain
     layouts against FP64, and a lattice row step (one row along y, `shear` pixels along x)
@@ -409,7 +413,7 @@ def test_sheared_lattice_precision_and_walk(az):
     kappa, s_r = 10.0e9 / C, 200.0e6 * 8 / C
     m = choose_shear(scene, all_tx, all_tx, s_r)
     assert m != 0
-    ph, bn = host_eval_sheared(scene, tx, tx, srp, kappa, s_r, m)
+    ph, bn = host_eval_sheared(scene, tx, tx, srp, kappa, s_r, m, lanes=lanes)
     assert not np.isnan(bn).any() and not np.isnan(ph).any()
     pos = scene.positions
     for s in range(tx.shape[0]):

@@ -173,7 +173,9 @@ def test_gather_lane_layouts_match_oracle(turn, mode):
     read-modify-writes (nearest) in both layouts.  turn = +-0.5: looking along a grid diagonal,
     where bins change alike along both axes: linear sampling walks a lattice sheared by -+1 pixel
     per row along the iso-range lines (register run windows again, partial lattice tiles at every
-    image edge), nearest sampling keeps the plain layout (two-phase read-modify-writes)."""
+    image edge), nearest sampling keeps the plain layout (two-phase read-modify-writes); the linear
+    backprojection runs on the same lattice with its lanes along the iso-range axis, where its
+    window loads are broadcast, writing each image pixel from exactly one lattice tile."""
     rng = np.random.default_rng(21 + int(2 * turn))
     case = spotlight_case(37, 96, 70, 0.3, 4.0, weights=np.exp(1j * rng.uniform(-3, 3, 37)))
     if turn:
@@ -187,6 +189,8 @@ def test_gather_lane_layouts_match_oracle(turn, mode):
     if abs(turn) != 0.5:
         assert plan.gather_lanes_y == (turn == 0) and plan.scatter_lanes_y == (turn == 1)
     assert plan.scatter_shear == ((-1 if turn > 0 else 1) if abs(turn) == 0.5 and mode == "linear" else 0)
+    # the backprojection's lanes follow the same lattice axis on a diagonal (linear sampling)
+    assert plan.gather_shear == ((-1 if turn > 0 else 1) if abs(turn) == 0.5 and mode == "linear" else 0)
     y = crandn(rng, 37, 96)
     tol = LINEAR_TOL   # nearest bins too: those near a rounding boundary are decided exactly
     e_a = rel_l2(gpu_adjoint(plan, y), oracle.adjoint(case.problem(), y, mode, threads=8))
