@@ -528,17 +528,19 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
         // from global memory directly.
         p->staged = false;
         p->pb = 32;
-        // stages the two producer warps split evenly.  Nearest-bin sampling with windows wider than
-        // 256 bins (large upsampling factors) stores and stages plain values, half the bytes of
-        // pairs: at upsample 128 that measured a third faster, at upsample 8 slower (wider
-        // addressing in the gather), so narrower windows keep pairs.
-        p->values = p->interp == SAR_INTERP_NEAREST_REF && p->wwin > 256;
+        // stages the two producer warps split evenly.  Windows wider than 256 bins (large upsampling
+        // factors) store and stage plain values, half the bytes of pairs (linear sampling reads two
+        // neighbours): at upsample 128 that measured a third faster for nearest bins, at upsample 8
+        // slower (wider addressing in the gather), so narrower windows keep pairs.  The unstaged
+        // gather reads pairs for linear sampling.
+        p->values = p->wwin > 256;
         for (int pb = 32; pb >= 2; pb /= 2)
             if (bp_grid_ws_smem_bytes(p->wwin, pb, p->values) <= kBpSmemBudget) {
                 p->pb = pb;
                 p->staged = true;
                 break;
             }
+        if (!p->staged && p->interp == SAR_INTERP_LINEAR) p->values = false;
         // Forward scatter layout: it walks the gather's lane axis (the transpose of its lane
         // choice), or, for linear sampling across the grid axes, a sheared lattice whose rows
         // follow the iso-range lines (choose_shear), walked with lanes along x.

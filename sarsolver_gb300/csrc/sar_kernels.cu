@@ -537,9 +537,9 @@ template <bool LANES_Y, bool PRECISE, bool NEAREST, bool VALUES = false, bool SH
 __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const BpGridArgs a) {
     extern __shared__ __align__(16) float4 smem[];
     const int pb = a.pb, ww = a.wwin;
-    // VALUES (nearest-bin sampling with wide windows): windows of plain values, half the bytes of
-    // pairs, whose difference half nearest-bin sampling never reads.  A window's size in float4
-    // units: ww pairs, or (ww + 2) / 2 for ww + 2 values
+    // VALUES (wide windows): windows of plain values, half the bytes of pairs; nearest-bin sampling
+    // reads one value, linear sampling two neighbours.  A window's size in float4 units: ww pairs,
+    // or (ww + 2) / 2 for ww + 2 values
     const int wst = VALUES ? win_elems(ww, 1) / 2 : ww;
     float4* win0 = smem;
     float4* coef0 = win0 + 2 * pb * wst;
@@ -776,10 +776,15 @@ __global__ void __launch_bounds__(kWsThreads, 2) bp_grid_ws_pair_kernel(const Bp
                     }
                 }
                 float2 re, im;
-                if (VALUES) {   // the bin's value, no interpolation
+                if (VALUES && NEAREST) {   // the bin's value, no interpolation
                     const float2 pa = va[ia], pq = vb[ib];
                     re = f2(pa.x, pq.x);
                     im = f2(pa.y, pq.y);
+                } else if (VALUES) {   // p(n) + (s + 1/2) (p(n + 1) - p(n)), s in [-1/2, 1/2]
+                    const float2 pa = va[ia], pq = vb[ib], pa1 = va[ia + 1], pq1 = vb[ib + 1];
+                    const float2 t = add2(s, f2(0.5f, 0.5f));
+                    re = fma2(t, f2(pa1.x - pa.x, pq1.x - pq.x), f2(pa.x, pq.x));
+                    im = fma2(t, f2(pa1.y - pa.y, pq1.y - pq.y), f2(pa.y, pq.y));
                 } else {
                     const float4 pa = LANES_Y ? wa[ia] : lds_f4(aa), pq = LANES_Y ? wb[ib] : lds_f4(ab);
                     re = f2(fmaf(s.x, pa.z, pa.x), fmaf(s.y, pq.z, pq.x));
@@ -854,7 +859,7 @@ cudaError_t launch_bp_grid_ws(const BpGridArgs& a_in, cudaStream_t st) {
         if (z != cudaSuccess) return z;
     }
     // value windows copy from even bins of rows of an even length (16-byte aligned)
-    if (a.values && (!a.nearest || (a.Lg & 1) || a.Lg < a.wwin + 2)) return cudaErrorInvalidValue;
+    if (a.values && ((a.Lg & 1) || a.Lg < a.wwin + 2)) return cudaErrorInvalidValue;
     const size_t smem = bp_grid_ws_smem_bytes(a.wwin, a.pb, a.values);
     const unsigned blocks = (unsigned)(tiles * a.parts);
     cudaError_t e;
@@ -865,9 +870,12 @@ cudaError_t launch_bp_grid_ws(const BpGridArgs& a_in, cudaStream_t st) {
         return cudaSuccess;
     };
     if (a.g.shear) {   // sheared lattices: linear sampling, lanes along the lattice's second axis
-        if (a.nearest || a.values || !a.lanes_y) return cudaErrorInvalidValue;
-        e = a.g.precise_bins ? go(bp_grid_ws_pair_kernel<true, true, false, false, true>)
-                             : go(bp_grid_ws_pair_kernel<true, false, false, false, true>);
+        if (a.nearest || !a.lanes_y || (a.values && !a.g.precise_bins)) return cudaErrorInvalidValue;
+        if (a.values)
+            e = go(bp_grid_ws_pair_kernel<true, true, false, true, true>);
+        else
+            e = a.g.precise_bins ? go(bp_grid_ws_pair_kernel<true, true, false, false, true>)
+                                 : go(bp_grid_ws_pair_kernel<true, false, false, false, true>);
     } else if (a.nearest) {
         if (!a.g.precise_bins || !a.steps || !a.alpha2) return cudaErrorInvalidValue;
         if (a.values)
@@ -875,6 +883,10 @@ cudaError_t launch_bp_grid_ws(const BpGridArgs& a_in, cudaStream_t st) {
                           : go(bp_grid_ws_pair_kernel<false, true, true, true>);
         else
             e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, true, true>) : go(bp_grid_ws_pair_kernel<false, true, true>);
+    } else if (a.values) {   // linear sampling from value windows (wide windows: split bins)
+        if (!a.g.precise_bins) return cudaErrorInvalidValue;
+        e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, true, false, true>)
+                      : go(bp_grid_ws_pair_kernel<false, true, false, true>);
     } else if (a.g.precise_bins) {
         e = a.lanes_y ? go(bp_grid_ws_pair_kernel<true, true, false>) : go(bp_grid_ws_pair_kernel<false, true, false>);
     } else {

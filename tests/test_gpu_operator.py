@@ -201,12 +201,14 @@ def test_gather_lane_layouts_match_oracle(turn, mode):
     assert plan.device_flags() == 0
 
 
+@pytest.mark.parametrize("mode", ["nearest_ref", "linear"])
 @pytest.mark.parametrize("turn", [0, 1])
-def test_value_windows_match_oracle(turn):
-    """nearest_ref at the reference's default upsample 128: staged windows wider than 256 bins,
-    which store and stage plain values (half the bytes of pairs), in both lane layouts, with an
-    odd pulse count and partial tiles, against the FP64 oracle (bins near a rounding boundary are
-    decided exactly, so the linear-mode tolerance holds)."""
+def test_value_windows_match_oracle(turn, mode):
+    """Upsample 128 (nearest_ref with it: the reference's defaults): staged windows wider than 256
+    bins, which store and stage plain values (half the bytes of pairs; linear sampling reads two
+    neighbours), in both lane layouts, with an odd pulse count and partial tiles, against the FP64
+    oracle (nearest bins near a rounding boundary are decided exactly, so the linear-mode
+    tolerance holds)."""
     rng = np.random.default_rng(41 + turn)
     case = spotlight_case(37, 96, 70, 0.1, 4.0, upsample=128.0, weights=np.exp(1j * rng.uniform(-3, 3, 37)))
     if turn:
@@ -215,13 +217,39 @@ def test_value_windows_match_oracle(turn):
         case.aperture = NumpySimpleSarAperture(ap.transmitter_positions @ rot.T, ap.receiver_positions @ rot.T,
                                                ap.stab_ref_posns, ap.centre_frequency, ap.sample_bandwidth,
                                                num_freqs=ap.num_freqs, slow_time_weighting=ap.slow_time_weighting)
-    plan = SarPlan(case.scene, case.aperture, upsample_ratio=128.0, interp="nearest_ref", path="grid")
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=128.0, interp=mode, path="grid")
     assert plan.is_grid and plan.tile_window > 256 and plan.gather_lanes_y == (turn == 0)
     y = crandn(rng, 37, 96)
-    e_a = rel_l2(gpu_adjoint(plan, y), oracle.adjoint(case.problem(), y, "nearest_ref", threads=8))
+    e_a = rel_l2(gpu_adjoint(plan, y), oracle.adjoint(case.problem(), y, mode, threads=8))
     assert e_a < LINEAR_TOL, e_a
     x = crandn(rng, case.scene.num_scatterers)
-    e_f = rel_l2(gpu_forward(plan, x), oracle.forward(case.problem(), x, "nearest_ref", threads=8))
+    e_f = rel_l2(gpu_forward(plan, x), oracle.forward(case.problem(), x, mode, threads=8))
+    assert e_f < LINEAR_TOL, e_f
+    assert plan.device_flags() == 0
+
+
+@pytest.mark.parametrize("turn", [0.5, -0.5])
+def test_sheared_gather_with_split_bins_matches_oracle(turn):
+    """Linear sampling at upsample 128 looking along a diagonal: the backprojection runs on the
+    sheared lattice with split bins (windows wider than 256 bins: exact integer parts), the
+    forward projection on the plain layout (split bins take no lattice); both against the FP64
+    oracle, with an odd pulse count and partial lattice tiles."""
+    rng = np.random.default_rng(61)
+    case = spotlight_case(37, 96, 70, 0.1, 4.0, upsample=128.0, weights=np.exp(1j * rng.uniform(-3, 3, 37)))
+    c, s_ = np.cos(turn * np.pi / 2), np.sin(turn * np.pi / 2)
+    rot = np.array([[c, -s_, 0.0], [s_, c, 0.0], [0.0, 0.0, 1.0]])
+    ap = case.aperture
+    case.aperture = NumpySimpleSarAperture(ap.transmitter_positions @ rot.T, ap.receiver_positions @ rot.T,
+                                           ap.stab_ref_posns, ap.centre_frequency, ap.sample_bandwidth,
+                                           num_freqs=ap.num_freqs, slow_time_weighting=ap.slow_time_weighting)
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=128.0, interp="linear", path="grid")
+    assert plan.gather_shear == (-1 if turn > 0 else 1) and plan.scatter_shear == 0
+    assert plan.tile_window > 256
+    y = crandn(rng, 37, 96)
+    e_a = rel_l2(gpu_adjoint(plan, y), oracle.adjoint(case.problem(), y, "linear", threads=8))
+    assert e_a < LINEAR_TOL, e_a
+    x = crandn(rng, case.scene.num_scatterers)
+    e_f = rel_l2(gpu_forward(plan, x), oracle.forward(case.problem(), x, "linear", threads=8))
     assert e_f < LINEAR_TOL, e_f
     assert plan.device_flags() == 0
 
