@@ -134,6 +134,9 @@ typedef struct sar_plan_info {
                                    for linear sampling of collections looking across the grid axes */
     int gather_shear;           /* m != 0: the grid backprojection runs on a sheared lattice with warp
                                    lanes along ey + m ex (collections looking across the grid axes) */
+    int scatter_ring_half;      /* > 0: the grid forward scatter keeps ring windows of strip_window
+                                   slots per pulse holding a tile's bins within this many of its base
+                                   (split bins with tiles too wide for strip windows, e.g. upsample 128) */
 } sar_plan_info;
 
 /* Create a plan on `device` (-1: the current device).  Copies all host inputs. */

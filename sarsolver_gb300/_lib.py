@@ -96,7 +96,7 @@ class SarPlanInfo(ctypes.Structure):
         ("interp", c_int), ("num_fast_times", c_size_t), ("num_slow_times", c_size_t), ("num_scatterers", c_size_t),
         ("device", c_int), ("fft_callbacks", c_int), ("gather_lanes_y", c_int), ("fused_upsampling", c_int), ("fused_downsampling", c_int),
         ("scatter_lanes_y", c_int), ("block_pulses", c_size_t), ("scatter_shear", c_int),
-        ("gather_shear", c_int),
+        ("gather_shear", c_int), ("scatter_ring_half", c_int),
     ]
 
 

@@ -86,6 +86,7 @@ bool finite3(const double* v, size_t n) {
 // Shared-memory budgets: two tile CTAs per SM.
 constexpr size_t kBpSmemBudget = 110 * 1024;
 constexpr size_t kFpSmemBudget = 110 * 1024;
+constexpr size_t kFpRingSmemBudget = 220 * 1024;   // ring windows: one CTA per SM
 constexpr size_t kSpecBudget = (size_t)4 << 30;   // bytes of FFT work rows per chunk
 
 }  // namespace
@@ -106,6 +107,7 @@ struct sar_plan {
     int lanes_y = 0;
     bool fwd_transposed = false;   // forward scatter: lanes along y, rows walked along x
     int gather_shear = 0;          // backprojection on a sheared lattice (gc_adj), lanes along ey + m ex
+    int ring_half = 0;             // forward scatter on ring windows (FpGridArgs.ring_half), 0: strips
     long tiles_valid = 0;          // its tiles that hold image pixels (0: all tiles of the grid)
     bool staged = true;
     bool values = false;   // stored profiles are plain values (kProfValues), not pairs
@@ -628,6 +630,33 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
             }
             if (!p->forward_points) break;
         }
+        // Ring windows (split bins): where strip windows hold only one or two tiles (a 32-pixel tile
+        // spans ~1200 bins at upsample 128), every CTA would clear and merge a whole window for 1024
+        // pixels per pulse.  A ring of W = 2^k >= 2 H + 1 slots per pulse instead holds one tile's
+        // range (its base bin +- H, H from the look directions as for the gather's windows) and a CTA
+        // walks its whole line, adding and clearing only the bins each tile step leaves behind.
+        if (p->gc_fwd.precise_bins && (p->forward_points || p->seg_tiles <= 2)) {
+            const double hd = tile_halfspan_directional(tx, rx, S, origin, ex, ey, ez, kTile, p->gc_fwd.tiles_x,
+                                                        p->gc_fwd.tiles_y, nz, s_r);
+            const double h = hd >= 0.0 ? hd : 0.5 * grid_tile_window(g, s_r);
+            if (h >= 0.0 && h < 1.0e6) {
+                const int H = (int)std::ceil(h) + 4;
+                int W = 32;
+                while (W < 2 * H + 1) W *= 2;
+                for (int pbf : {16, 8})
+                    if (fp_grid_ws_smem_bytes(W, pbf, 0) <= kFpRingSmemBudget) {
+                        p->ring_half = H;
+                        p->ws = W;
+                        p->pbf = pbf;
+                        p->seg_tiles = along;
+                        p->segs_per_column = 1;
+                        p->n_strips = (size_t)nz * lines;
+                        strip_start.assign(p->n_strips * S, 0);   // not read with ring windows
+                        p->forward_points = false;
+                        break;
+                    }
+            }
+        }
         if (p->forward_points) {
             // Extremely coarse grids: forward through the unstructured kernels.
             points.resize(P);
@@ -910,6 +939,7 @@ int sar_plan_get_info(const sar_plan* p, sar_plan_info* info) {
     info->scatter_lanes_y = (p->grid && !p->forward_points && p->fwd_transposed) ? 1 : 0;
     info->scatter_shear = (p->grid && !p->forward_points) ? p->gc_fwd.shear : 0;
     info->gather_shear = p->grid ? p->gather_shear : 0;
+    info->scatter_ring_half = (p->grid && !p->forward_points) ? p->ring_half : 0;
     info->block_pulses = p->block;
     return SAR_OK;
 }
@@ -1082,6 +1112,7 @@ static int scatter_pulses(sar_plan* p, const float2* x, float2* acc, size_t firs
     a.seg_tiles = p->seg_tiles;
     a.segs_per_column = p->segs_per_column;
     a.ws = p->ws;
+    a.ring_half = p->ring_half;
     a.pbf = p->pbf;
     a.linear = p->interp == SAR_INTERP_LINEAR;
     // the scatter walks the axis along which bins change slowly: the transpose of the gather's

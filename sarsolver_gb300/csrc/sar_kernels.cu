@@ -396,7 +396,7 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
 // Producer: coefficient sets for pulses s0 + pass .. s0 + pass + 7 (lane = 4*pulse + sub-tile).
 __device__ __forceinline__ void producer_coeffs(const GridConst& g, const PulseGeom* __restrict__ pulses, int s0,
                                                 int npb, int pass, const df3* anchors, float4* coef, int* base,
-                                                int lane) {
+                                                int lane, int ring_half = 0, unsigned* flags = nullptr) {
     const int pi = pass + (lane >> 2), q = lane & 3;
     const bool valid = pi < npb;
     AnchorExpansion ae = {};
@@ -415,6 +415,17 @@ __device__ __forceinline__ void producer_coeffs(const GridConst& g, const PulseG
     b = __shfl_sync(all, b, lane & ~3);
     if (valid) {
         bin_coeffs(ae, vb, b, g, co);
+        if (ring_half > 0) {
+            // ring windows: every bin the sub-tile touches (n - 1 .. n + 1 around its position) must
+            // lie within ring_half of the base bin, or it would alias another bin's slot
+            float lo, hi;
+            bin_extent(co, &lo, &hi);
+            const float lim = (float)(ring_half - 2);
+            if (!(lo >= -lim && hi <= lim)) {
+                raise_flag(flags, FLAG_STRIP_WINDOW);
+                co = Coeffs{};   // invalid result (flagged), every bin then at the base
+            }
+        }
         float4* dst = coef + (pi * 4 + q) * kSetF4;
         dst[0] = make_float4(co.c[0], co.c[1], co.c[2], co.c[3]);
         dst[1] = make_float4(co.c[4], co.c[5], co.c[6], co.c[7]);
@@ -996,11 +1007,16 @@ struct NearCtx {
 // disjoint (one phase per row); MODE 1: bins n distinct (two phases); MODE 0: atomics.  Nearest
 // bins within 5e-5 of a rounding boundary are decided again exactly; such a bin may equal a
 // neighbouring lane's, so those contributions go in with atomics in a phase of their own.
-template <bool LINEAR, bool PRECISE, int MODE, bool TWO, typename XT>
+// RING: ring windows (ws a power of two; off_p / off_q are the pulses' absolute base bins and a
+// bin's slot is its absolute index mod ws), else strip windows (off = base - window start).
+template <bool LINEAR, bool PRECISE, int MODE, bool TWO, typename XT, bool RING = false>
 __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, float w9p, float ibp,
                                              const ColumnTerms& ctq, float c9q, float w9q, float ibq,
                                              const XT* xrow, float2* wp, float2* wq, int off_p, int off_q,
                                              int ws, int lane, const NearCtx& nc) {
+    const int mask = ws - 1;
+    // the slot after slot i (the second tap of linear sampling)
+    auto next = [&](int i) { return RING ? ((i + 1) & mask) : i + 1; };
     // the lane's phase constant and its rate along the rows mod 1 (rows are integer offsets)
     ColumnTerms cp = ctp, cq = ctq;
     cp.cph -= rintf(cp.cph);
@@ -1012,39 +1028,39 @@ __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, 
         const float dj = (float)(rr - 8);
         const float2 xv = staged_value(xrow[rr * kXtStride + lane]);
         const RowEval<PRECISE> ep = scatter_eval<PRECISE>(cp, c9p, w9p, ibp, dj, xv);
-        const int ip = (int)min((unsigned)(ep.bp.n + off_p), (unsigned)(ws - 2));
+        const int ip = RING ? ((ep.bp.n + off_p) & mask) : (int)min((unsigned)(ep.bp.n + off_p), (unsigned)(ws - 2));
         RowEval<PRECISE> eq;
         int iq = 0;
         if (TWO) {
             eq = scatter_eval<PRECISE>(cq, c9q, w9q, ibq, dj, xv);
-            iq = (int)min((unsigned)(eq.bp.n + off_q), (unsigned)(ws - 2));
+            iq = RING ? ((eq.bp.n + off_q) & mask) : (int)min((unsigned)(eq.bp.n + off_q), (unsigned)(ws - 2));
         }
         if (LINEAR) {
             const float w0p = 0.5f - ep.bp.s, w1p = 0.5f + ep.bp.s;
             const float w0q = TWO ? 0.5f - eq.bp.s : 0.f, w1q = TWO ? 0.5f + eq.bp.s : 0.f;
             if (MODE == 2) {
                 rmw_add(wp, ip, w0p, ep.cr, ep.ci);
-                rmw_add(wp, ip + 1, w1p, ep.cr, ep.ci);
+                rmw_add(wp, next(ip), w1p, ep.cr, ep.ci);
                 if (TWO) {
                     rmw_add(wq, iq, w0q, eq.cr, eq.ci);
-                    rmw_add(wq, iq + 1, w1q, eq.cr, eq.ci);
+                    rmw_add(wq, next(iq), w1q, eq.cr, eq.ci);
                 }
                 __syncwarp();
             } else if (MODE == 1) {
                 rmw_add(wp, ip, w0p, ep.cr, ep.ci);
                 if (TWO) rmw_add(wq, iq, w0q, eq.cr, eq.ci);
                 __syncwarp();
-                rmw_add(wp, ip + 1, w1p, ep.cr, ep.ci);
-                if (TWO) rmw_add(wq, iq + 1, w1q, eq.cr, eq.ci);
+                rmw_add(wp, next(ip), w1p, ep.cr, ep.ci);
+                if (TWO) rmw_add(wq, next(iq), w1q, eq.cr, eq.ci);
                 __syncwarp();
             } else {
                 float2* a0 = wp + wslot(ip);
-                float2* a1 = wp + wslot(ip + 1);
+                float2* a1 = wp + wslot(next(ip));
                 atomicAdd(&a0->x, w0p * ep.cr); atomicAdd(&a0->y, w0p * ep.ci);
                 atomicAdd(&a1->x, w1p * ep.cr); atomicAdd(&a1->y, w1p * ep.ci);
                 if (TWO) {
                     float2* b0 = wq + wslot(iq);
-                    float2* b1 = wq + wslot(iq + 1);
+                    float2* b1 = wq + wslot(next(iq));
                     atomicAdd(&b0->x, w0q * eq.cr); atomicAdd(&b0->y, w0q * eq.ci);
                     atomicAdd(&b1->x, w1q * eq.cr); atomicAdd(&b1->y, w1q * eq.ci);
                 }
@@ -1058,12 +1074,17 @@ __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, 
                 if (fp || fq) {
                     const int pj = nc.j0 + (nc.transposed ? lane : rr);
                     const int pi = nc.i0 + (nc.transposed ? rr : lane) + nc.a_off + nc.shear * pj;
-                    if (fp)
-                        xp = min(max(exact_grid_bin(nc.steps, nc.pulses, nc.alpha2, nc.sr_hi, nc.sr_lo, nc.bg0,
-                                                    BIN_FWD_NEAREST, pi, pj, nc.k, nc.sp) + nc.bg0 - nc.wsp, 0), ws - 1);
-                    if (fq)
-                        xq = min(max(exact_grid_bin(nc.steps, nc.pulses, nc.alpha2, nc.sr_hi, nc.sr_lo, nc.bg0,
-                                                    BIN_FWD_NEAREST, pi, pj, nc.k, nc.sq) + nc.bg0 - nc.wsq, 0), ws - 1);
+                    // the exact bin (bins from bg0) as a window slot
+                    if (fp) {
+                        const int b = exact_grid_bin(nc.steps, nc.pulses, nc.alpha2, nc.sr_hi, nc.sr_lo, nc.bg0,
+                                                     BIN_FWD_NEAREST, pi, pj, nc.k, nc.sp) + nc.bg0;
+                        xp = RING ? (b & mask) : min(max(b - nc.wsp, 0), ws - 1);
+                    }
+                    if (fq) {
+                        const int b = exact_grid_bin(nc.steps, nc.pulses, nc.alpha2, nc.sr_hi, nc.sr_lo, nc.bg0,
+                                                     BIN_FWD_NEAREST, pi, pj, nc.k, nc.sq) + nc.bg0;
+                        xq = RING ? (b & mask) : min(max(b - nc.wsq, 0), ws - 1);
+                    }
                 }
             }
             if (MODE >= 1) {
@@ -1177,12 +1198,12 @@ __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float 
   }
 }
 
-template <bool LINEAR, bool PRECISE, bool TWO, typename XT>
+template <bool LINEAR, bool PRECISE, bool TWO, typename XT, bool RING = false>
 __device__ __forceinline__ void scatter_half(int mode, const ColumnTerms& ctp, float c9p, float w9p, float ibp,
                                              const ColumnTerms& ctq, float c9q, float w9q, float ibq,
                                              const XT* xrow, float2* wp, float2* wq, int off_p, int off_q,
                                              int ws, int lane, const NearCtx& nc) {
-    if constexpr (LINEAR && !PRECISE) {
+    if constexpr (LINEAR && !PRECISE && !RING) {
         if (mode == 5) {
             scatter_rows_runs<TWO, 16>(ctp, c9p, ctq, c9q, xrow, wp, wq, off_p, off_q, ws, lane);
             return;
@@ -1197,18 +1218,39 @@ __device__ __forceinline__ void scatter_half(int mode, const ColumnTerms& ctp, f
         }
     }
     if (mode >= 2)
-        scatter_rows<LINEAR, PRECISE, 2, TWO, XT>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
+        scatter_rows<LINEAR, PRECISE, 2, TWO, XT, RING>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
                                               nc);
     else if (mode == 1)
-        scatter_rows<LINEAR, PRECISE, 1, TWO, XT>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
+        scatter_rows<LINEAR, PRECISE, 1, TWO, XT, RING>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
                                               nc);
     else
-        scatter_rows<LINEAR, PRECISE, 0, TWO, XT>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
+        scatter_rows<LINEAR, PRECISE, 0, TWO, XT, RING>(ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq, off_p, off_q, ws, lane,
                                               nc);
 }
 
-template <bool LINEAR, bool PRECISE, bool TRANSPOSED>
-__global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridArgs a) {
+// Adds the window slots of bins [lo, hi] (absolute) of one pulse into its accumulator row and clears
+// them (ring windows: the bins a tile step leaves behind, and the last tile's at the end).
+__device__ __forceinline__ void ring_flush(float2* wp, int lo, int hi, int mask, const FpGridArgs& a, int s,
+                                           int lane) {
+    for (int bin = lo + lane; bin <= hi; bin += 32) {
+        float2* q = wp + wslot(bin & mask);
+        const float2 v = *q;
+        if (v.x == 0.f && v.y == 0.f) continue;
+        *q = make_float2(0.f, 0.f);
+        const long gi = (long)bin - a.bg0;
+        if (gi < 0 || gi >= a.Lg) {
+            raise_flag(a.flags, FLAG_STRIP_WINDOW);
+            continue;
+        }
+        atomicAdd(a.acc + (size_t)s * a.Lg + gi, v);
+    }
+}
+
+// RING (split bins only): ring windows instead of strip windows (FpGridArgs.ring_half): a CTA walks
+// its whole line of tiles and, between tiles, each warp adds and clears the bins its pulses leave
+// behind, so windows no longer bound the length of a strip (1-tile strips at upsample 128 otherwise).
+template <bool LINEAR, bool PRECISE, bool TRANSPOSED, bool RING = false>
+__global__ void __launch_bounds__(kWsThreads, RING ? 1 : 2) fp_grid_ws_kernel(const FpGridArgs a) {
     extern __shared__ __align__(16) unsigned char fsm[];
     const int pbf = a.pbf, ws = a.ws, wslots = window_slots(ws);
     constexpr bool WIDE_X = LINEAR && !PRECISE;
@@ -1244,7 +1286,8 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     for (int e = threadIdx.x; e < pbf * wslots; e += blockDim.x) win[e] = make_float2(0.f, 0.f);
-    for (int e = threadIdx.x; e < npb; e += blockDim.x) wst[e] = a.strip_start[(size_t)strip * a.strip_stride + s0 + e];
+    for (int e = threadIdx.x; e < npb; e += blockDim.x)
+        wst[e] = RING ? 0 : a.strip_start[(size_t)strip * a.strip_stride + s0 + e];
     if (threadIdx.x == 0) {
         mbar_init(&bars[0], kWsProducers);
         mbar_init(&bars[1], kWsProducers);
@@ -1287,7 +1330,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
             int* base = base0 + b * pbf;
             int* fast = fast0 + b * pbf;
             for (int pass = 8 * pw; pass < npb; pass += 8 * kWsProducers) {
-                producer_coeffs(g, a.pulses, s0, npb, pass, anchors, coef, base, lane);
+                producer_coeffs(g, a.pulses, s0, npb, pass, anchors, coef, base, lane, RING ? a.ring_half : 0, a.flags);
                 __syncwarp();
                 // Distinct-bin guarantee along x for each pulse of the pass: the smallest
                 // |dv/di| over the sub-tile from the quadratic bin model (di, dj in [-8, 7]).
@@ -1351,9 +1394,30 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
     tt.di2 = di * di;
     tt.di3 = tt.di2 * di;
     bool ok = true;
+    // ring windows: the base bin of each of this warp's pulses (warp + 8 k) at the previous tile
+    const int mask = ws - 1, rh = a.ring_half;
+    int prev_base[kMaxStagePulses / (kWsConsumers / 32)];
     for (int t = 0; t < ntile; ++t) {
         const int b = t & 1;
         if (ok && !mbar_wait(&bars[b], (t >> 1) & 1, 32, 256)) ok = false;
+        if (ok && RING) {
+            // bins the step from the previous tile's range [base - rh, base + rh] leaves behind
+#pragma unroll
+            for (int k = 0; k < kMaxStagePulses / (kWsConsumers / 32); ++k) {
+                const int p = warp + k * (kWsConsumers / 32);
+                if (p >= npb) break;
+                const int nb = base0[b * pbf + p];
+                if (t > 0 && nb != prev_base[k]) {
+                    const int ob = prev_base[k];
+                    if (nb > ob)
+                        ring_flush(win + p * wslots, ob - rh, min(ob + rh, nb - rh - 1), mask, a, s0 + p, lane);
+                    else
+                        ring_flush(win + p * wslots, max(ob - rh, nb + rh + 1), ob + rh, mask, a, s0 + p, lane);
+                }
+                prev_base[k] = nb;
+            }
+            __syncwarp();
+        }
         if (ok) {
             const float4* coef = coef0 + b * pbf * 4 * kSetF4;
             const XT* xt = xt0 + b * kTile * kXtStride;
@@ -1365,7 +1429,7 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                 const int pq = two ? p2 : p;
                 float2* wp = win + p * wslots;
                 float2* wq = win + pq * wslots;
-                const int off_p = base0[b * pbf + p] - wst[p];
+                const int off_p = base0[b * pbf + p] - wst[p];    // ring: the absolute base bin
                 const int off_q = base0[b * pbf + pq] - wst[pq];
                 const int mode = two ? min(fast0[b * pbf + p], fast0[b * pbf + p2]) : fast0[b * pbf + p];
 #pragma unroll
@@ -1398,11 +1462,11 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
                         nc.shear = g.shear;
                     }
                     if (two)
-                        scatter_half<LINEAR, PRECISE, true>(mode, ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp, wq,
-                                                            off_p, off_q, ws, lane, nc);
+                        scatter_half<LINEAR, PRECISE, true, XT, RING>(mode, ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq,
+                                                                      xrow, wp, wq, off_p, off_q, ws, lane, nc);
                     else
-                        scatter_half<LINEAR, PRECISE, false>(mode, ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq, xrow, wp,
-                                                             wq, off_p, off_q, ws, lane, nc);
+                        scatter_half<LINEAR, PRECISE, false, XT, RING>(mode, ctp, c9p, w9p, ibp, ctq, c9q, w9q, ibq,
+                                                                       xrow, wp, wq, off_p, off_q, ws, lane, nc);
                 }
             }
         }
@@ -1413,38 +1477,50 @@ __global__ void __launch_bounds__(kWsThreads, 2) fp_grid_ws_kernel(const FpGridA
         if (lane == 0) raise_flag(a.flags, FLAG_WAIT_TIMEOUT);
         return;
     }
-    // merge this warp's windows into the global accumulator
     __syncwarp();
-    for (int p = warp; p < npb; p += kWsConsumers / 32) {
-        const float2* wp = win + p * wslots;
-        for (int w = lane; w < ws; w += 32) {
-            const float2 v = wp[wslot(w)];
-            if (v.x == 0.f && v.y == 0.f) continue;
-            const long gi = (long)wst[p] + w - a.bg0;
-            if (gi < 0 || gi >= a.Lg) {
-                raise_flag(a.flags, FLAG_STRIP_WINDOW);
-                continue;
+    if constexpr (RING) {   // the last tile's ranges
+#pragma unroll
+        for (int k = 0; k < kMaxStagePulses / (kWsConsumers / 32); ++k) {
+            const int p = warp + k * (kWsConsumers / 32);
+            if (p >= npb) break;
+            ring_flush(win + p * wslots, prev_base[k] - rh, prev_base[k] + rh, mask, a, s0 + p, lane);
+        }
+    } else {
+        // merge this warp's windows into the global accumulator
+        for (int p = warp; p < npb; p += kWsConsumers / 32) {
+            const float2* wp = win + p * wslots;
+            for (int w = lane; w < ws; w += 32) {
+                const float2 v = wp[wslot(w)];
+                if (v.x == 0.f && v.y == 0.f) continue;
+                const long gi = (long)wst[p] + w - a.bg0;
+                if (gi < 0 || gi >= a.Lg) {
+                    raise_flag(a.flags, FLAG_STRIP_WINDOW);
+                    continue;
+                }
+                float2* dst = a.acc + (size_t)(s0 + p) * a.Lg + gi;
+                atomicAdd(dst, v);   // one vector reduction for both components
             }
-            float2* dst = a.acc + (size_t)(s0 + p) * a.Lg + gi;
-            atomicAdd(dst, v);   // one vector reduction for both components
         }
     }
 }
 
-template <bool LINEAR, bool PRECISE, bool TRANSPOSED>
+template <bool LINEAR, bool PRECISE, bool TRANSPOSED, bool RING = false>
 static cudaError_t launch_fp_grid_ws_t(const FpGridArgs& a, cudaStream_t st) {
     const size_t smem = fp_grid_ws_smem_bytes(a.ws, a.pbf, LINEAR && !PRECISE);
     const int lines = TRANSPOSED ? a.g.tiles_y : a.g.tiles_x;
     const dim3 grid((unsigned)(a.segs_per_column * lines * a.g.nz), (unsigned)((a.S + a.pbf - 1) / a.pbf));
-    cudaError_t e = cudaFuncSetAttribute(fp_grid_ws_kernel<LINEAR, PRECISE, TRANSPOSED>,
+    cudaError_t e = cudaFuncSetAttribute(fp_grid_ws_kernel<LINEAR, PRECISE, TRANSPOSED, RING>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    fp_grid_ws_kernel<LINEAR, PRECISE, TRANSPOSED><<<grid, kWsThreads, smem, st>>>(a);
+    fp_grid_ws_kernel<LINEAR, PRECISE, TRANSPOSED, RING><<<grid, kWsThreads, smem, st>>>(a);
     return cudaGetLastError();
 }
 
 template <bool TRANSPOSED>
 static cudaError_t launch_fp_grid_ws_o(const FpGridArgs& a, cudaStream_t st) {
+    if (a.ring_half > 0)   // ring windows: split bins only
+        return a.linear ? launch_fp_grid_ws_t<true, true, TRANSPOSED, true>(a, st)
+                        : launch_fp_grid_ws_t<false, true, TRANSPOSED, true>(a, st);
     if (a.linear)
         return a.g.precise_bins ? launch_fp_grid_ws_t<true, true, TRANSPOSED>(a, st)
                                 : launch_fp_grid_ws_t<true, false, TRANSPOSED>(a, st);
@@ -1454,6 +1530,9 @@ static cudaError_t launch_fp_grid_ws_o(const FpGridArgs& a, cudaStream_t st) {
 
 cudaError_t launch_fp_grid_ws(const FpGridArgs& a, cudaStream_t st) {
     if (a.pbf < 8 || a.pbf > 32 || (a.pbf & 7) || a.ws < 32 || (a.ws & 31)) return cudaErrorInvalidValue;
+    // ring windows: split bins, a power-of-two ring holding a tile's whole range
+    if (a.ring_half > 0 && (!a.g.precise_bins || (a.ws & (a.ws - 1)) || 2 * a.ring_half + 1 > a.ws))
+        return cudaErrorInvalidValue;
     if (!a.linear && a.g.precise_bins && (!a.steps || !a.alpha2)) return cudaErrorInvalidValue;
     return a.transposed ? launch_fp_grid_ws_o<true>(a, st) : launch_fp_grid_ws_o<false>(a, st);
 }

@@ -84,6 +84,9 @@ struct FpGridArgs {
     int transposed;            // 1: lanes along y, rows walked along x (bins change slowly along x)
     const double* steps;       // nearest bins: FP64 grid steps and antenna norms for the exact
     const float4* alpha2;      //   decisions near rounding boundaries (as BpGridArgs)
+    int ring_half = 0;         // > 0 (split bins only): ring windows -- ws is a power of two, slot of
+                               //    absolute bin b is b mod ws, and a tile touches bins within
+                               //    ring_half of its base bin; 0: strip windows from strip_start
 };
 // Warp-specialised variant: producer warps stage image tiles and coefficient sets; each
 // gathering warp owns whole pulses, so its windows need no atomics when bins along a row of

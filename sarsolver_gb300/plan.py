@@ -132,6 +132,7 @@ class SarPlan:
         self.block_pulses = int(info.block_pulses)
         self.scatter_shear = int(info.scatter_shear)
         self.gather_shear = int(info.gather_shear)
+        self.scatter_ring_half = int(info.scatter_ring_half)
         # The aperture's own weighting; phase corrections multiply it (autodiff.phase_weights).
         self.base_weights = torch.as_tensor(
             np.asarray(aperture.slow_time_weighting, dtype=np.complex64).reshape(-1)).to(self.device)

@@ -228,6 +228,40 @@ def test_value_windows_match_oracle(turn, mode):
     assert plan.device_flags() == 0
 
 
+@pytest.mark.parametrize("mode", ["nearest_ref", "linear"])
+@pytest.mark.parametrize("turn", [0, 1])
+def test_ring_windows_match_oracle(turn, mode):
+    """Upsample 128 on 0.25 m pixels: a 32-pixel tile spans ~1200 range bins, so strip windows hold
+    at most single tiles; the forward scatter keeps ring windows instead (slots = absolute bin mod a
+    power of two, the bins each tile step leaves behind added to the accumulator), walking whole
+    lines of tiles in both layouts.  Against the FP64 oracle with an odd pulse count and partial
+    tiles (nearest bins near a rounding boundary decided exactly)."""
+    rng = np.random.default_rng(71 + turn)
+    # a 20 degree aperture: bins also drift ~6.6 per pixel along the lines, so no strip window holds
+    # even one tile (strip windows would leave the scatter to the per-pixel kernel)
+    case = spotlight_case(37, 96, 100, 0.25, 20.0, upsample=128.0, weights=np.exp(1j * rng.uniform(-3, 3, 37)))
+    if turn:
+        ap = case.aperture
+        rot = np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+        case.aperture = NumpySimpleSarAperture(ap.transmitter_positions @ rot.T, ap.receiver_positions @ rot.T,
+                                               ap.stab_ref_posns, ap.centre_frequency, ap.sample_bandwidth,
+                                               num_freqs=ap.num_freqs, slow_time_weighting=ap.slow_time_weighting)
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=128.0, interp=mode, path="grid")
+    assert plan.scatter_ring_half > 0, (plan.strip_window, plan.tile_window)
+    assert plan.scatter_lanes_y == (turn == 1)
+    x = crandn(rng, case.scene.num_scatterers)
+    e_f = rel_l2(gpu_forward(plan, x), oracle.forward(case.problem(), x, mode, threads=8))
+    assert e_f < LINEAR_TOL, e_f
+    y = crandn(rng, 37, 96)
+    e_a = rel_l2(gpu_adjoint(plan, y), oracle.adjoint(case.problem(), y, mode, threads=8))
+    assert e_a < LINEAR_TOL, e_a
+    if mode == "linear":   # exact transposes (nearest_ref's two rounding rules differ by design)
+        lhs = np.vdot(gpu_forward(plan, x), y)
+        rhs = np.vdot(x, gpu_adjoint(plan, y))
+        assert abs(lhs - rhs) / abs(lhs) < 1e-5
+    assert plan.device_flags() == 0
+
+
 @pytest.mark.parametrize("turn", [0.5, -0.5])
 def test_sheared_gather_with_split_bins_matches_oracle(turn):
     """Linear sampling at upsample 128 looking along a diagonal: the backprojection runs on the
