@@ -42,6 +42,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--case", default="config2")
+    ap.add_argument("--interp", choices=["linear", "nearest_ref"], default="linear",
+                    help="interpolation of the --case run (profiling other settings; the headline is linear)")
+    ap.add_argument("--upsample", type=float, default=None, help="upsample ratio of the --case run (default: the case's)")
     ap.add_argument("--cpu-pulses", type=int, default=96, help="pulse sample of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-cgls", action="store_true", help="skip the learned-vs-plain CGLS timing")
@@ -152,9 +155,11 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
     aperture, scene, upsample, desc = config_workload(args.case)
+    if args.upsample:
+        upsample = args.upsample
     S, N, P = aperture.num_slow_times, aperture.num_freqs, scene.num_scatterers
     n = scene.grid_shape[2]
-    op = NumpySimpleSarOperator(scene, aperture, upsample_ratio=upsample, interp="linear", device=dev)
+    op = NumpySimpleSarOperator(scene, aperture, upsample_ratio=upsample, interp=args.interp, device=dev)
     plan = op.plan
     x_true = reflectivity(n, 500, 8.0, SEED, device=dev)
     y = add_noise(plan.forward(x_true), 20.0, SEED + 1)
@@ -240,10 +245,10 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "c64 (fp32 arithmetic; double-float fp32 pairs for range/phase)",
         "data": "synthetic, seeded: 500 point scatterers + Gaussian-filtered (sigma 8 px) clutter x complex "
                 "speckle, forward-projected by this operator, complex white noise at 20 dB SNR",
-        "config": {"workload": f"{args.case}: backprojection, {desc}, linear interpolation",
+        "config": {"workload": f"{args.case}: backprojection, {desc}, {args.interp.replace('_ref', '')} interpolation",
                    "pixels": P, "pulses": S, "samples": N, "upsample": upsample,
                    "l2": "inputs larger than L2 (phase history %.0f MB, stored range profiles %.0f MB)"
-                         % (S * N * 8 / 1e6, S * plan.profile_length * 16 / 1e6),
+                         % (S * N * 8 / 1e6, S * plan.profile_length * (8 if plan.tile_window > 256 else 16) / 1e6),
                    "parallelism": "replicas (each GPU runs the whole workload)" if world > 1 else "single GPU"},
         "stages_ms": {"upsample_fft_side": fft_ms, "gather_kernel": k2_ms},
         "forward": {"value": P * S / (fwd_ms * 1e-3), "unit": UNIT, "ms_per_step": fwd_ms,
@@ -273,7 +278,7 @@ def run_ours(args):
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         result["cpu_baseline"] = cpu_baseline(aperture, scene, upsample, y, args.cpu_pulses, steps=1)
-        check = oracle_check(aperture, scene, upsample, y, x)
+        check = oracle_check(aperture, scene, upsample, y, x, args.interp)
         result["oracle_rel_l2"] = check["rel_l2"]
         result["cpu_baseline"]["oracle_check"] = check
         result["cpu_baseline"]["config1"] = config1_cpu_gpu(dev)
@@ -393,7 +398,7 @@ def cpu_baseline(aperture, scene, upsample, y, pulses, steps=1):
                       f"{secs['nearest_ref']:.2f} s per sample"}
 
 
-def oracle_check(aperture, scene, upsample, y, x_gpu):
+def oracle_check(aperture, scene, upsample, y, x_gpu, mode="linear"):
     """FP64-oracle error of the timed workload's GPU image: the exact 256^2-pixel patch at the
     scene centre over all pulses (CPU-baseline leg; the oracle only checks, it is not timed as ours)."""
     import oracle
@@ -405,12 +410,12 @@ def oracle_check(aperture, scene, upsample, y, x_gpu):
     prob = oracle.Problem(aperture.transmitter_positions, aperture.receiver_positions, aperture.stab_ref_posns,
                           patch, aperture.centre_frequency, aperture.sample_bandwidth, N, upsample_ratio=upsample)
     t0 = time.perf_counter()
-    ref = oracle.adjoint(prob, y.cpu().numpy(), "linear", threads=oracle.default_threads())
+    ref = oracle.adjoint(prob, y.cpu().numpy(), mode, threads=oracle.default_threads())
     dt = time.perf_counter() - t0
     got = x_gpu.reshape(n, n)[j0:j0 + 256, i0:i0 + 256].reshape(-1).cpu().numpy().astype(np.complex128)
     err = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
     return {"rel_l2": err, "pixels": int(patch.shape[0]), "pulses": S, "oracle_seconds": dt,
-            "what": "GPU backprojection of the timed workload vs the FP64 oracle (linear), 256^2 patch at the "
+            "what": f"GPU backprojection of the timed workload vs the FP64 oracle ({mode}), 256^2 patch at the "
                     "scene centre, all pulses; target 1e-5"}
 
 

@@ -801,16 +801,27 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
     const bool up_ok = upsample_fused_supported((int)N, (long)M, p->Lg);
     const bool down_ok = downsample_fused_supported((int)N, (long)M, p->Lg);
     if (up_ok || down_ok) {
-        std::vector<float2> tn(N), tm(M);
+        // tw_m: e^{2 pi i q / M} for q < M, then for each residue r < 2U the 16 thread-independent
+        // factors e^{2 pi i (T e - N [e >= 8]) r / M} (T = N / 16) of the fused kernels' twiddles
+        const size_t U = M / N, T = N / 16;
+        std::vector<float2> tn(N), tm(M + 2 * U * 16);
         const double two_pi = 6.283185307179586476925286766559;
         for (size_t q = 0; q < N; ++q)
             tn[q] = make_float2((float)std::cos(two_pi * (double)q / (double)N), (float)std::sin(two_pi * (double)q / (double)N));
         for (size_t q = 0; q < M; ++q)
             tm[q] = make_float2((float)std::cos(two_pi * (double)q / (double)M), (float)std::sin(two_pi * (double)q / (double)M));
+        for (size_t r = 0; r < 2 * U; ++r)
+            for (size_t e = 0; e < 16; ++e) {
+                const long k = (long)(T * e) - (e >= 8 ? (long)N : 0L);
+                long q = (k * (long)r) % (long)M;   // exact integer phase, then one FP64 angle
+                if (q < 0) q += (long)M;
+                tm[M + 16 * r + e] = make_float2((float)std::cos(two_pi * (double)q / (double)M),
+                                                 (float)std::sin(two_pi * (double)q / (double)M));
+            }
         if ((rc = p->alloc(&p->d_tw_n, N, "twiddles"))) return rc;
-        if ((rc = p->alloc(&p->d_tw_m, M, "twiddles"))) return rc;
+        if ((rc = p->alloc(&p->d_tw_m, tm.size(), "twiddles"))) return rc;
         SAR_CUDA(cudaMemcpy(p->d_tw_n, tn.data(), sizeof(float2) * N, cudaMemcpyHostToDevice), "twiddles");
-        SAR_CUDA(cudaMemcpy(p->d_tw_m, tm.data(), sizeof(float2) * M, cudaMemcpyHostToDevice), "twiddles");
+        SAR_CUDA(cudaMemcpy(p->d_tw_m, tm.data(), sizeof(float2) * tm.size(), cudaMemcpyHostToDevice), "twiddles");
         p->fused_up = up_ok;
         p->fused_down = down_ok;
     }

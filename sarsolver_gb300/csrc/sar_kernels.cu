@@ -1941,9 +1941,12 @@ cudaError_t launch_unpack_pairs(const void* spec, int dbl, const float2* wfac, f
 // keeps the bins of the stored span [bg0, bg0 + Lg] (taken modulo M) and writes the (value,
 // difference) pairs of unpack_pairs_kernel directly: the row is read once (N values) and only the
 // span is written, where the unfused path writes and reads the M-point rows three times.
-// Twiddles come from FP64-computed tables e^{2 pi i q / N} and e^{2 pi i q / M}, each transform's
-// e^{2 pi i k r / M} read from the table at k r mod M (no chained products, so any U keeps FP32
-// accuracy).
+// Twiddles come from FP64-computed tables e^{2 pi i q / N} and e^{2 pi i q / M}.  A thread holds
+// the frequencies k = t + T e (e < 16, minus N for e >= 8), so a transform's e^{2 pi i k r / M}
+// factors into e^{2 pi i t r / M} (one table read per thread, t r < M / 8) times
+// e^{2 pi i (T e - N [e >= 8]) r / M}, the same for every thread (a small table after the first, read
+// as broadcasts): no chained products, so any U keeps FP32 accuracy, and one scattered read per
+// thread and transform instead of sixteen.
 //
 // Staged form (spans whose U residues fit shared memory): the span is gathered residue-major in
 // shared memory and written row-contiguously at the end.  Direct form (longer spans, i.e. large
@@ -2079,12 +2082,16 @@ __device__ __forceinline__ void apply_powers(float2 (&v)[16], float2 w) {
     v[15] = cmulf(v[15], cmulf(w8, w7));
 }
 
-// Table index of e^{2 pi i k r / M} for the FFT-order index kp (signed frequency k = kp or kp - N)
-// and 0 <= r < 2U: |k r| < M < 2^30 (checked by the launchers), so one wrap suffices.
+// e^{2 pi i k r / M} for the 16 frequencies k = t + T e of thread t (signed: minus N for e >= 8),
+// 0 <= r < 2U, as the product of e^{2 pi i t r / M} (tw_m[t r]) and the thread-independent factor
+// tw_e[16 r + e] = e^{2 pi i (T e - N [e >= 8]) r / M} (stored after the M entries of tw_m).
 template <int N>
-__device__ __forceinline__ int tw_index(int kp, int r, int M) {
-    const int kr = (kp < N / 2 ? kp : kp - N) * r;
-    return kr < 0 ? kr + M : kr;
+__device__ __forceinline__ void residue_twiddles(const float2* __restrict__ tw_m, long M, int t, int r,
+                                                 float2 (&w)[16]) {
+    const float2 a = __ldg(tw_m + t * r);
+    const float2* __restrict__ b = tw_m + M + 16 * r;
+#pragma unroll
+    for (int e = 0; e < 16; ++e) w[e] = cmulf(a, __ldg(b + e));
 }
 
 // Radix-16 Stockham pass over N points (sub-transform length ns = N / 256 or N / 16 before it).
@@ -2156,8 +2163,9 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) upsample_pairs_kernel(
         const int r = DIRECT ? bmod + q : q;
         // pass 1 straight from registers: the spectrum times e^{2 pi i k r / M}
         float2 v[16];
+        residue_twiddles<N>(tw_m, M, t, r, v);
 #pragma unroll
-        for (int e = 0; e < 16; ++e) v[e] = cmulf(X[e], __ldg(tw_m + tw_index<N>(t + T * e, r, (int)M)));
+        for (int e = 0; e < 16; ++e) v[e] = cmulf(X[e], v[e]);
         up_first_pass<N>(v, A, t);
         __syncthreads();
         const float2* F = up_passes<N>(A, B, tw_n);   // F[j] = p(U j + r)
@@ -2271,10 +2279,12 @@ __global__ void __launch_bounds__(N / 16, 8192 / N) downsample_forward_kernel(
         __syncthreads();
         const float2* F = up_passes<N>(B, A, tw_n);
         // Y += e^{2 pi i k r / M} F[k]  (conjugate domain)
+        float2 w[16];
+        residue_twiddles<N>(tw_m, M, t, r, w);
 #pragma unroll
         for (int e = 0; e < 16; ++e) {
             const int kp = t + T * e;
-            const float2 c = cmulf(__ldg(tw_m + tw_index<N>(kp, r, (int)M)), F[up_pad(kp)]);
+            const float2 c = cmulf(w[e], F[up_pad(kp)]);
             Y[e].x += c.x;
             Y[e].y += c.y;
         }

@@ -118,7 +118,8 @@ cudaError_t launch_unpack_compact(const float2* compact, int Lc, const float2* w
                                   long M, int Lg, int rows, int first, int linear, cudaStream_t st);
 // Fused adjoint upsampling for N = 1024, 2048 or 4096 and M a multiple of N: pairs over the stored span straight
 // from the fftshifted phase history (replaces pack + inverse FFT + unpack_pairs); twiddle tables
-// tw_n[q] = e^{2 pi i q / N}, tw_m[q] = e^{2 pi i q / M}.
+// tw_n[q] = e^{2 pi i q / N}, tw_m[q] = e^{2 pi i q / M} for q < M, followed by 2 (M / N) x 16 entries
+// tw_m[M + 16 r + e] = e^{2 pi i (e N / 16 - N [e >= 8]) r / M}.
 bool upsample_fused_supported(int N, long M, int Lg);
 size_t upsample_fused_smem_bytes(int N, int Lg, int U);
 cudaError_t launch_upsample_pairs_fused(const float2* y, const float2* wave, const float2* wfac, const float2* tw_n,

@@ -100,6 +100,9 @@ def config_workload(name: str):
     if name == "config2_quarter_turned":
         return (spotlight_aperture(4096, 4096, 5.0, centre_az_deg=90.0), grid_scene(1024, 0.25), 8.0,
                 "4096 pulses x 4096 samples, U=8, 1024^2 at 0.25 m, 5 deg, looking along y")
+    if name == "config2_slice256":
+        return (spotlight_aperture(256, 4096, 5.0 * 256 / 4096), grid_scene(2048, 0.25), 8.0,
+                "256 of 4096 pulses x 4096 samples (the same pulse spacing), U=8, 2048^2 at 0.25 m")
     if name == "config2_quarter_diagonal":
         return (spotlight_aperture(4096, 4096, 5.0, centre_az_deg=45.0), grid_scene(1024, 0.25), 8.0,
                 "4096 pulses x 4096 samples, U=8, 1024^2 at 0.25 m, 5 deg, looking along the grid diagonal")
