@@ -973,7 +973,7 @@ __device__ __forceinline__ RowEval<PRECISE> scatter_eval(const ColumnTerms& ct, 
     e.bp = bin_position<PRECISE>(v, PRECISE ? fmaf(ib, dj, ct.ci) : 0.f);
     float sn, cn;
     __sincosf(SAR_TWO_PI * ph, &sn, &cn);   // |ph| < ~5 cycles: the caller reduced the constants
-    e.cr = xv.x * cn - xv.y * sn;   // x * exp(+2 pi i f)
+    e.cr = fmaf(xv.x, cn, -xv.y * sn);   // x * exp(+2 pi i f)
     e.ci = fmaf(xv.x, sn, xv.y * cn);
     return e;
 }
@@ -1023,6 +1023,7 @@ __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, 
     cp.b1 -= rintf(cp.b1);
     cq.cph -= rintf(cq.cph);
     cq.b1 -= rintf(cq.b1);
+    unsigned edge = 0;   // nearest bins: bit 2 row + h for the pulse h contribution near a rounding boundary
 #pragma unroll 2
     for (int rr = 0; rr < 16; ++rr) {
         const float dj = (float)(rr - 8);
@@ -1066,51 +1067,49 @@ __device__ __forceinline__ void scatter_rows(const ColumnTerms& ctp, float c9p, 
                 }
             }
         } else {
-            bool fp = false, fq = false;
-            int xp = ip, xq = iq;
-            if (PRECISE) {   // nearest bins are always split: re-decide those near a boundary
-                fp = fabsf(ep.bp.s) > kNearEdge;
-                fq = TWO && fabsf(eq.bp.s) > kNearEdge;
-                if (fp || fq) {
-                    const int pj = nc.j0 + (nc.transposed ? lane : rr);
-                    const int pi = nc.i0 + (nc.transposed ? rr : lane) + nc.a_off + nc.shear * pj;
-                    // the exact bin (bins from bg0) as a window slot
-                    if (fp) {
-                        const int b = exact_grid_bin(nc.steps, nc.pulses, nc.alpha2, nc.sr_hi, nc.sr_lo, nc.bg0,
-                                                     BIN_FWD_NEAREST, pi, pj, nc.k, nc.sp) + nc.bg0;
-                        xp = RING ? (b & mask) : min(max(b - nc.wsp, 0), ws - 1);
-                    }
-                    if (fq) {
-                        const int b = exact_grid_bin(nc.steps, nc.pulses, nc.alpha2, nc.sr_hi, nc.sr_lo, nc.bg0,
-                                                     BIN_FWD_NEAREST, pi, pj, nc.k, nc.sq) + nc.bg0;
-                        xq = RING ? (b & mask) : min(max(b - nc.wsq, 0), ws - 1);
-                    }
-                }
-            }
+            if (PRECISE)   // decided again after the rows, off the common path
+                edge |= ((fabsf(ep.bp.s) > kNearEdge ? 1u : 0u) | (TWO && fabsf(eq.bp.s) > kNearEdge ? 2u : 0u))
+                        << (2 * rr);
             if (MODE >= 1) {
-                if (!fp) rmw_add(wp, ip, 1.0f, ep.cr, ep.ci);
-                if (TWO && !fq) rmw_add(wq, iq, 1.0f, eq.cr, eq.ci);
+                rmw_add(wp, ip, 1.0f, ep.cr, ep.ci);
+                if (TWO) rmw_add(wq, iq, 1.0f, eq.cr, eq.ci);
                 __syncwarp();
-                if (PRECISE && __any_sync(0xffffffffu, fp || fq)) {
-                    if (fp) {
-                        float2* a0 = wp + wslot(xp);
-                        atomicAdd(&a0->x, ep.cr); atomicAdd(&a0->y, ep.ci);
-                    }
-                    if (fq) {
-                        float2* b0 = wq + wslot(xq);
-                        atomicAdd(&b0->x, eq.cr); atomicAdd(&b0->y, eq.ci);
-                    }
-                    __syncwarp();
-                }
             } else {
-                float2* a0 = wp + wslot(xp);
+                float2* a0 = wp + wslot(ip);
                 atomicAdd(&a0->x, ep.cr); atomicAdd(&a0->y, ep.ci);
                 if (TWO) {
-                    float2* b0 = wq + wslot(xq);
+                    float2* b0 = wq + wslot(iq);
                     atomicAdd(&b0->x, eq.cr); atomicAdd(&b0->y, eq.ci);
                 }
             }
         }
+    }
+    if (!LINEAR && PRECISE && __any_sync(0xffffffffu, edge != 0u)) {
+        // Contributions whose FP32 bin position lay within 5e-5 of a rounding boundary: the exact bin
+        // from the per-pixel double-float range; where it differs from the FP32 bin (where the rows
+        // added it) the contribution moves there, with shared-memory atomics (the lanes' exact bins
+        // may coincide).  The row's evaluation is repeated exactly as the rows made it.
+        for (unsigned m = edge; m != 0u; m &= m - 1u) {
+            const int bit = __ffs(m) - 1, rr = bit >> 1, h = bit & 1;
+            const float dj = (float)(rr - 8);
+            const float2 xv = staged_value(xrow[rr * kXtStride + lane]);
+            const RowEval<PRECISE> e = h ? scatter_eval<PRECISE>(cq, c9q, w9q, ibq, dj, xv)
+                                         : scatter_eval<PRECISE>(cp, c9p, w9p, ibp, dj, xv);
+            const int off = h ? off_q : off_p;
+            const int i32 = RING ? ((e.bp.n + off) & mask) : (int)min((unsigned)(e.bp.n + off), (unsigned)(ws - 2));
+            const int pj = nc.j0 + (nc.transposed ? lane : rr);
+            const int pi = nc.i0 + (nc.transposed ? rr : lane) + nc.a_off + nc.shear * pj;
+            const int bx = exact_grid_bin(nc.steps, nc.pulses, nc.alpha2, nc.sr_hi, nc.sr_lo, nc.bg0, BIN_FWD_NEAREST,
+                                          pi, pj, nc.k, h ? nc.sq : nc.sp) + nc.bg0;
+            const int ix = RING ? (bx & mask) : min(max(bx - (h ? nc.wsq : nc.wsp), 0), ws - 1);
+            if (ix == i32) continue;
+            float2* w = h ? wq : wp;
+            atomicAdd(&w[wslot(i32)].x, -e.cr);
+            atomicAdd(&w[wslot(i32)].y, -e.ci);
+            atomicAdd(&w[wslot(ix)].x, e.cr);
+            atomicAdd(&w[wslot(ix)].y, e.ci);
+        }
+        __syncwarp();
     }
 }
 
