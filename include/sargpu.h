@@ -48,7 +48,8 @@ extern "C" {
 
 /* Device check flags reported by sar_device_flags(). */
 #define SAR_FLAG_TILE_WINDOW 1u   /* a tile's staged window left the stored profile span */
-#define SAR_FLAG_STRIP_WINDOW 2u  /* a forward strip window left the stored profile span */
+#define SAR_FLAG_STRIP_WINDOW 2u  /* a forward strip window left the stored profile span, or a tile's
+                                     bins left the range its ring window holds */
 #define SAR_FLAG_WAIT_TIMEOUT 8u  /* a bounded in-kernel wait expired; that call's result is invalid */
 #define SAR_FLAG_GATHER_WINDOW 16u /* a pixel's range bin could fall outside its tile's staged window
                                       (window narrower than the tile's bin extent); result suspect */
@@ -123,9 +124,9 @@ typedef struct sar_plan_info {
     int gather_lanes_y;         /* 1: the grid backprojection runs warp lanes along y (bins change
                                    more slowly along y than along x), 0: along x */
     int fused_upsampling;       /* 1: the backprojection's range profiles come from the fused
-                                   upsampling kernel (N = 1024, 2048 or 4096, M a multiple of N), 0: cuFFT */
+                                   upsampling kernel (N = 512 ... 8192, M a multiple of N), 0: cuFFT */
     int fused_downsampling;     /* 1: the forward projection's FFT side is the fused downsampling
-                                   kernel (N = 1024, 2048 or 4096, M a multiple of N), 0: cuFFT */
+                                   kernel (N = 512 ... 8192, M a multiple of N), 0: cuFFT */
     int scatter_lanes_y;        /* 1: the grid forward scatter runs warp lanes along y and walks the
                                    tile along x (bins change more slowly along x), 0: lanes along x */
     size_t block_pulses;        /* streamed plan: pulses per block (0: resident plan) */

@@ -795,7 +795,7 @@ int build_plan(const sar_geometry* g_in, sar_plan* p) {
         p->have_tail = true;
         p->tail_rows = tail;
     }
-    // Fused adjoint upsampling: for N = 1024, 2048 or 4096 and M a multiple of N the backprojection's range
+    // Fused adjoint upsampling: for N = 512, 1024, 2048, 4096 or 8192 and M a multiple of N the backprojection's range
     // profiles come from one kernel (U-way split of the length-M transform into N-point ones,
     // stored span only) instead of pack + inverse FFT + unpack; twiddles computed in FP64.
     const bool up_ok = upsample_fused_supported((int)N, (long)M, p->Lg);

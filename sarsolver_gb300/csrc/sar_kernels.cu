@@ -1930,7 +1930,7 @@ cudaError_t launch_unpack_pairs(const void* spec, int dbl, const float2* wfac, f
 }
 
 // ------------------------------------------- K1 fused: upsampling FFT straight into pairs
-// For N = 1024, 2048 or 4096 and M = U N (integer U): bin b = U j + r of the inverse length-M transform of the
+// For N = 512, 1024, 2048, 4096 or 8192 and M = U N (integer U): bin b = U j + r of the inverse length-M transform of the
 // zero-padded spectrum (frequencies k in [-N/2, N/2), X_k = conj(W) y at k mod N) is
 //   p(U j + r) = sum_k X_k e^{2 pi i k r / M} e^{2 pi i k j / N},
 // an N-point inverse DFT of the spectrum twiddled by e^{2 pi i k r / M} (the same holds for any
@@ -2235,7 +2235,7 @@ static int up_stage_row(int Lg, int U) {
     return ((n + 13) & ~15) + 2;
 }
 
-// Fused forward downsampling for N = 1024, 2048 or 4096, M = U N: the transpose of the fused upsampling.  With
+// Fused forward downsampling for N = 512 ... 8192, M = U N: the transpose of the fused upsampling.  With
 // the accumulated bins a[b] (b = U j + r, taken modulo M) the forward transform at frequency k in
 // [-N/2, N/2) is  K(k) = sum_r e^{-2 pi i k r / M} DFT_N(a_r)[k mod N],  a_r[j] = a[U j + r]; each
 // forward DFT is computed as conj(inverse DFT(conj a_r)) with the Stockham passes above, and

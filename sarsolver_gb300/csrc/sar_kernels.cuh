@@ -11,7 +11,8 @@ namespace sar {
 // Device check flags (OR-ed into a plan-owned word; read back by sar_device_flags()).
 enum : unsigned {
     FLAG_TILE_WINDOW = 1u,    // a tile's staged window left the stored profile span
-    FLAG_STRIP_WINDOW = 2u,   // a forward strip window left the stored profile span
+    FLAG_STRIP_WINDOW = 2u,   // a forward strip window left the stored profile span, or a tile's bins
+                              // left its ring window's range
     FLAG_BIN_CLAMP = 4u,      // a per-pixel bin index was clamped (debug builds only)
     FLAG_WAIT_TIMEOUT = 8u,   // a bounded mbarrier wait gave up (the result is invalid)
     FLAG_GATHER_WINDOW = 16u, // a sub-tile's bin extent exceeded its tile's staged window
@@ -116,7 +117,7 @@ cudaError_t launch_pack_adjoint(const float2* y, const float2* wave, void* spec,
                                 int first, cudaStream_t st);
 cudaError_t launch_unpack_compact(const float2* compact, int Lc, const float2* wfac, float4* pairs, float2* prof,
                                   long M, int Lg, int rows, int first, int linear, cudaStream_t st);
-// Fused adjoint upsampling for N = 1024, 2048 or 4096 and M a multiple of N: pairs over the stored span straight
+// Fused adjoint upsampling for N = 512, 1024, 2048, 4096 or 8192 and M a multiple of N: pairs over the stored span straight
 // from the fftshifted phase history (replaces pack + inverse FFT + unpack_pairs); twiddle tables
 // tw_n[q] = e^{2 pi i q / N}, tw_m[q] = e^{2 pi i q / M} for q < M, followed by 2 (M / N) x 16 entries
 // tw_m[M + 16 r + e] = e^{2 pi i (e N / 16 - N [e >= 8]) r / M}.
@@ -125,7 +126,7 @@ size_t upsample_fused_smem_bytes(int N, int Lg, int U);
 cudaError_t launch_upsample_pairs_fused(const float2* y, const float2* wave, const float2* wfac, const float2* tw_n,
                                         const float2* tw_m, float4* pairs, int N, long M, int Lg, long bg0, int rows,
                                         int first, int linear, cudaStream_t st);
-// Fused forward downsampling for N = 1024, 2048 or 4096, M a multiple of N and Lg <= M: y straight from the
+// Fused forward downsampling for N = 512 ... 8192, M a multiple of N and Lg <= M: y straight from the
 // bin accumulator acc [S][Lg] (replaces pack_forward + forward FFT + extract_forward).
 bool downsample_fused_supported(int N, long M, int Lg);
 cudaError_t launch_downsample_forward_fused(const float2* acc, const float2* wave, const float2* wfac,
