@@ -44,6 +44,26 @@ def test_streamed_plan_matches_resident(interp, block):
     assert stm.device_flags() == 0 and res.device_flags() == 0
 
 
+@pytest.mark.parametrize("interp", ["linear", "nearest_ref"])
+def test_streamed_plan_with_ring_and_value_windows(interp):
+    """Upsample 128 on 0.25 m pixels with a 20 degree aperture: the forward scatter keeps ring
+    windows and the backprojection stages windows of plain values; streamed in blocks of 24 pulses
+    (ring slots of 8-byte rows, the scatter per block) the plan equals the resident one."""
+    rng = np.random.default_rng(5)
+    case = spotlight_case(64, 96, 100, 0.25, 20.0, upsample=128.0, weights=np.exp(1j * rng.uniform(-1, 1, 64)))
+    res = SarPlan(case.scene, case.aperture, upsample_ratio=128.0, interp=interp)
+    stm = SarPlan(case.scene, case.aperture, upsample_ratio=128.0, interp=interp, block_pulses=24)
+    assert stm.block_pulses == 24
+    assert res.scatter_ring_half > 0 and stm.scatter_ring_half > 0 and res.tile_window > 256
+    x = torch.from_numpy(crandn(rng, case.scene.num_scatterers)).to(torch.complex64).cuda()
+    y = torch.from_numpy(crandn(rng, 64, 96)).to(torch.complex64).cuda()
+    assert rel_l2(stm.forward(x).cpu().numpy(), res.forward(x).cpu().numpy()) < 1e-6
+    ref = res.adjoint(y).cpu().numpy()
+    assert rel_l2(stm.adjoint(y).cpu().numpy(), ref) < 2e-6
+    assert rel_l2(stm.adjoint_streamed(y.cpu().pin_memory(), block=24).cpu().numpy(), ref) < 2e-6
+    assert stm.device_flags() == 0 and res.device_flags() == 0
+
+
 def test_resident_pulse_blocks_nearest_ref_match_whole():
     """Pulse blocks of a resident plan in nearest_ref: exact re-decisions use the block's own pulses."""
     rng = np.random.default_rng(4)
