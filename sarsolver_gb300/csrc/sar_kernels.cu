@@ -486,11 +486,14 @@ __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __
 __device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 // 16-byte shared-memory load at a 32-bit shared address.
+// volatile: the loads stay after the (volatile) mbarrier wait that publishes the staged windows,
+// which a non-volatile statement without a memory clobber could be moved across.
 __device__ __forceinline__ float4 lds_f4(uint32_t addr) {
     float4 v;
-    asm("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(addr));
     return v;
 }
+
 
 __device__ __forceinline__ void producer_coeffs_pair(const GridConst& g, const PulseGeom* __restrict__ pulses, int s0,
                                                      int npb, int pass, const df3* anchors, float4* coef, int* base,
