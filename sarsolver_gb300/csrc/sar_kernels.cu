@@ -494,7 +494,6 @@ __device__ __forceinline__ float4 lds_f4(uint32_t addr) {
     return v;
 }
 
-
 __device__ __forceinline__ void producer_coeffs_pair(const GridConst& g, const PulseGeom* __restrict__ pulses, int s0,
                                                      int npb, int pass, const df3* anchors, float4* coef, int* base,
                                                      int lane, int ww, unsigned* flags) {
