@@ -263,6 +263,37 @@ def test_ring_windows_match_oracle(turn, mode):
 
 
 @pytest.mark.parametrize("turn", [0.5, -0.5])
+def test_sheared_lattices_on_a_non_square_volume(turn):
+    """The sheared lattices on a 2 x 40 x 70 grid (two height planes, 0.3 m pixels, not square) seen
+    along a diagonal: lattice widths nx + (ny - 1), tiles clipped to the image per column, both
+    planes; linear forward and backprojection against the FP64 oracle and their dot product."""
+    rng = np.random.default_rng(81)
+    base = spotlight_case(29, 96, 8, 0.3, 4.0, weights=np.exp(1j * rng.uniform(-3, 3, 29)))
+    c, s_ = np.cos(turn * np.pi / 2), np.sin(turn * np.pi / 2)
+    rot = np.array([[c, -s_, 0.0], [s_, c, 0.0], [0.0, 0.0, 1.0]])
+    ap = base.aperture
+    ap = NumpySimpleSarAperture(ap.transmitter_positions @ rot.T, ap.receiver_positions @ rot.T, ap.stab_ref_posns,
+                                ap.centre_frequency, ap.sample_bandwidth, num_freqs=ap.num_freqs,
+                                slow_time_weighting=ap.slow_time_weighting)
+    scene = GridSarScene([2, 40, 70], [0.5, 0.3 * 39, 0.3 * 69])
+    from cases import Case
+    case = Case(scene, ap, 8.0, {})
+    plan = SarPlan(scene, ap, upsample_ratio=8.0, interp="linear", path="grid")
+    m = -1 if turn > 0 else 1
+    assert plan.scatter_shear == m and plan.gather_shear == m
+    x = crandn(rng, scene.num_scatterers)
+    e_f = rel_l2(gpu_forward(plan, x), oracle.forward(case.problem(), x, "linear", threads=8))
+    assert e_f < LINEAR_TOL, e_f
+    y = crandn(rng, 29, 96)
+    e_a = rel_l2(gpu_adjoint(plan, y), oracle.adjoint(case.problem(), y, "linear", threads=8))
+    assert e_a < LINEAR_TOL, e_a
+    lhs = np.vdot(gpu_forward(plan, x), y)
+    rhs = np.vdot(x, gpu_adjoint(plan, y))
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+    assert plan.device_flags() == 0
+
+
+@pytest.mark.parametrize("turn", [0.5, -0.5])
 def test_sheared_gather_with_split_bins_matches_oracle(turn):
     """Linear sampling at upsample 128 looking along a diagonal: the backprojection runs on the
     sheared lattice with split bins (windows wider than 256 bins: exact integer parts), the
