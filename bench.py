@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--cpu-pulses", type=int, default=96, help="pulse sample of the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-cgls", action="store_true", help="skip the learned-vs-plain CGLS timing")
+    ap.add_argument("--no-settings", action="store_true",
+                    help="skip the other-settings timings (turned, diagonal, the reference's defaults)")
     ap.add_argument("--cgls-scenes", type=int, default=8)
     ap.add_argument("--suite", choices=["cgls", "autofocus", "resample", "cphd", "pdhg", "settings", "unet"],
                     default=None, help="run one of the library's other workloads instead of the benchmark")
@@ -269,7 +271,6 @@ def run_ours(args):
         "e2e": {"value": job_throughput(P * S, world, e2e_ms), "unit": UNIT, "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": S * N * 8, "d2h_bytes_per_step": P * 8,
                 "api": "NumpySimpleSarOperator.backproject(pinned host complex64 tensor) -> pinned host copy"},
-        # our kernels per call: pack + unpack per FFT chunk, then the gather (cuFFT's own excluded)
         # our kernels per backprojection: per FFT chunk the fused upsampling kernel, or the packing
         # and unpacking kernels around cuFFT; then the gather
         "gpu_launches": args.steps * ((1 if plan.fused_upsampling else 2)
@@ -285,6 +286,16 @@ def run_ours(args):
         result["cpu_baseline"]["config4_lsqr"] = config4_lsqr_reference()
     if rank == 0 and not args.no_cgls:
         result["cgls"] = learned_vs_plain(args.cgls_scenes)
+    if rank == 0 and not args.no_settings and args.case == "config2" and args.interp == "linear" and not args.upsample:
+        # the same image and collection under the other settings (not the metric): looking along y
+        # and along the diagonal, and the reference's defaults (nearest_ref, upsample 128)
+        rows = settings_workload(rows=(("config2_turned", "linear", 8.0, "auto"),
+                                       ("config2_diagonal", "linear", 8.0, "auto"),
+                                       ("config2", "nearest_ref", 128.0, "auto")), verbose=False)
+        result["settings"] = [{k: r[k] for k in ("case", "interp", "upsample", "adjoint_ms", "forward_ms",
+                                                 "gather_shear", "scatter_shear", "scatter_ring_half")}
+                              | {"gather_kernel_ms": r["adjoint_stages_ms"][1],
+                                 "scatter_kernel_ms": r["forward_stages_ms"][1]} for r in rows]
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
@@ -754,19 +765,23 @@ def cphd_workload() -> dict:
     return out
 
 
-def settings_workload() -> list:
+SETTINGS_ROWS = (("config2", "linear", 8.0, "auto"), ("config2_turned", "linear", 8.0, "auto"),
+                 ("config2_diagonal", "linear", 8.0, "auto"), ("config2", "nearest_ref", 8.0, "auto"),
+                 ("config2", "linear", 128.0, "auto"), ("config2", "nearest_ref", 128.0, "auto"),
+                 ("config2", "nearest_ref", 128.0, "points"))
+
+
+def settings_workload(rows=SETTINGS_ROWS, verbose: bool = True) -> list:
     """The benchmark scene under other operator settings: linear / nearest_ref interpolation, upsample
-    8 / 128 (the reference's default), and the collection turned by 90 degrees (range along y).
-    Mean of 3 calls after one warm-up, CUDA events around each operator call."""
+    8 / 128 (the reference's default), and the collection turned by 90 degrees (range along y) or
+    looking along the grid diagonal.  Mean of 3 calls after one warm-up, CUDA events around each
+    operator call."""
     import torch
 
     from sarsolver_gb300.plan import SarPlan
     from sarsolver_gb300.scenes import config_workload
     out = []
-    for case, interp, U, path in (("config2", "linear", 8.0, "auto"), ("config2_turned", "linear", 8.0, "auto"),
-                                  ("config2_diagonal", "linear", 8.0, "auto"),
-                                  ("config2", "nearest_ref", 8.0, "auto"), ("config2", "linear", 128.0, "auto"),
-                                  ("config2", "nearest_ref", 128.0, "auto"), ("config2", "nearest_ref", 128.0, "points")):
+    for case, interp, U, path in rows:
         aperture, scene, _, _ = config_workload(case)
         plan = SarPlan(scene, aperture, upsample_ratio=U, interp=interp, path=path)
         g = torch.Generator(device="cuda")
@@ -778,7 +793,9 @@ def settings_workload() -> list:
         row = {"workload": "settings", "case": case, "interp": interp, "upsample": U, "path": path,
                "grid_path": plan.is_grid,
                "tile_window": plan.tile_window, "strip_window": plan.strip_window,
-               "gather_lanes_y": plan.gather_lanes_y, "scatter_lanes_y": plan.scatter_lanes_y}
+               "gather_lanes_y": plan.gather_lanes_y, "scatter_lanes_y": plan.scatter_lanes_y,
+               "gather_shear": plan.gather_shear, "scatter_shear": plan.scatter_shear,
+               "scatter_ring_half": plan.scatter_ring_half}
         for name, fn in (("adjoint_ms", lambda: plan.adjoint(y)), ("forward_ms", lambda: plan.forward(x))):
             fn()
             plan.enable_stage_timing(True)
@@ -792,7 +809,8 @@ def settings_workload() -> list:
         plan.close()
         del y, x
         torch.cuda.empty_cache()
-        print(json.dumps(row), flush=True)
+        if verbose:
+            print(json.dumps(row), flush=True)
         out.append(row)
     return out
 
