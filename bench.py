@@ -766,15 +766,16 @@ def cphd_workload() -> dict:
 
 
 SETTINGS_ROWS = (("config2", "linear", 8.0, "auto"), ("config2_turned", "linear", 8.0, "auto"),
-                 ("config2_diagonal", "linear", 8.0, "auto"), ("config2", "nearest_ref", 8.0, "auto"),
+                 ("config2_diagonal", "linear", 8.0, "auto"), ("config2_steep", "linear", 8.0, "auto"),
+                 ("config2", "nearest_ref", 8.0, "auto"),
                  ("config2", "linear", 128.0, "auto"), ("config2", "nearest_ref", 128.0, "auto"),
                  ("config2", "nearest_ref", 128.0, "points"))
 
 
 def settings_workload(rows=SETTINGS_ROWS, verbose: bool = True) -> list:
     """The benchmark scene under other operator settings: linear / nearest_ref interpolation, upsample
-    8 / 128 (the reference's default), and the collection turned by 90 degrees (range along y) or
-    looking along the grid diagonal.  Mean of 3 calls after one warm-up, CUDA events around each
+    8 / 128 (the reference's default), and the collection turned by 90 degrees (range along y),
+    looking along the grid diagonal or at 63.4 degrees to x.  Mean of 3 calls after one warm-up, CUDA events around each
     operator call."""
     import torch
 

@@ -187,16 +187,22 @@ constexpr double kShearWalk = 0.25;
 
 // Shear of the backprojection's lattice: its lanes run along the lattice's second axis (steps
 // ey + m ex), so that a quarter-warp's window loads land on one or two bins and are broadcast.
-// Returns m in {-1, +1} when the better plain lane axis still changes by more than half a bin per
-// pixel over the pulses (bank-conflicted loads: collections looking across the grid axes) and the
-// sheared axis changes by less than half of that; 0 otherwise.
+// Returns m in {-2, -1, +1, +2} (the one whose axis changes least) when the better plain lane axis
+// still changes by more than kGatherShearRate bins per pixel over the pulses (bank-conflicted
+// loads: collections looking across the grid axes, e.g. at 45 or 63 degrees) and the sheared axis
+// changes by less than half of that; 0 otherwise.  Below that rate the plain layout's loads cost
+// less than the lattice's partial tiles at the image's edges (measured, 2048^2 at 0.25 m, 4096
+// pulses, linear: looking at 63.4 degrees, 1.16 bins per pixel at upsample 8, the m = -2 lattice
+// took 16.7 ms against 15.4 ms; at 2.32 (upsample 16) 16.6 against 18.6 ms; on the diagonal, 1.76
+// at upsample 8, the m = -1 lattice 16.1 against 17.6 ms).
+constexpr double kGatherShearRate = 1.5;
 static inline int choose_gather_shear(const double* tx, const double* rx, size_t S, const double* origin,
                                       const double* ex, const double* ey, const double* ez, int nx, int ny, int nz,
                                       double s_r) {
     double c[3];
     for (int d = 0; d < 3; ++d)
         c[d] = origin[d] + 0.5 * ((nx - 1) * ex[d] + (ny - 1) * ey[d] + (nz - 1) * ez[d]);
-    double ax = 0.0, ay = 0.0, am[2] = {0.0, 0.0};
+    double ax = 0.0, ay = 0.0, am[4] = {0.0, 0.0, 0.0, 0.0};   // m = -2, -1, +1, +2
     for (size_t s = 0; s < S; ++s) {
         double gx = 0.0, gy = 0.0;
         for (int ant = 0; ant < 2; ++ant) {
@@ -210,12 +216,17 @@ static inline int choose_gather_shear(const double* tx, const double* rx, size_t
         if (!isfinite(gx) || !isfinite(gy)) return 0;
         ax = fmax(ax, fabs(gx) * s_r);
         ay = fmax(ay, fabs(gy) * s_r);
-        am[0] = fmax(am[0], fabs(gy - gx) * s_r);
-        am[1] = fmax(am[1], fabs(gy + gx) * s_r);
+        am[0] = fmax(am[0], fabs(gy - 2.0 * gx) * s_r);
+        am[1] = fmax(am[1], fabs(gy - gx) * s_r);
+        am[2] = fmax(am[2], fabs(gy + gx) * s_r);
+        am[3] = fmax(am[3], fabs(gy + 2.0 * gx) * s_r);
     }
     const double plain = fmin(ax, ay);
-    const int m = am[0] <= am[1] ? -1 : 1;
-    return (plain > 0.5 && am[m > 0] < 0.5 * plain) ? m : 0;
+    int best = 1;
+    for (int i = 0; i < 4; ++i)
+        if (am[i] < am[best]) best = i;
+    const int m = best < 2 ? best - 2 : best - 1;
+    return (plain > kGatherShearRate && am[best] < 0.5 * plain) ? m : 0;
 }
 static inline int choose_shear(const double* tx, const double* rx, size_t S, const double* origin,
                                const double* ex, const double* ey, const double* ez, int nx, int ny, int nz,

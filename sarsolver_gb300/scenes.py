@@ -109,6 +109,9 @@ def config_workload(name: str):
     if name == "config2_diagonal":
         return (spotlight_aperture(4096, 4096, 5.0, centre_az_deg=45.0), grid_scene(2048, 0.25), 8.0,
                 "4096 pulses x 4096 samples, U=8, 2048^2 at 0.25 m, 5 deg, looking along the grid diagonal")
+    if name == "config2_steep":
+        return (spotlight_aperture(4096, 4096, 5.0, centre_az_deg=63.43), grid_scene(2048, 0.25), 8.0,
+                "4096 pulses x 4096 samples, U=8, 2048^2 at 0.25 m, 5 deg, looking at 63.4 deg to x (tan 2)")
     if name == "config3":
         return (spotlight_aperture(2048, 2048, 3.0), grid_scene(1024, 0.25), 8.0,
                 "2048 pulses x 2048 samples, U=8, 1024^2 at 0.25 m")

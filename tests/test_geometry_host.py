@@ -397,6 +397,21 @@ def test_scatter_shear_choice(az, expect):
         assert choose_shear(scene, tx, tx, 200.0e6 * U / C, gather=True) == expect
 
 
+@pytest.mark.parametrize("U", [8, 16, 128])
+@pytest.mark.parametrize("az,expect", [(63.43, -2), (116.57, 2), (26.57, 0)])
+def test_gather_shear_by_two(az, expect, U):
+    """Collections looking at ~63 (or 117) degrees: from upsample 16 on, the backprojection's lanes
+    run along ey -+ 2 ex, where the bins change least; at upsample 8 the better plain axis changes
+    by only ~1.2 bins per pixel, below the rate where the lattice pays, and the plain layout stays.
+    The scatter keeps its plain layout throughout.  At ~27 degrees no shear of ey fits (it would
+    take ex + 2 ey)."""
+    tx = spotlight(4096, 5.0, centre_az_deg=az)
+    n, spacing = 2048, 0.25
+    scene = GridSarScene([1, n, n], [0.0, spacing * (n - 1), spacing * (n - 1)])
+    assert choose_shear(scene, tx, tx, 200.0e6 * U / C, gather=True) == (expect if U > 8 else 0)
+    assert choose_shear(scene, tx, tx, 200.0e6 * 8 / C) == 0
+
+
 @pytest.mark.parametrize("az,lanes", [(45.0, False), (135.0, False), (45.0, True)])
 def test_sheared_lattice_precision_and_walk(az, lanes):
     """The benchmark image seen along a diagonal, on the sheared lattice the forward scatter

@@ -319,6 +319,33 @@ def test_sheared_gather_with_split_bins_matches_oracle(turn):
     assert plan.device_flags() == 0
 
 
+@pytest.mark.parametrize("U", [16.0, 128.0])
+@pytest.mark.parametrize("az,m", [(63.43, -2), (-63.43, 2), (116.57, 2)])
+def test_gather_lattice_sheared_by_two(az, m, U):
+    """Collections looking at ~63 degrees to the grid's x axis (tan = 2): the bins change least
+    along ey - 2 ex (or ey + 2 ex), so the linear backprojection runs on a lattice sheared by two
+    pixels per row (lattice width nx + 2 (ny - 1), slanted tile clipping at every image edge) with
+    its lanes along that axis; the forward projection keeps the plain layout.  Against the FP64
+    oracle at upsample 16 and 128 (split bins), with an odd pulse count."""
+    rng = np.random.default_rng(91)
+    case = spotlight_case(37, 96, 70, 0.3, 4.0, upsample=U, weights=np.exp(1j * rng.uniform(-3, 3, 37)))
+    c, s_ = np.cos(np.radians(az)), np.sin(np.radians(az))
+    rot = np.array([[c, -s_, 0.0], [s_, c, 0.0], [0.0, 0.0, 1.0]])
+    ap = case.aperture
+    case.aperture = NumpySimpleSarAperture(ap.transmitter_positions @ rot.T, ap.receiver_positions @ rot.T,
+                                           ap.stab_ref_posns, ap.centre_frequency, ap.sample_bandwidth,
+                                           num_freqs=ap.num_freqs, slow_time_weighting=ap.slow_time_weighting)
+    plan = SarPlan(case.scene, case.aperture, upsample_ratio=U, interp="linear", path="grid")
+    assert plan.gather_shear == m and plan.scatter_shear == 0
+    y = crandn(rng, 37, 96)
+    e_a = rel_l2(gpu_adjoint(plan, y), oracle.adjoint(case.problem(), y, "linear", threads=8))
+    assert e_a < LINEAR_TOL, e_a
+    x = crandn(rng, case.scene.num_scatterers)
+    e_f = rel_l2(gpu_forward(plan, x), oracle.forward(case.problem(), x, "linear", threads=8))
+    assert e_f < LINEAR_TOL, e_f
+    assert plan.device_flags() == 0
+
+
 @pytest.mark.parametrize("mode,srp_shift,nf,U,spacing,direct", [
     ("linear", 0.0, 4096, 8, 0.5, False), ("nearest_ref", 0.0, 4096, 8, 0.5, False),
     ("linear", 1.0, 4096, 8, 0.5, False), ("linear", 0.0, 2048, 8, 0.5, False),
