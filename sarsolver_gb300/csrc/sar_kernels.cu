@@ -1199,6 +1199,16 @@ __device__ __forceinline__ void scatter_rows_runs(const ColumnTerms& ctp, float 
   }
 }
 
+// Mode of a pulse pair that shares one pass over the rows: a mode both pulses' guarantees admit.
+// The run modes nest (16-row runs imply 8- and 4-row runs), so two of them take the smaller; any
+// other two different modes share only the distinct-bin guarantee (a run mode may rest on MODE 1's
+// rather than MODE 2's) or nothing (MODE 0).
+__device__ __forceinline__ int pair_mode(int a, int b) {
+    if (a == b) return a;
+    if (a >= 3 && b >= 3) return min(a, b);
+    return min(min(a, b), 1);
+}
+
 template <bool LINEAR, bool PRECISE, bool TWO, typename XT, bool RING = false>
 __device__ __forceinline__ void scatter_half(int mode, const ColumnTerms& ctp, float c9p, float w9p, float ibp,
                                              const ColumnTerms& ctq, float c9q, float w9q, float ibq,
@@ -1432,7 +1442,7 @@ __global__ void __launch_bounds__(kWsThreads, RING ? 1 : 2) fp_grid_ws_kernel(co
                 float2* wq = win + pq * wslots;
                 const int off_p = base0[b * pbf + p] - wst[p];    // ring: the absolute base bin
                 const int off_q = base0[b * pbf + pq] - wst[pq];
-                const int mode = two ? min(fast0[b * pbf + p], fast0[b * pbf + p2]) : fast0[b * pbf + p];
+                const int mode = two ? pair_mode(fast0[b * pbf + p], fast0[b * pbf + p2]) : fast0[b * pbf + p];
 #pragma unroll
                 for (int half = 0; half < 2; ++half) {
                     float c9p, w9p, ibp, c9q, w9q, ibq;
