@@ -130,11 +130,14 @@ typedef struct sar_plan_info {
     int scatter_lanes_y;        /* 1: the grid forward scatter runs warp lanes along y and walks the
                                    tile along x (bins change more slowly along x), 0: lanes along x */
     size_t block_pulses;        /* streamed plan: pulses per block (0: resident plan) */
-    int scatter_shear;          /* m != 0: the grid forward scatter walks the rows of a sheared
+    int scatter_shear;          /* m = +-1: the grid forward scatter walks the rows of a sheared
                                    lattice (steps ex, ey + m ex) that follow the iso-range lines,
-                                   for linear sampling of collections looking across the grid axes */
-    int gather_shear;           /* m != 0: the grid backprojection runs on a sheared lattice with warp
-                                   lanes along ey + m ex (collections looking across the grid axes) */
+                                   for linear sampling of collections looking along a grid diagonal;
+                                   0: the plain tile layout */
+    int gather_shear;           /* m = +-1 or +-2: the grid backprojection runs on a sheared lattice
+                                   with warp lanes along ey + m ex (linear sampling of collections
+                                   looking near a diagonal or at ~63 / ~117 degrees to x, where the
+                                   plain lanes' bins change fast); 0: the plain tile layout */
     int scatter_ring_half;      /* > 0: the grid forward scatter keeps ring windows of strip_window
                                    slots per pulse holding a tile's bins within this many of its base
                                    (split bins with tiles too wide for strip windows, e.g. upsample 128) */
